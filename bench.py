@@ -1,0 +1,328 @@
+"""Benchmark of the colour-gradient D3Q19 two-phase step on GB300.
+
+Workload (the precision-form two-phase configuration): 256^3 periodic box,
+solid = union of radius-10 spheres (seeded centres) down to porosity 0.35,
+red saturation 0.5 in random 8^3 blobs, tau_red 0.8 / tau_blue 1.5 (TRT,
+magic 3/16), surface tension 1e-3, recolouring beta 0.7, contact angle 30
+degrees (wetting colour cos 30), body force 1e-6 along x.  The reference
+ships no benchmark geometry; seeded synthetic inputs with these sizes stand
+in for it.
+
+A step is one full lattice update (one launch of the fused step kernel).
+`value` is MLUPS (fluid-node updates per second, all ranks) of the headline
+precision (FP16 deviation storage, FP32 arithmetic) with the state resident
+in HBM; `e2e` is the same metric through the C ABI with host buffers (state
+uploaded from pinned host memory, `itw` steps, observables and state read
+back, every e2e step).  FP64 (plain) and FP32 legs run on the same box.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic bytes per fluid-node update: 2 components x 19 populations x
+# (1 read + 1 write) x storage size + the per-node density field (1 write +
+# 1 read per component)
+ALGO_BYTES = {"f64": 640, "f32": 320, "f16": 168, "bf16": 168}
+PREC_ID = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
+
+
+def workload_config(size: int):
+    tau_r, tau_b = 0.8, 1.5
+    return {
+        "workload": f"two-phase colour-gradient D3Q19, {size}^3 sphere pack (r=10, porosity 0.35), "
+                    f"S_r0=0.5 in 8^3 blobs",
+        "size": size, "radius": 10, "porosity": 0.35, "seed": 20240531, "blob": 8, "red_fraction": 0.5,
+        "tau_red": tau_r, "tau_blue": tau_b, "vir": (tau_r - 0.5) / 3.0, "vib": (tau_b - 0.5) / 3.0,
+        "sig": 1e-3, "B": 0.7, "wet": math.cos(math.radians(30.0)), "bf": 1e-6,
+    }
+
+
+def make_workload(cfg):
+    from porescale_gb300 import geometry
+    from porescale_gb300.lattice import make_params
+    n = cfg["size"]
+    ind = geometry.sphere_pack(n, cfg["porosity"], cfg["radius"], cfg["seed"])
+    col = geometry.blob_colours(ind, cfg["red_fraction"], cfg["blob"], cfg["seed"] + 1)
+    fr, fb = geometry.colour_state(ind, col)
+    p = make_params(B=cfg["B"], sig=cfg["sig"], vir=cfg["vir"], vib=cfg["vib"], wet=cfg["wet"],
+                    bfr=(cfg["bf"], 0, 0), bfb=(cfg["bf"], 0, 0))
+    return ind, p, fr, fb
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(prec: str, nl: int):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary
+    (scaled to this workload's fluid-node count), or None."""
+    path = os.path.join(ROOT, "profiles", "lbm_step_dram.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    e = d.get(prec)
+    if not e:
+        return None
+    return float(e["dram_bytes_per_fluid_node"]) * nl
+
+
+def time_steps(L, steps, warmup, torch):
+    """Device time of `steps` step launches on the lattice's stream (CUDA events)."""
+    stream = torch.cuda.ExternalStream(L.stream)
+    L.step(warmup)
+    L.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    L.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0
+
+
+def cpu_oracle_mlups(ind, p, fr, fb, threads: int, budget_s: float):
+    """Times the CPU restatement (OpenMP, `threads` threads) on the workload:
+    whole-lattice steps until `budget_s` seconds are used."""
+    import oracle
+    o = oracle.OracleLattice(p, ind)
+    o.set_state(fr, fb)
+    t = time.perf_counter()
+    o.run(1, threads)
+    one = time.perf_counter() - t
+    n = max(1, int(budget_s / max(one, 1e-6)))
+    t = time.perf_counter()
+    o.run(n, threads)
+    dt = time.perf_counter() - t
+    nl = o.nl
+    o.close()
+    return nl * n / dt / 1e6, n, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--prec", default="f16", choices=list(PREC_ID))
+    ap.add_argument("--itw", type=int, default=100, help="steps per e2e step (check_state cadence)")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-legs", action="store_true", help="skip the FP64/FP32 comparison legs")
+    ap.add_argument("--accuracy-steps", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    cfg = workload_config(args.size)
+    metric = "D3Q19 two-phase MLUPS"
+
+    if args.impl == "reference":
+        # the reference is Fortran and no Fortran compiler exists here or on
+        # the GPU machine: its CPU path is timed through the C restatement
+        if rank != 0:
+            return
+        from porescale_gb300 import _build
+        _build.build_oracle()
+        ind, p, fr, fb = make_workload(cfg)
+        threads = os.cpu_count() or 1
+        import oracle
+        o = oracle.OracleLattice(p, ind)
+        o.set_state(fr, fb)
+        o.run(args.warmup, threads)
+        t = time.perf_counter()
+        o.run(args.steps, threads)
+        dt = time.perf_counter() - t
+        v = o.nl * args.steps / dt / 1e6
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "MLUPS", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {k: cfg[k] for k in ("workload", "size", "seed")},
+                "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
+                                 "sample": f"{args.steps} full-lattice steps of the {args.size}^3 workload"},
+                "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from porescale_gb300 import _build
+    _build.build_all()
+    from porescale_gb300.lattice import Lattice
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local_rank)
+
+    ind, p, fr, fb = make_workload(cfg)
+    peak, peak_kind = load_peaks()
+    res = {}
+    legs = [args.prec] if args.no_legs else [args.prec] + [q for q in ("f64", "f32") if q != args.prec]
+    clocks = None
+    nl = None
+    for q in legs:
+        L = Lattice(p, ind, PREC_ID[q])
+        nl = L.nl
+        L.set_state(fr, fb)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        steps = args.steps if q == args.prec else max(3, args.steps // 5 if q == "f64" else args.steps)
+        sampler = ClockSampler(local_rank) if q == args.prec else None
+        if sampler:
+            sampler.start()
+        t = time_steps(L, steps, args.warmup, torch)
+        if sampler:
+            clocks = sampler.stop()
+        if world > 1:
+            tt = torch.tensor([t], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t = float(tt.item())
+        mlups = nl * steps / t / 1e6 * world
+        launch_s = t / steps
+        achieved = nl * ALGO_BYTES[q] / launch_s / 1e9
+        res[q] = {"mlups": mlups, "ms_per_step": launch_s * 1e3, "steps": steps, "achieved_gbs": achieved,
+                  "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.zchunk]}
+        if q == args.prec:
+            # e2e through the C ABI with host buffers (pinned)
+            hfr = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
+            hfb = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
+            hfr[:] = fr
+            hfb[:] = fb
+            ofr = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
+            ofb = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
+            L.set_state(hfr, hfb)
+            L.step(args.itw)
+            L.observables()
+            L.get_state((ofr, ofb))
+            if world > 1:
+                torch.distributed.barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                L.set_state(hfr, hfb)
+                L.step(args.itw)
+                obs = L.observables()
+                L.get_state((ofr, ofb))
+            te = time.perf_counter() - t0
+            if world > 1:
+                tt = torch.tensor([te], device="cuda")
+                torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+                te = float(tt.item())
+            res["e2e"] = {"value": nl * args.itw * args.e2e_steps / te / 1e6 * world, "unit": "MLUPS",
+                          "h2d_bytes_per_step": 2 * 19 * nl * 8, "d2h_bytes_per_step": 2 * 19 * nl * 8 + 8 * 40,
+                          "steps_per_e2e_step": args.itw, "e2e_steps": args.e2e_steps,
+                          "permr": obs.permr, "permb": obs.permb}
+        L.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, dt = cpu_oracle_mlups(ind, p, fr, fb, threads, args.cpu_budget)
+        cpu = {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"{n} full-lattice steps of the {args.size}^3 workload ({dt:.1f} s, FP64 C restatement)"}
+
+    h = res[args.prec]
+    traffic = load_traffic(args.prec, nl)
+    line = {
+        "metric": metric, "value": h["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": h["steps"],
+        "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.prec, "data": "synthetic",
+        "config": {"workload": cfg["workload"], "precision": args.prec, "fluid_nodes": nl, "size": args.size,
+                   "seed": cfg["seed"], "l2": "state > L2 (no flush needed)", "tile": h["tile"]},
+        "roofline": {"bound": "hbm", "achieved": h["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": h["frac"], "traffic": traffic, "peak_kind": peak_kind,
+                     "algo_bytes_per_node": ALGO_BYTES[args.prec]},
+        "e2e": res.get("e2e"),
+        "cpu_baseline": cpu,
+        "gpu_launches": h["steps"],
+        "clocks": clocks,
+        "legs": {q: res[q] for q in legs},
+    }
+    if "f64" in res:
+        line["mixed_vs_f64"] = h["mlups"] / res["f64"]["mlups"]
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+"""ctypes wrapper of the CPU FP64 oracle (libps_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline leg, never by the porescale_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libps_oracle.so")
+
+
+class OrLbmParams(C.Structure):
+    _fields_ = [("cr2", C.c_double), ("rr0", C.c_double), ("rb0", C.c_double), ("B", C.c_double),
+                ("sig", C.c_double), ("vir", C.c_double), ("vib", C.c_double), ("wet", C.c_double),
+                ("ee", C.c_double), ("dt", C.c_double), ("bfr", C.c_double * 3), ("bfb", C.c_double * 3),
+                ("idir", C.c_int32), ("iipore", C.c_int32)]
+
+
+_lib = None
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int32)
+_LP = C.POINTER(C.c_int64)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from porescale_gb300 import _build
+            _build.build_oracle()
+        L = C.CDLL(LIB_PATH)
+        sig = {
+            "or_lbm_create": (C.c_void_p, [C.POINTER(OrLbmParams), _IP, C.c_int, C.c_int, C.c_int]),
+            "or_lbm_destroy": (None, [C.c_void_p]),
+            "or_lbm_sizes": (None, [C.c_void_p, _LP]),
+            "or_lbm_tables": (None, [C.c_void_p, _IP, _IP, _IP, _IP, _IP, _IP]),
+            "or_lbm_init_random": (None, [C.c_void_p, C.c_double]),
+            "or_lbm_set_state": (None, [C.c_void_p, _DP, _DP]),
+            "or_lbm_get_state": (None, [C.c_void_p, _DP, _DP]),
+            "or_lbm_fields": (None, [C.c_void_p, _DP, _DP, _DP]),
+            "or_lbm_run": (None, [C.c_void_p, C.c_int, C.c_int]),
+            "or_lbm_observables": (None, [C.c_void_p, _DP]),
+            "or_collision": (None, [C.c_double, C.c_double, C.c_double, _DP, _DP, C.c_double, _DP, _DP, _DP,
+                                    C.c_double, C.c_double, C.c_double]),
+            "or_collmatr_trt": (None, [C.c_double, _DP]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_DP)
+
+
+def _i(a):
+    return a.ctypes.data_as(_IP)
+
+
+OBS_NAMES = ["tmr", "tmb", "tm", "Cpr", "Cpb", "nr", "nb", "Qr0", "Qr1", "Qr2", "Qb0", "Qb1", "Qb2", "um0", "um1",
+             "um2", "umr0", "umr1", "umr2", "umb0", "umb1", "umb2", "tfr0", "tfr1", "tfr2", "tfb0", "tfb1", "tfb2",
+             "bmt0", "bmt1", "bmt2", "rmt0", "rmt1", "rmt2", "isneg", "nneg_rr", "nneg_rb", "permr", "permb",
+             "nr_cf", "nb_cf"]
+
+
+class OracleLattice:
+    """FP64 CPU restatement of the reference LBM (see ps_oracle.h)."""
+
+    def __init__(self, params, ind: np.ndarray):
+        p = OrLbmParams()
+        for name, _ in OrLbmParams._fields_:
+            v = getattr(params, name)
+            if name in ("bfr", "bfb"):
+                for i in range(3):
+                    getattr(p, name)[i] = v[i]
+            else:
+                setattr(p, name, v)
+        ind = np.ascontiguousarray(ind, np.int32)
+        nz, ny, nx = ind.shape
+        self.shape = (nz, ny, nx)
+        self._h = C.c_void_p(lib().or_lbm_create(C.byref(p), _i(ind), nx, ny, nz))
+        s = np.zeros(6, np.int64)
+        lib().or_lbm_sizes(self._h, s.ctypes.data_as(_LP))
+        self.nl, self.nps, self.npb2, self.npb4, self.ns, self.n_overflow = (int(v) for v in s)
+
+    def close(self):
+        if self._h:
+            lib().or_lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tables(self):
+        nz, ny, nx = self.shape
+        icor = np.zeros((self.nl, 3), np.int32)
+        ips = np.zeros((self.nps, 3), np.int32)
+        ipb2 = np.zeros((self.npb2, 4), np.int32)
+        ipb4 = np.zeros((self.npb4, 6), np.int32)
+        mijk = np.zeros((nz, ny, nx), np.int32)
+        mijks = np.zeros((nz, ny, nx), np.int32)
+        lib().or_lbm_tables(self._h, _i(icor), _i(ips), _i(ipb2), _i(ipb4), _i(mijk), _i(mijks))
+        return icor, ips, ipb2, ipb4, mijk, mijks
+
+    def init_random(self, sat):
+        lib().or_lbm_init_random(self._h, sat)
+
+    def set_state(self, fr, fb):
+        fr = np.ascontiguousarray(fr, np.float64)
+        fb = np.ascontiguousarray(fb, np.float64)
+        lib().or_lbm_set_state(self._h, _d(fr), _d(fb))
+
+    def get_state(self):
+        fr, fb = np.empty((self.nl, 19)), np.empty((self.nl, 19))
+        lib().or_lbm_get_state(self._h, _d(fr), _d(fb))
+        return fr, fb
+
+    def fields(self):
+        rr, rb, cf = np.empty(self.nl), np.empty(self.nl), np.empty(self.nl)
+        lib().or_lbm_fields(self._h, _d(rr), _d(rb), _d(cf))
+        return rr, rb, cf
+
+    def run(self, nsteps, nthreads=1):
+        lib().or_lbm_run(self._h, int(nsteps), int(nthreads))
+
+    def observables(self) -> dict:
+        out = np.zeros(41)
+        lib().or_lbm_observables(self._h, _d(out))
+        return dict(zip(OBS_NAMES, out.tolist()))

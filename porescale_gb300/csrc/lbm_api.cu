@@ -1,0 +1,763 @@
+// lbm_api.cu -- C ABI of the colour-gradient lattice (include/porescale.h).
+//
+// Host work done once per lattice (ps_lbm_create): the fluid list and the
+// link classification of S1:1026-1340, turned into a per-voxel link mask for
+// the pull kernels; the collision constants of S1:1355-1382 and
+// S1:3411-3431.  Everything per step runs on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "lbm_launch.h"
+#include "ps_common.h"
+
+namespace ps {
+
+std::string& last_error()
+{
+  static thread_local std::string s;
+  return s;
+}
+
+namespace {
+
+// D3Q19 in reference order, host copy
+const int kC[19][3] = {{0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},  {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
+                       {1, 1, 0},  {-1, 1, 0}, {1, -1, 0}, {-1, -1, 0}, {1, 0, 1},  {-1, 0, 1}, {1, 0, -1},
+                       {-1, 0, -1}, {0, 1, 1},  {0, -1, 1}, {0, 1, -1}, {0, -1, -1}};
+
+struct Lattice {
+  ps_lbm_params p{};
+  int nx = 0, ny = 0, nz = 0, prec = 0;
+  long long nvox = 0, nl = 0, nps = 0, npb2 = 0, npb4 = 0, ns = 0;
+  std::vector<int32_t> ind;   // as given
+  std::vector<int32_t> fvox;  // fluid index -> voxel (reference order)
+  std::vector<int32_t> pvox;  // fluid voxels in ascending order (processing order)
+  LbmConst<double> Kd{};
+  LbmConst<float> Kf{};
+  // device
+  cudaStream_t stream = nullptr;
+  uint32_t* d_mask = nullptr;
+  int32_t* d_fid = nullptr;
+  int32_t* d_fvox = nullptr;
+  int32_t* d_pvox = nullptr;
+  void* d_col = nullptr;  // colour field of the step kernels (R per voxel)
+  void* d_pop[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer][component]
+  float* d_rho[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  LbmConst<double>* d_Kd = nullptr;
+  double *d_fr = nullptr, *d_fb = nullptr;                       // state staging (reference layout)
+  double *d_rr = nullptr, *d_rb = nullptr, *d_cf = nullptr, *d_cc = nullptr;  // dense fields
+  double* d_partial = nullptr;
+  double* d_obs = nullptr;
+  int obs_blocks = 0;
+  int cur = 0;           // buffer holding the current state
+  bool have_state = false;
+  int tx = 128, ty = 256, zchunk = 0;  // collide / density block sizes
+  long long dev_bytes = 0;
+
+  GeomDev geom() const
+  {
+    GeomDev g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.nvox = nvox;
+    g.mask = d_mask;
+    g.fid = d_fid;
+    g.fvox = d_fvox;
+    g.pvox = d_pvox;
+    g.nl = nl;
+    return g;
+  }
+  BufDev buf(int b) const
+  {
+    BufDev r;
+    r.pop[0] = d_pop[b][0];
+    r.pop[1] = d_pop[b][1];
+    r.rho[0] = d_rho[b][0];
+    r.rho[1] = d_rho[b][1];
+    return r;
+  }
+  LbmLaunchArgs args(int src, int dst) const
+  {
+    LbmLaunchArgs a;
+    a.K = prec == 0 ? (const void*)&Kd : (const void*)&Kf;
+    a.Kd_dev = d_Kd;
+    a.G = geom();
+    a.src = buf(src);
+    a.dst = buf(dst);
+    a.cc = d_col;
+    a.stream = stream;
+    return a;
+  }
+  size_t elem() const { return prec == 0 ? 8 : (prec == 1 ? 4 : 2); }
+};
+
+template <typename T>
+int dalloc(Lattice* L, T** p, size_t bytes)
+{
+  cudaError_t e = cudaMalloc((void**)p, bytes > 0 ? bytes : 16);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  L->dev_bytes += (long long)bytes;
+  return PS_OK;
+}
+
+void free_lattice(Lattice* L)
+{
+  if (!L) return;
+  cudaFree(L->d_mask);
+  cudaFree(L->d_fid);
+  cudaFree(L->d_fvox);
+  cudaFree(L->d_pvox);
+  cudaFree(L->d_col);
+  for (int b = 0; b < 2; b++)
+    for (int k = 0; k < 2; k++) {
+      cudaFree(L->d_pop[b][k]);
+      cudaFree(L->d_rho[b][k]);
+    }
+  cudaFree(L->d_Kd);
+  cudaFree(L->d_fr);
+  cudaFree(L->d_fb);
+  cudaFree(L->d_rr);
+  cudaFree(L->d_rb);
+  cudaFree(L->d_cf);
+  cudaFree(L->d_cc);
+  cudaFree(L->d_partial);
+  cudaFree(L->d_obs);
+  if (L->stream) cudaStreamDestroy(L->stream);
+  delete L;
+}
+
+// S1:1355-1382 and S1:3411-3431: collision constants in FP64
+void make_constants(Lattice* L)
+{
+  const ps_lbm_params& p = L->p;
+  LbmConst<double>& K = L->Kd;
+  K.c1d6 = 1.0 / 6.0;
+  K.c1d12 = 1.0 / 12.0;
+  K.c5d399 = 5.0 / 399.0;
+  K.c19d399 = 19.0 / 399.0;
+  K.c11d2394 = 11.0 / 2394.0;
+  K.c1d63 = 1.0 / 63.0;
+  K.c1d18 = 1.0 / 18.0;
+  K.c1d36 = 1.0 / 36.0;
+  K.c4d1197 = 4.0 / 1197.0;
+  K.c1d252 = 1.0 / 252.0;
+  K.c1d72 = 1.0 / 72.0;
+  K.c1d24 = 1.0 / 24.0;
+  K.cn = 1.0 / std::sqrt(2.0);
+  const double dt = p.dt;
+  K.dt = dt;
+  K.dti = 1.0 / dt;
+  K.dt2 = dt * dt;
+  const double cb2 = p.rr0 * p.cr2 / p.rb0;
+  K.cs2[0] = p.cr2;
+  K.cs2[1] = cb2;
+  const double c2[2] = {p.cr2, cb2};
+  for (int k = 0; k < 2; k++) {
+    K.t[k][0] = 1.0 - 2.0 * c2[k] * dt * dt;
+    K.t[k][1] = c2[k] * dt * dt * K.c1d6;
+    K.t[k][2] = c2[k] * dt * dt * K.c1d12;
+  }
+  const double vis[2] = {p.vir, p.vib};
+  const double* bfs[2] = {p.bfr, p.bfb};
+  for (int k = 0; k < 2; k++) {
+    const double sv = 1.0 / (3.0 * vis[k] * dt + 0.5);
+    const double sq = 8.0 * (2.0 - sv) / (8.0 - sv);
+    // TRT rates in the d'Humieres moment order (collmatrTRT)
+    const double S[19] = {0.0, sv, sv, 0.0, sq, 0.0, sq, 0.0, sq, sv, sv, sv, sv, sv, sv, sv, sq, sq, sq};
+    for (int i = 0; i < 19; i++) K.S[k][i] = S[i];
+    for (int d = 0; d < 3; d++) K.bf[k][d] = bfs[k][d];
+    for (int i = 0; i < 19; i++) {
+      const double rk = i == 0 ? 1.0 : (i < 7 ? K.c1d6 : K.c1d12);
+      const double cdotf = (double)kC[i][0] * bfs[k][0] + (double)kC[i][1] * bfs[k][1] + (double)kC[i][2] * bfs[k][2];
+      K.Fp[k][i] = rk * cdotf * K.dt2;
+    }
+  }
+  K.B = p.B;
+  K.sig = 0.03125 * p.sig;
+  K.wet = p.wet;
+  K.ee = p.ee;
+  // FP32 copy for the low-precision lattices
+  LbmConst<float>& F = L->Kf;
+  const double* src = reinterpret_cast<const double*>(&K);
+  float* dstf = reinterpret_cast<float*>(&F);
+  static_assert(sizeof(LbmConst<double>) == 2 * sizeof(LbmConst<float>), "layout");
+  for (size_t i = 0; i < sizeof(LbmConst<double>) / sizeof(double); i++) dstf[i] = (float)src[i];
+}
+
+inline int wrapc(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
+
+// Fluid list (S1:1036-1072, i outer, k inner), link mask and link counts
+// (S1:1077-1134).  A diagonal link streams only when its target and both
+// axis-intermediate voxels are fluid.
+void build_geometry(Lattice* L, std::vector<uint32_t>& mask, std::vector<int32_t>& fid)
+{
+  const int nx = L->nx, ny = L->ny, nz = L->nz;
+  const long long nv = L->nvox;
+  const int32_t pore = L->p.iipore;
+  auto V = [&](int x, int y, int z) -> long long { return x + (long long)nx * (y + (long long)ny * z); };
+  fid.assign(nv, -1);
+  L->fvox.clear();
+  for (int x = 0; x < nx; x++)
+    for (int y = 0; y < ny; y++)
+      for (int z = 0; z < nz; z++) {
+        const long long v = V(x, y, z);
+        if (L->ind[v] == pore) {
+          fid[v] = (int32_t)L->fvox.size();
+          L->fvox.push_back((int32_t)v);
+        }
+      }
+  L->nl = (long long)L->fvox.size();
+  L->pvox = L->fvox;
+  std::sort(L->pvox.begin(), L->pvox.end());
+  mask.assign(nv, 0u);
+  long long nps = 0, npb2 = 0, npb4 = 0;
+  auto fl = [&](int x, int y, int z) { return fid[V(wrapc(x, nx), wrapc(y, ny), wrapc(z, nz))] >= 0; };
+  for (long long i = 0; i < L->nl; i++) {
+    const long long v = L->fvox[i];
+    const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long long)nx * ny));
+    uint32_t m = kFluidBit;
+    // incoming link d is open when the outgoing link d of x - c_d streams;
+    // by symmetry that is the outgoing link opp(d) of x itself
+    for (int d = 1; d < 19; d++) {
+      const int* c = kC[d];
+      bool stream = fl(x + c[0], y + c[1], z + c[2]);
+      if (stream && d >= 7) stream = fl(x + c[0], y, z) && fl(x, y + c[1], z) && fl(x, y, z + c[2]);
+      if (stream)
+        nps++;
+      else if (d < 7)
+        npb4++;
+      else
+        npb2++;
+      // outgoing d of x is incoming opp(d)... recorded below on the target
+    }
+    for (int d = 1; d < 19; d++) {
+      const int* c = kC[d];
+      const int sx = x - c[0], sy = y - c[1], sz = z - c[2];
+      bool open = fl(sx, sy, sz);
+      if (open && d >= 7) open = fl(sx + c[0], sy, sz) && fl(sx, sy + c[1], sz) && fl(sx, sy, sz + c[2]);
+      if (open) m |= 1u << (d - 1);
+    }
+    mask[v] = m;
+  }
+  L->nps = nps;
+  L->npb2 = npb2;
+  L->npb4 = npb4;
+}
+
+// LSM node numbering by corner dilation of the solid voxels with periodic
+// stitching (S1:541-602, 647-660): returns mijks(nx,ny,nz), 1-based or 0.
+std::vector<int32_t> lsm_node_numbers(const Lattice* L, long long* ns_out)
+{
+  const int nx = L->nx, ny = L->ny, nz = L->nz;
+  // a voxel corner (i,j,k) is a solid node when any of the up to 8 voxels
+  // sharing it (periodically) is solid (ind == 0 after the reset of values
+  // > 1 to pore)
+  std::vector<int32_t> num((size_t)L->nvox, 0);
+  long long ns = 0;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        bool solid = false;
+        for (int dk = -1; dk <= 0 && !solid; dk++)
+          for (int dj = -1; dj <= 0 && !solid; dj++)
+            for (int di = -1; di <= 0 && !solid; di++) {
+              const long long v = wrapc(i + di, nx) + (long long)nx * (wrapc(j + dj, ny) + (long long)ny * wrapc(k + dk, nz));
+              if (L->ind[v] == 0) solid = true;
+            }
+        if (solid) num[i + (long long)nx * (j + (long long)ny * k)] = (int32_t)(++ns);
+      }
+  if (ns_out) *ns_out = ns;
+  return num;
+}
+
+int ensure_staging(Lattice* L)
+{
+  if (!L->d_fr) {
+    const size_t b = sizeof(double) * 19 * (size_t)std::max(L->nl, 1LL);
+    if (int r = dalloc(L, &L->d_fr, b)) return r;
+    if (int r = dalloc(L, &L->d_fb, b)) return r;
+  }
+  return PS_OK;
+}
+
+int ensure_fields(Lattice* L)
+{
+  if (!L->d_cc) {
+    const size_t b = sizeof(double) * (size_t)L->nvox;
+    if (int r = dalloc(L, &L->d_rr, b)) return r;
+    if (int r = dalloc(L, &L->d_rb, b)) return r;
+    if (int r = dalloc(L, &L->d_cf, b)) return r;
+    if (int r = dalloc(L, &L->d_cc, b)) return r;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    L->obs_blocks = std::max(1, std::min<int>(sms * 4, (int)((L->nl + 255) / 256)));
+    if (int r = dalloc(L, &L->d_partial, sizeof(double) * kObsN * L->obs_blocks)) return r;
+    if (int r = dalloc(L, &L->d_obs, sizeof(double) * kObsN)) return r;
+  }
+  return PS_OK;
+}
+
+#define PREC_DISPATCH(fn, prec, ...)                                        \
+  ((prec) == 0   ? fn##_0(__VA_ARGS__)                                      \
+   : (prec) == 1 ? fn##_1(__VA_ARGS__)                                      \
+   : (prec) == 2 ? fn##_2(__VA_ARGS__)                                      \
+                 : fn##_3(__VA_ARGS__))
+
+Lattice* as_lattice(void* h) { return static_cast<Lattice*>(h); }
+
+int launch_steps(Lattice* L, int n)
+{
+  for (int s = 0; s < n; s++) {
+    LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
+    cudaError_t e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, 0, a);
+    if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
+    L->cur = 1 - L->cur;
+  }
+  return PS_OK;
+}
+
+}  // namespace
+
+// dispatchers declared in lbm_launch.h
+cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunchArgs& a)
+{
+  return PREC_DISPATCH(lbm_step_launch, prec, tx, ty, zchunk, a);
+}
+int lbm_tiles(int prec, TileCfg* out, int cap) { return PREC_DISPATCH(lbm_tiles, prec, out, cap); }
+size_t lbm_step_smem(int prec, int tx, int ty) { return PREC_DISPATCH(lbm_step_smem, prec, tx, ty); }
+
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" {
+
+int ps_last_error(char* buf, int32_t len)
+{
+  if (!buf || len <= 0) return PS_ERR_ARG;
+  const std::string& s = last_error();
+  const size_t n = std::min<size_t>(s.size(), (size_t)len - 1);
+  memcpy(buf, s.data(), n);
+  buf[n] = '\0';
+  return PS_OK;
+}
+
+const char* ps_version(void) { return "porescale_gb300 0.1 sm_103a"; }
+
+int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_t ny, int32_t nz, int32_t precision,
+                  void** handle)
+{
+  if (!p || !ind || !handle) return fail(PS_ERR_ARG, "ps_lbm_create: null argument");
+  *handle = nullptr;
+  if (nx < 1 || ny < 1 || nz < 1) return fail(PS_ERR_ARG, "ps_lbm_create: bad box %d x %d x %d", nx, ny, nz);
+  if ((long long)nx * ny * nz > (1LL << 31) - 1) return fail(PS_ERR_ARG, "ps_lbm_create: box too large for int32 voxel ids");
+  if (precision < 0 || precision > 3) return fail(PS_ERR_ARG, "ps_lbm_create: precision %d not in 0..3", precision);
+  if (!(p->dt > 0.0) || !(p->rb0 != 0.0)) return fail(PS_ERR_ARG, "ps_lbm_create: dt must be > 0 and rb0 != 0");
+  if (p->idir < 1 || p->idir > 3) return fail(PS_ERR_ARG, "ps_lbm_create: idir %d not in 1..3", p->idir);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PS_ERR_NODEVICE, "ps_lbm_create: no CUDA device");
+  std::unique_ptr<Lattice, void (*)(Lattice*)> L(new Lattice, free_lattice);
+  L->p = *p;
+  L->nx = nx;
+  L->ny = ny;
+  L->nz = nz;
+  L->prec = precision;
+  L->nvox = (long long)nx * ny * nz;
+  L->ind.assign(ind, ind + L->nvox);
+  std::vector<uint32_t> mask;
+  std::vector<int32_t> fid;
+  build_geometry(L.get(), mask, fid);
+  lsm_node_numbers(L.get(), &L->ns);
+  make_constants(L.get());
+  PS_CUDA(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+  const size_t nv = (size_t)L->nvox;
+  if (int r = dalloc(L.get(), &L->d_mask, sizeof(uint32_t) * nv)) return r;
+  if (int r = dalloc(L.get(), &L->d_fid, sizeof(int32_t) * nv)) return r;
+  if (int r = dalloc(L.get(), &L->d_fvox, sizeof(int32_t) * std::max<size_t>(1, L->fvox.size()))) return r;
+  PS_CUDA(cudaMemcpyAsync(L->d_mask, mask.data(), sizeof(uint32_t) * nv, cudaMemcpyHostToDevice, L->stream));
+  PS_CUDA(cudaMemcpyAsync(L->d_fid, fid.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice, L->stream));
+  if (int r = dalloc(L.get(), &L->d_pvox, sizeof(int32_t) * std::max<size_t>(1, L->pvox.size()))) return r;
+  if (!L->fvox.empty()) {
+    PS_CUDA(cudaMemcpyAsync(L->d_fvox, L->fvox.data(), sizeof(int32_t) * L->fvox.size(), cudaMemcpyHostToDevice, L->stream));
+    PS_CUDA(cudaMemcpyAsync(L->d_pvox, L->pvox.data(), sizeof(int32_t) * L->pvox.size(), cudaMemcpyHostToDevice, L->stream));
+  }
+  // colour field: the wetting colour everywhere; fluid voxels are rewritten
+  // by every step before they are read
+  {
+    const size_t cs = precision == 0 ? sizeof(double) : sizeof(float);
+    if (int r = dalloc(L.get(), (char**)&L->d_col, cs * nv)) return r;
+    if (precision == 0) {
+      std::vector<double> w(nv, p->wet);
+      PS_CUDA(cudaMemcpyAsync(L->d_col, w.data(), cs * nv, cudaMemcpyHostToDevice, L->stream));
+      PS_CUDA(cudaStreamSynchronize(L->stream));
+    } else {
+      std::vector<float> w(nv, (float)p->wet);
+      PS_CUDA(cudaMemcpyAsync(L->d_col, w.data(), cs * nv, cudaMemcpyHostToDevice, L->stream));
+      PS_CUDA(cudaStreamSynchronize(L->stream));
+    }
+  }
+  const size_t popb = L->elem() * 19 * nv;
+  for (int b = 0; b < 2; b++)
+    for (int k = 0; k < 2; k++) {
+      if (int r = dalloc(L.get(), &L->d_pop[b][k], popb)) return r;
+      PS_CUDA(cudaMemsetAsync(L->d_pop[b][k], 0, popb, L->stream));
+      if (precision >= 2) {
+        if (int r = dalloc(L.get(), &L->d_rho[b][k], sizeof(float) * nv)) return r;
+        PS_CUDA(cudaMemsetAsync(L->d_rho[b][k], 0, sizeof(float) * nv, L->stream));
+      }
+    }
+  if (int r = dalloc(L.get(), &L->d_Kd, sizeof(LbmConst<double>))) return r;
+  PS_CUDA(cudaMemcpyAsync(L->d_Kd, &L->Kd, sizeof(LbmConst<double>), cudaMemcpyHostToDevice, L->stream));
+  L->tx = 128;
+  L->ty = 256;
+  L->zchunk = 0;
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  *handle = L.release();
+  return PS_OK;
+}
+
+int ps_lbm_destroy(void* h)
+{
+  if (!h) return PS_OK;
+  Lattice* L = as_lattice(h);
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  free_lattice(L);
+  return PS_OK;
+}
+
+int ps_lbm_get_info(void* h, ps_lbm_info* o)
+{
+  if (!h || !o) return fail(PS_ERR_ARG, "ps_lbm_get_info: null argument");
+  Lattice* L = as_lattice(h);
+  memset(o, 0, sizeof *o);
+  o->nl = L->nl;
+  o->nps = L->nps;
+  o->npb2 = L->npb2;
+  o->npb4 = L->npb4;
+  o->ns = L->ns;
+  o->nvox = L->nvox;
+  o->nx = L->nx;
+  o->ny = L->ny;
+  o->nz = L->nz;
+  o->precision = L->prec;
+  o->tile_x = L->tx;
+  o->tile_y = L->ty;
+  o->zchunk = L->zchunk;
+  o->device_bytes = L->dev_bytes;
+  return PS_OK;
+}
+
+int ps_lbm_tables(void* h, int32_t* icor, int32_t* ips, int32_t* ipb2, int32_t* ipb4)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_tables: null handle");
+  Lattice* L = as_lattice(h);
+  const int nx = L->nx, ny = L->ny, nz = L->nz;
+  auto V = [&](int x, int y, int z) -> long long {
+    return wrapc(x, nx) + (long long)nx * (wrapc(y, ny) + (long long)ny * wrapc(z, nz));
+  };
+  std::vector<int32_t> num;  // fluid numbers, 1-based (mijk)
+  num.assign((size_t)L->nvox, 0);
+  for (long long i = 0; i < L->nl; i++) num[L->fvox[i]] = (int32_t)(i + 1);
+  std::vector<int32_t> snum;
+  if (ipb2 || ipb4) snum = lsm_node_numbers(L, nullptr);
+  long long a = 0, b2 = 0, b4 = 0;
+  for (long long i = 0; i < L->nl; i++) {
+    const long long v = L->fvox[i];
+    const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long long)nx * ny));
+    if (icor) {
+      icor[3 * i] = x + 1;
+      icor[3 * i + 1] = y + 1;
+      icor[3 * i + 2] = z + 1;
+    }
+    for (int d = 1; d < 19; d++) {
+      const int* c = kC[d];
+      const int32_t to = num[V(x + c[0], y + c[1], z + c[2])];
+      bool stream = to != 0;
+      if (stream && d >= 7)
+        stream = num[V(x + c[0], y, z)] != 0 && num[V(x, y + c[1], z)] != 0 && num[V(x, y, z + c[2])] != 0;
+      if (stream) {
+        if (ips) {
+          ips[3 * a] = (int32_t)(i + 1);
+          ips[3 * a + 1] = to;
+          ips[3 * a + 2] = d + 1;
+        }
+        a++;
+        continue;
+      }
+      // wall link: reflected direction and the LSM nodes bounding the wall
+      // face (axis links, 4 nodes) or wall edge (diagonal links, 2 nodes);
+      // the offset of the face/edge from the node is (c+1)/2 per component
+      const int off[3] = {(c[0] + 1) / 2, (c[1] + 1) / 2, (c[2] + 1) / 2};
+      const int back = opp(d) + 1;
+      if (d < 7) {
+        if (ipb4) {
+          const int ax = c[0] != 0 ? 0 : (c[1] != 0 ? 1 : 2);
+          const int u = ax == 0 ? 1 : 0, w = ax == 2 ? 1 : 2;  // the two in-plane axes
+          int32_t* r = ipb4 + 6 * b4;
+          r[0] = (int32_t)(i + 1);
+          r[1] = back;
+          int q = 0;
+          for (int s = 0; s < 2; s++)
+            for (int t = 0; t < 2; t++) {
+              int e[3] = {0, 0, 0};
+              e[ax] = off[ax];
+              e[u] = t;
+              e[w] = s;
+              r[2 + q++] = snum[V(x + e[0], y + e[1], z + e[2])];
+            }
+        }
+        b4++;
+      } else {
+        if (ipb2) {
+          const int ax = c[0] == 0 ? 0 : (c[1] == 0 ? 1 : 2);  // edge direction
+          int32_t* r = ipb2 + 4 * b2;
+          r[0] = (int32_t)(i + 1);
+          r[1] = back;
+          for (int s = 0; s < 2; s++) {
+            int e[3] = {off[0], off[1], off[2]};
+            e[ax] = s;
+            r[2 + s] = snum[V(x + e[0], y + e[1], z + e[2])];
+          }
+        }
+        b2++;
+      }
+    }
+  }
+  return PS_OK;
+}
+
+int ps_lbm_set_state(void* h, const double* fr, const double* fb)
+{
+  if (!h || !fr || !fb) return fail(PS_ERR_ARG, "ps_lbm_set_state: null argument");
+  Lattice* L = as_lattice(h);
+  if (int r = ensure_staging(L)) return r;
+  const size_t b = sizeof(double) * 19 * (size_t)L->nl;
+  if (b) {
+    PS_CUDA(cudaMemcpyAsync(L->d_fr, fr, b, cudaMemcpyHostToDevice, L->stream));
+    PS_CUDA(cudaMemcpyAsync(L->d_fb, fb, b, cudaMemcpyHostToDevice, L->stream));
+  }
+  LbmLaunchArgs a = L->args(L->cur, L->cur);
+  cudaError_t e = PREC_DISPATCH(lbm_set_state_launch, L->prec, a, L->d_fr, L->d_fb);
+  if (e != cudaSuccess) return cuda_fail(e, "set_state kernel");
+  L->have_state = true;
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  return PS_OK;
+}
+
+int ps_lbm_get_state(void* h, double* fr, double* fb)
+{
+  if (!h || !fr || !fb) return fail(PS_ERR_ARG, "ps_lbm_get_state: null argument");
+  Lattice* L = as_lattice(h);
+  if (!L->have_state) return fail(PS_ERR_STATE, "ps_lbm_get_state: no state set");
+  if (int r = ensure_staging(L)) return r;
+  LbmLaunchArgs a = L->args(L->cur, L->cur);
+  cudaError_t e = PREC_DISPATCH(lbm_get_state_launch, L->prec, a, L->d_fr, L->d_fb);
+  if (e != cudaSuccess) return cuda_fail(e, "get_state kernel");
+  const size_t b = sizeof(double) * 19 * (size_t)L->nl;
+  if (b) {
+    PS_CUDA(cudaMemcpyAsync(fr, L->d_fr, b, cudaMemcpyDeviceToHost, L->stream));
+    PS_CUDA(cudaMemcpyAsync(fb, L->d_fb, b, cudaMemcpyDeviceToHost, L->stream));
+  }
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  return PS_OK;
+}
+
+int ps_lbm_init_random(void* h, double sat)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_init_random: null handle");
+  Lattice* L = as_lattice(h);
+  // Park-Miller minimal standard generator on doubles (S1:2828-2843)
+  std::vector<double> fr((size_t)19 * L->nl), fb((size_t)19 * L->nl);
+  double seed = 13.081984;
+  const double m31 = 2147483647.0, p31 = 2147483648.0;
+  for (long long i = 0; i < L->nl; i++) {
+    seed = std::fmod(16807.0 * seed, m31);
+    const double red = seed / p31 <= sat ? 0.0 : 1.0;
+    for (int d = 0; d < 19; d++) {
+      fr[19 * i + d] = L->Kd.t[0][wcls(d)] * red * L->p.rr0;
+      fb[19 * i + d] = L->Kd.t[1][wcls(d)] * (1.0 - red) * L->p.rb0;
+    }
+  }
+  return ps_lbm_set_state(h, fr.data(), fb.data());
+}
+
+int ps_lbm_step(void* h, int32_t nsteps)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_step: null handle");
+  if (nsteps < 0) return fail(PS_ERR_ARG, "ps_lbm_step: nsteps < 0");
+  Lattice* L = as_lattice(h);
+  if (!L->have_state) return fail(PS_ERR_STATE, "ps_lbm_step: no state set");
+  return launch_steps(L, nsteps);
+}
+
+int ps_lbm_observables(void* h, ps_lbm_obs* out)
+{
+  if (!h || !out) return fail(PS_ERR_ARG, "ps_lbm_observables: null argument");
+  Lattice* L = as_lattice(h);
+  if (!L->have_state) return fail(PS_ERR_STATE, "ps_lbm_observables: no state set");
+  if (int r = ensure_fields(L)) return r;
+  LbmLaunchArgs a = L->args(L->cur, L->cur);
+  cudaError_t e = PREC_DISPATCH(lbm_fields_launch, L->prec, a, L->d_rr, L->d_rb, L->d_cf, L->d_cc);
+  if (e != cudaSuccess) return cuda_fail(e, "fields kernel");
+  e = PREC_DISPATCH(lbm_obs_launch, L->prec, a, L->d_cc, L->d_partial, L->obs_blocks, L->d_obs);
+  if (e != cudaSuccess) return cuda_fail(e, "observables kernel");
+  double s[kObsN];
+  PS_CUDA(cudaMemcpyAsync(s, L->d_obs, sizeof s, cudaMemcpyDeviceToHost, L->stream));
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  memset(out, 0, sizeof *out);
+  const LbmConst<double>& K = L->Kd;
+  out->tmr = s[0];
+  out->tmb = s[1];
+  out->tm = s[2];
+  out->nr_cf = s[5];
+  out->nb_cf = s[6];
+  out->Cpr = K.cs2[0] * s[3] / s[5];
+  out->Cpb = K.cs2[1] * s[4] / s[6];
+  out->nr = s[7];
+  out->nb = s[8];
+  const double t0 = (double)L->nx * L->ny * L->nz;
+  for (int d = 0; d < 3; d++) {
+    out->Qr[d] = s[9 + d] / t0;
+    out->Qb[d] = s[12 + d] / t0;
+    out->um[d] = s[15 + d] / t0;
+    out->umr[d] = s[18 + d];
+    out->umb[d] = s[21 + d];
+    out->tfr[d] = s[24 + d];
+    out->tfb[d] = s[27 + d];
+    out->bmt[d] = s[30 + d];
+    out->rmt[d] = s[33 + d];
+  }
+  out->isneg = s[36] > 0.0 ? 1 : 0;
+  out->nneg_rr = (int32_t)s[37];
+  out->nneg_rb = (int32_t)s[38];
+  // viscosities re-derived from the relaxation rates (S1:3419-3420)
+  const double vir = K.dti * (1.0 / K.S[0][1] - 0.5) / 3.0, vib = K.dti * (1.0 / K.S[1][1] - 0.5) / 3.0;
+  const int id = L->p.idir - 1;
+  out->permr = out->Qr[id] * vir / L->p.bfr[id];
+  out->permb = out->Qb[id] * vib / L->p.bfb[id];
+  out->sat_r = out->nr / (double)L->nl;
+  out->sat_b = out->nb / (double)L->nl;
+  return PS_OK;
+}
+
+int ps_lbm_fields(void* h, double* rr, double* rb, double* cf)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_fields: null handle");
+  Lattice* L = as_lattice(h);
+  if (!L->have_state) return fail(PS_ERR_STATE, "ps_lbm_fields: no state set");
+  if (int r = ensure_fields(L)) return r;
+  LbmLaunchArgs a = L->args(L->cur, L->cur);
+  cudaError_t e = PREC_DISPATCH(lbm_fields_launch, L->prec, a, L->d_rr, L->d_rb, L->d_cf, L->d_cc);
+  if (e != cudaSuccess) return cuda_fail(e, "fields kernel");
+  std::vector<double> buf((size_t)L->nvox);
+  double* outs[3] = {rr, rb, cf};
+  double* srcs[3] = {L->d_rr, L->d_rb, L->d_cf};
+  for (int q = 0; q < 3; q++) {
+    if (!outs[q]) continue;
+    PS_CUDA(cudaMemcpyAsync(buf.data(), srcs[q], sizeof(double) * L->nvox, cudaMemcpyDeviceToHost, L->stream));
+    PS_CUDA(cudaStreamSynchronize(L->stream));
+    for (long long i = 0; i < L->nl; i++) outs[q][i] = buf[L->fvox[i]];
+  }
+  return PS_OK;
+}
+
+void* ps_lbm_stream(void* h) { return h ? (void*)as_lattice(h)->stream : nullptr; }
+
+int ps_lbm_sync(void* h)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_sync: null handle");
+  PS_CUDA(cudaStreamSynchronize(as_lattice(h)->stream));
+  return PS_OK;
+}
+
+int ps_lbm_set_tile(void* h, int32_t tx, int32_t ty, int32_t zchunk)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_tile: null handle");
+  Lattice* L = as_lattice(h);
+  if (lbm_step_smem(L->prec, tx, ty) == 0)
+    return fail(PS_ERR_ARG, "ps_lbm_set_tile: blocks %d/%d not compiled for precision %d", tx, ty, L->prec);
+  if (zchunk != 0) return fail(PS_ERR_ARG, "ps_lbm_set_tile: zchunk must be 0 (the step kernels do not march in z)");
+  L->tx = tx;
+  L->ty = ty;
+  return PS_OK;
+}
+
+int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, int32_t* zc_out)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_autotune: null handle");
+  Lattice* L = as_lattice(h);
+  if (!L->have_state) return fail(PS_ERR_STATE, "ps_lbm_autotune: no state set");
+  if (steps < 1) steps = 4;
+  // candidates: every compiled tile x a few z-chunk lengths; the state is
+  // advanced an even number of steps per candidate and then restored by
+  // re-running from a saved copy of the current buffer
+  const size_t popb = L->elem() * 19 * (size_t)L->nvox;
+  void* save[2] = {nullptr, nullptr};
+  float* saver[2] = {nullptr, nullptr};
+  for (int k = 0; k < 2; k++) {
+    PS_CUDA(cudaMalloc(&save[k], popb));
+    PS_CUDA(cudaMemcpyAsync(save[k], L->d_pop[L->cur][k], popb, cudaMemcpyDeviceToDevice, L->stream));
+    if (L->prec >= 2) {
+      PS_CUDA(cudaMalloc((void**)&saver[k], sizeof(float) * L->nvox));
+      PS_CUDA(cudaMemcpyAsync(saver[k], L->d_rho[L->cur][k], sizeof(float) * L->nvox, cudaMemcpyDeviceToDevice, L->stream));
+    }
+  }
+  TileCfg tiles[16];
+  const int nt = lbm_tiles(L->prec, tiles, 16);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int btx = L->tx, bty = L->ty, bzc = L->zchunk;
+  const int saved_cur = L->cur;
+  int rc = PS_OK;
+  for (int i = 0; i < nt && rc == PS_OK; i++) {
+    L->tx = tiles[i].tx;
+    L->ty = tiles[i].ty;
+    rc = launch_steps(L, 2);  // warm-up
+    if (rc) break;
+    cudaEventRecord(e0, L->stream);
+    rc = launch_steps(L, steps);
+    cudaEventRecord(e1, L->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rc == PS_OK && ms < best) {
+      best = ms;
+      btx = L->tx;
+      bty = L->ty;
+      bzc = 0;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // restore the state
+  L->cur = saved_cur;
+  for (int k = 0; k < 2; k++) {
+    cudaMemcpyAsync(L->d_pop[L->cur][k], save[k], popb, cudaMemcpyDeviceToDevice, L->stream);
+    if (saver[k]) cudaMemcpyAsync(L->d_rho[L->cur][k], saver[k], sizeof(float) * L->nvox, cudaMemcpyDeviceToDevice, L->stream);
+  }
+  cudaStreamSynchronize(L->stream);
+  for (int k = 0; k < 2; k++) {
+    cudaFree(save[k]);
+    cudaFree(saver[k]);
+  }
+  L->tx = btx;
+  L->ty = bty;
+  L->zchunk = bzc;
+  if (tx_out) *tx_out = btx;
+  if (ty_out) *ty_out = bty;
+  if (zc_out) *zc_out = bzc;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// lbm_launch.h -- host-callable launchers of the LBM kernels, one set per
+// storage precision (implemented in lbm_prec_f64.cu and lbm_prec_lp.cu so
+// that the FP64 kernels can be compiled without FMA contraction).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "lbm_kernels.cuh"
+
+namespace ps {
+
+struct LbmLaunchArgs {
+  const void* K;        // LbmConst<R> of the storage precision (host copy)
+  const LbmConst<double>* Kd_dev;  // FP64 constants in device memory
+  GeomDev G;
+  BufDev src, dst;
+  void* cc;             // colour field (R per voxel) used by the step kernels
+  cudaStream_t stream;
+};
+
+// block sizes compiled for the step kernels: tx = collide kernel, ty =
+// density kernel (threads per CTA)
+struct TileCfg {
+  int tx, ty;
+};
+
+// returns cudaErrorInvalidValue when (tx,ty) is not a compiled block pair
+cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunchArgs& a);
+cudaError_t lbm_fields_launch(int prec, const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc);
+cudaError_t lbm_get_state_launch(int prec, const LbmLaunchArgs& a, double* fr, double* fb);
+cudaError_t lbm_set_state_launch(int prec, const LbmLaunchArgs& a, const double* fr, const double* fb);
+cudaError_t lbm_obs_launch(int prec, const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,
+                           double* out);
+// the compiled tiles of a precision (n returned, at most cap written)
+int lbm_tiles(int prec, TileCfg* out, int cap);
+// smem bytes of the step kernel for a tile (0 if not compiled)
+size_t lbm_step_smem(int prec, int tx, int ty);
+
+// per-precision implementations
+#define PS_DECL_PREC(P)                                                                                     \
+  cudaError_t lbm_step_launch_##P(int tx, int ty, int zchunk, const LbmLaunchArgs& a);                     \
+  cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc); \
+  cudaError_t lbm_get_state_launch_##P(const LbmLaunchArgs& a, double* fr, double* fb);                    \
+  cudaError_t lbm_set_state_launch_##P(const LbmLaunchArgs& a, const double* fr, const double* fb);        \
+  cudaError_t lbm_obs_launch_##P(const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,   \
+                                 double* out);                                                              \
+  int lbm_tiles_##P(TileCfg* out, int cap);                                                                 \
+  size_t lbm_step_smem_##P(int tx, int ty);
+PS_DECL_PREC(0)
+PS_DECL_PREC(1)
+PS_DECL_PREC(2)
+PS_DECL_PREC(3)
+#undef PS_DECL_PREC
+
+}  // namespace ps

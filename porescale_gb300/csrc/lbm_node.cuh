@@ -1,0 +1,309 @@
+// lbm_node.cuh -- per-node arithmetic of the colour-gradient D3Q19 step.
+//
+// Three pieces, each a function of one lattice node:
+//   mrt_collide   the forced MRT collision with TRT rates  (S1:2407-2620)
+//   csf_force     the CSF surface-tension force and unit colour normal from
+//                 the 3x3x3 colour neighbourhood            (S1:2626-2796)
+//   node_update   branch selection (bulk red / bulk blue / interface), the
+//                 interface collision and Latva-Kokko recolouring
+//                                                           (S1:3663-3819)
+//
+// The operation order of every floating-point expression follows the
+// reference source, so that the FP64 instantiation compiled without FMA
+// contraction (--fmad=false) reproduces the reference arithmetic bit for bit.
+// The FP32 instantiation uses the same code with FMA contraction enabled.
+//
+// Directions are numbered as in the reference's `velocities19` file (0-based
+// here): 0 rest, 1..6 axis (+x,-x,+y,-y,+z,-z), 7..18 face diagonals.
+#pragma once
+
+#ifdef __CUDACC__
+#define PS_HD __host__ __device__ __forceinline__
+#else
+#define PS_HD inline
+#endif
+
+#include <math.h>
+
+namespace ps {
+
+template <typename R>
+struct LbmConst {
+  R c1d6, c1d12, c5d399, c19d399, c11d2394, c1d63, c1d18, c1d36, c4d1197, c1d252, c1d72, c1d24;
+  R cn;  // 1/sqrt(2): cosine factor of the diagonal directions
+  R dt, dti, dt2;
+  R t[2][3];     // lattice weights (rest, axis, diagonal) of red / blue (S1:1368-1376)
+  R cs2[2];      // cr2, cb2
+  R S[2][19];    // relaxation vectors Sr, Sb (collmatrTRT)
+  R Fp[2][19];   // body-force projections Fpr, Fpb (S1:3428-3430)
+  R bf[2][3];    // body forces bfr, bfb
+  R B, sig, wet, ee;  // recolouring beta, sig/32, wetting colour, bulk threshold
+};
+
+// Forced MRT collision of one node.  f: 19 populations (f[0] is updated in
+// place with the post-collision rest population); pcf[1..18] receives the
+// post-collision moving populations.
+template <typename R>
+PS_HD void mrt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r, const R* bf,
+                       const R* Fp, const R* S)
+{
+  const R dt = K.dt, dti = K.dti, dt2 = K.dt2;
+  // momentum
+  R jx = (f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14]) * dti;
+  R jy = (f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18]) * dti;
+  R jz = (f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18]) * dti;
+  // force-shifted velocity
+  const R rinv = R(1) / r;
+  const R ux = (jx + bf[0] * R(0.5) * dt) * rinv;
+  const R uy = (jy + bf[1] * R(0.5) * dt) * rinv;
+  const R uz = (jz + bf[2] * R(0.5) * dt) * rinv;
+  const R uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+  const R usq = (uxx + uyy + uzz) * R(0.5);
+
+  // second-order equilibrium with sound-speed dependent weights
+  R fl[19];
+  {
+    const R rq = r * R(0.25) * dt2;
+    const R e1 = (t2 - usq * K.c1d6 * dt2) * r;
+    const R ax = e1 + rq * uxx, ay = e1 + rq * uyy, az = e1 + rq * uzz;
+    const R sx = jx * K.c1d6 * dt, sy = jy * K.c1d6 * dt, sz = jz * K.c1d6 * dt;
+    fl[0] = f[0] - r * (t1 - usq * dt2);
+    fl[1] = f[1] - (ax + sx);
+    fl[2] = f[2] - (ax - sx);
+    fl[3] = f[3] - (ay + sy);
+    fl[4] = f[4] - (ay - sy);
+    fl[5] = f[5] - (az + sz);
+    fl[6] = f[6] - (az - sz);
+    const R ro = r * R(0.125) * dt2;
+    const R e2 = (t3 - usq * K.c1d12 * dt2) * r;
+    // pairs (a,b): j_a +/- j_b terms and u_a +/- u_b quadratic terms
+    const R pxy = (jx + jy) * K.c1d12 * dt, mxy = (jx - jy) * K.c1d12 * dt;
+    const R pxz = (jx + jz) * K.c1d12 * dt, mxz = (jx - jz) * K.c1d12 * dt;
+    const R pyz = (jy + jz) * K.c1d12 * dt, myz = (jy - jz) * K.c1d12 * dt;
+    const R qpxy = ro * (ux + uy) * (ux + uy), qmxy = ro * (ux - uy) * (ux - uy);
+    const R qpxz = ro * (ux + uz) * (ux + uz), qmxz = ro * (ux - uz) * (ux - uz);
+    const R qpyz = ro * (uy + uz) * (uy + uz), qmyz = ro * (uy - uz) * (uy - uz);
+    fl[7] = f[7] - (e2 + pxy + qpxy);
+    fl[10] = f[10] - (e2 - pxy + qpxy);
+    fl[8] = f[8] - (e2 - mxy + qmxy);
+    fl[9] = f[9] - (e2 + mxy + qmxy);
+    fl[11] = f[11] - (e2 + pxz + qpxz);
+    fl[14] = f[14] - (e2 - pxz + qpxz);
+    fl[13] = f[13] - (e2 + mxz + qmxz);
+    fl[12] = f[12] - (e2 - mxz + qmxz);
+    fl[15] = f[15] - (e2 + pyz + qpyz);
+    fl[18] = f[18] - (e2 - pyz + qpyz);
+    fl[17] = f[17] - (e2 + myz + qmyz);
+    fl[16] = f[16] - (e2 - myz + qmyz);
+  }
+
+  // non-conserved moments of the non-equilibrium part (d'Humieres basis),
+  // each already multiplied by its relaxation rate
+  const R a6 = fl[1] + fl[2] + fl[3] + fl[4] + fl[5] + fl[6];
+  const R a12 = fl[7] + fl[8] + fl[9] + fl[10] + fl[11] + fl[12] + fl[13] + fl[14] + fl[15] + fl[16] +
+                fl[17] + fl[18];
+  const R m_e = (-(R(30) * fl[0]) - R(11) * a6 + R(8) * a12) * S[1];
+  const R m_eps = (R(12) * fl[0] - R(4) * a6 + a12) * S[2];
+  const R m_qx = (R(4) * (fl[2] - fl[1]) + fl[7] - fl[8] + fl[9] - fl[10] + fl[11] - fl[12] + fl[13] - fl[14]) * S[4];
+  const R m_qy = (R(4) * (fl[4] - fl[3]) + fl[7] + fl[8] - fl[9] - fl[10] + fl[15] - fl[16] + fl[17] - fl[18]) * S[6];
+  const R m_qz = (R(4) * (fl[6] - fl[5]) + fl[11] + fl[12] - fl[13] - fl[14] + fl[15] + fl[16] - fl[17] - fl[18]) * S[8];
+  const R sxy4 = fl[7] + fl[8] + fl[9] + fl[10];
+  const R syz4 = fl[15] + fl[16] + fl[17] + fl[18];
+  const R sxz4 = fl[11] + fl[12] + fl[13] + fl[14];
+  const R dyz = fl[3] + fl[4] - fl[5] - fl[6];
+  const R syz2 = fl[3] + fl[4] + fl[5] + fl[6];
+  const R m_pxx = (R(2) * (fl[1] + fl[2] - syz4) - syz2 + sxy4 + sxz4) * S[9];
+  const R m_rxx = (-(R(4) * (fl[1] + fl[2])) + R(2) * (syz2 - syz4) + sxy4 + sxz4) * S[10];
+  const R m_pww = (dyz + sxy4 - sxz4) * S[11];
+  const R m_rww = (-(R(2) * dyz) + sxy4 - sxz4) * S[12];
+  const R m_pxy = (fl[7] - fl[8] - fl[9] + fl[10]) * S[13];
+  const R m_pyz = (fl[15] - fl[16] - fl[17] + fl[18]) * S[14];
+  const R m_pxz = (fl[11] - fl[12] - fl[13] + fl[14]) * S[15];
+  const R m_mx = (fl[7] - fl[8] + fl[9] - fl[10] - fl[11] + fl[12] - fl[13] + fl[14]) * S[16];
+  const R m_my = (-fl[7] - fl[8] + fl[9] + fl[10] + fl[15] - fl[16] + fl[17] - fl[18]) * S[17];
+  const R m_mz = (fl[11] + fl[12] - fl[13] - fl[14] - fl[15] - fl[16] + fl[17] + fl[18]) * S[18];
+
+  // back to population space (explicit inverse-basis coefficients)
+  R mb[19];
+  mb[0] = -(K.c5d399 * m_e) + K.c19d399 * m_eps;
+  const R b1 = -(K.c11d2394 * m_e) - K.c1d63 * m_eps;
+  mb[1] = b1 - R(0.1) * m_qx + K.c1d18 * (m_pxx - m_rxx);
+  mb[2] = mb[1] + m_qx * R(0.2);
+  mb[3] = b1 - R(0.1) * m_qy + K.c1d36 * (m_rxx - m_pxx) + K.c1d12 * (m_pww - m_rww);
+  mb[4] = mb[3] + m_qy * R(0.2);
+  mb[5] = b1 - R(0.1) * m_qz + K.c1d36 * (m_rxx - m_pxx) + K.c1d12 * (m_rww - m_pww);
+  mb[6] = mb[5] + m_qz * R(0.2);
+  const R b2 = K.c4d1197 * m_e + K.c1d252 * m_eps;
+  mb[7] = b2 + (m_qx + m_qy) * R(0.025) + K.c1d36 * m_pxx + K.c1d72 * m_rxx + K.c1d12 * m_pww +
+          K.c1d24 * m_rww + m_pxy * R(0.25) + (m_mx - m_my) * R(0.125);
+  mb[8] = mb[7] - R(0.05) * m_qx - R(0.5) * m_pxy - R(0.25) * m_mx;
+  mb[9] = mb[7] + R(0.25) * m_my - R(0.05) * m_qy - R(0.5) * m_pxy;
+  mb[10] = mb[9] + R(0.5) * m_pxy - R(0.05) * m_qx - R(0.25) * m_mx;
+  mb[11] = b2 + (m_qx + m_qz) * R(0.025) + K.c1d36 * m_pxx + K.c1d72 * m_rxx - K.c1d12 * m_pww -
+           K.c1d24 * m_rww + m_pxz * R(0.25) + (m_mz - m_mx) * R(0.125);
+  mb[12] = mb[11] + R(0.25) * m_mx - R(0.5) * m_pxz - R(0.05) * m_qx;
+  mb[13] = mb[11] - R(0.05) * m_qz - R(0.5) * m_pxz - R(0.25) * m_mz;
+  mb[14] = mb[12] + R(0.5) * m_pxz - R(0.05) * m_qz - R(0.25) * m_mz;
+  mb[15] = b2 + (m_qy + m_qz) * R(0.025) - K.c1d18 * m_pxx - K.c1d36 * m_rxx + m_pyz * R(0.25) +
+           (m_my - m_mz) * R(0.125);
+  mb[16] = mb[15] - R(0.05) * m_qy - R(0.5) * m_pyz - R(0.25) * m_my;
+  mb[17] = mb[15] + R(0.25) * m_mz - R(0.05) * m_qz - R(0.5) * m_pyz;
+  mb[18] = mb[17] + R(0.5) * m_pyz - R(0.05) * m_qy - R(0.25) * m_my;
+
+  f[0] = f[0] - mb[0] + Fp[0];
+#pragma unroll
+  for (int i = 1; i < 19; i++) pcf[i] = f[i] - mb[i] + Fp[i];
+}
+
+// CSF surface tension from the colour neighbourhood.  cc(i,j,k), i,j,k in
+// {0,1,2} (offsets -1,0,+1 in x,y,z) returns the stencil colour: the node's
+// colour for fluid voxels, the wetting colour for the others.  The colour
+// gradient is evaluated on the 8 sub-cubes of the 3x3x3 box; the curvature
+// is k2 - k1 with k1 = div of the sub-cube gradients and k2 the gradient of
+// their modulus along the normal.  Returns Fs = sig (k2 - k1) n and n.
+template <typename R, typename CC>
+PS_HD void csf_force(const LbmConst<R>& K, CC cc, R* n, R* Fs)
+{
+  // Sub-cube s = a + 2b + 4c has its low corner at offset (a,b,c).  Its
+  // gradient components are differences of the two 2x2 faces normal to each
+  // axis; every face sum is (edge + edge) with edges summed low index first.
+  R g[8][3];
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    const int a = s & 1, b = (s >> 1) & 1, c = s >> 2;
+    // x: faces at x=a+1 and x=a, edges along y, summed over z
+    const R xh = (cc(a + 1, b, c) + cc(a + 1, b + 1, c)) + (cc(a + 1, b, c + 1) + cc(a + 1, b + 1, c + 1));
+    const R xl = (cc(a, b, c) + cc(a, b + 1, c)) + (cc(a, b, c + 1) + cc(a, b + 1, c + 1));
+    // y: faces at y=b+1 and y=b, edges along x, summed over z
+    const R yh = (cc(a, b + 1, c) + cc(a + 1, b + 1, c)) + (cc(a, b + 1, c + 1) + cc(a + 1, b + 1, c + 1));
+    const R yl = (cc(a, b, c) + cc(a + 1, b, c)) + (cc(a, b, c + 1) + cc(a + 1, b, c + 1));
+    // z: faces at z=c+1 and z=c, edges along x, summed over y
+    const R zh = (cc(a, b, c + 1) + cc(a + 1, b, c + 1)) + (cc(a, b + 1, c + 1) + cc(a + 1, b + 1, c + 1));
+    const R zl = (cc(a, b, c) + cc(a + 1, b, c)) + (cc(a, b + 1, c) + cc(a + 1, b + 1, c));
+    g[s][0] = xh - xl;
+    g[s][1] = yh - yl;
+    g[s][2] = zh - zl;
+  }
+  R nx = g[0][0], ny = g[0][1], nz = g[0][2];
+#pragma unroll
+  for (int s = 1; s < 8; s++) {
+    nx = nx + g[s][0];
+    ny = ny + g[s][1];
+    nz = nz + g[s][2];
+  }
+  const R nrm = sqrt(nx * nx + ny * ny + nz * nz);
+  // divergence of the sub-cube gradients (high half minus low half per axis,
+  // in the reference's summation order)
+  const R k1 = (g[1][0] + g[3][0] + g[5][0] + g[7][0] - g[0][0] - g[2][0] - g[4][0] - g[6][0]) +
+               (g[3][1] + g[7][1] + g[2][1] + g[6][1] - g[0][1] - g[1][1] - g[4][1] - g[5][1]) +
+               (g[4][2] + g[5][2] + g[6][2] + g[7][2] - g[0][2] - g[1][2] - g[2][2] - g[3][2]);
+  R m[8];
+#pragma unroll
+  for (int s = 0; s < 8; s++) m[s] = sqrt(g[s][0] * g[s][0] + g[s][1] * g[s][1] + g[s][2] * g[s][2]);
+  const R mx = m[1] + m[3] + m[5] + m[7] - m[0] - m[2] - m[4] - m[6];
+  const R my = m[3] + m[7] + m[2] + m[6] - m[0] - m[1] - m[4] - m[5];
+  const R mz = m[4] + m[5] + m[6] + m[7] - m[0] - m[1] - m[2] - m[3];
+  R k2 = nx * mx + ny * my + nz * mz;
+  if (nrm != R(0)) {
+    k2 = k2 / nrm;
+    nx = nx / nrm;
+    ny = ny / nrm;
+    nz = nz / nrm;
+  }
+  const R s = K.sig * (k2 - k1);
+  n[0] = nx;
+  n[1] = ny;
+  n[2] = nz;
+  Fs[0] = s * nx;
+  Fs[1] = s * ny;
+  Fs[2] = s * nz;
+}
+
+// One node of the majority-rule step.  fr, fb: post-streaming populations
+// (19 each, modified); out_r/out_b receive all 19 post-collision populations
+// (index 0 = rest).  rr, rb are the component densities of fr, fb.
+template <typename R, typename CC>
+PS_HD void node_update(const LbmConst<R>& K, R* fr, R* fb, R rr, R rb, CC cc, R* out_r, R* out_b)
+{
+  if (rb <= K.ee) {  // bulk red
+    mrt_collide(K, K.t[0][0], K.t[0][1], K.t[0][2], fr, out_r, rr, K.bf[0], K.Fp[0], K.S[0]);
+    out_r[0] = fr[0];
+    out_b[0] = K.t[1][0] * rb;
+#pragma unroll
+    for (int i = 1; i < 19; i++) out_b[i] = K.t[1][i < 7 ? 1 : 2] * rb;
+  } else if (rr <= K.ee) {  // bulk blue
+    mrt_collide(K, K.t[1][0], K.t[1][1], K.t[1][2], fb, out_b, rb, K.bf[1], K.Fp[1], K.S[1]);
+    out_b[0] = fb[0];
+    out_r[0] = K.t[0][0] * rr;
+#pragma unroll
+    for (int i = 1; i < 19; i++) out_r[i] = K.t[0][i < 7 ? 1 : 2] * rr;
+  } else {  // interface: collide the mixture with the majority phase's rates
+    R n[3], Fs[3];
+    csf_force(K, cc, n, Fs);
+    R f[19], pcf[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) f[i] = fr[i] + fb[i];
+    const R ri = rr + rb;
+    const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / ri;
+    const R ti1 = R(1) - R(2) * ci2 * K.dt2;
+    const R ti2 = ci2 * K.c1d6 * K.dt2;
+    const R ti3 = ci2 * K.c1d12 * K.dt2;
+    const int ph = rr >= rb ? 0 : 1;
+    R bfi[3], Fpi[19];
+    bfi[0] = K.bf[ph][0] + Fs[0];
+    bfi[1] = K.bf[ph][1] + Fs[1];
+    bfi[2] = K.bf[ph][2] + Fs[2];
+    const R dt2 = K.dt2;
+    Fpi[0] = R(0);
+    Fpi[1] = K.c1d6 * bfi[0] * dt2;
+    Fpi[2] = -Fpi[1];
+    Fpi[3] = K.c1d6 * bfi[1] * dt2;
+    Fpi[4] = -Fpi[3];
+    Fpi[5] = K.c1d6 * bfi[2] * dt2;
+    Fpi[6] = -Fpi[5];
+    Fpi[7] = K.c1d12 * (bfi[0] + bfi[1]) * dt2;
+    Fpi[8] = K.c1d12 * (-bfi[0] + bfi[1]) * dt2;
+    Fpi[9] = -Fpi[8];
+    Fpi[10] = -Fpi[7];
+    Fpi[11] = K.c1d12 * (bfi[0] + bfi[2]) * dt2;
+    Fpi[12] = K.c1d12 * (-bfi[0] + bfi[2]) * dt2;
+    Fpi[13] = -Fpi[12];
+    Fpi[14] = -Fpi[11];
+    Fpi[15] = K.c1d12 * (bfi[1] + bfi[2]) * dt2;
+    Fpi[16] = K.c1d12 * (-bfi[1] + bfi[2]) * dt2;
+    Fpi[17] = -Fpi[16];
+    Fpi[18] = -Fpi[15];
+    mrt_collide(K, ti1, ti2, ti3, f, pcf, ri, bfi, Fpi, K.S[ph]);
+    // cosine between the colour normal and each direction
+    R cs[19];
+    cs[1] = n[0];
+    cs[2] = -cs[1];
+    cs[3] = n[1];
+    cs[4] = -cs[3];
+    cs[5] = n[2];
+    cs[6] = -cs[5];
+    cs[7] = (n[0] + n[1]) * K.cn;
+    cs[8] = (-n[0] + n[1]) * K.cn;
+    cs[9] = -cs[8];
+    cs[10] = -cs[7];
+    cs[11] = (n[0] + n[2]) * K.cn;
+    cs[12] = (-n[0] + n[2]) * K.cn;
+    cs[13] = -cs[12];
+    cs[14] = -cs[11];
+    cs[15] = (n[1] + n[2]) * K.cn;
+    cs[16] = (-n[1] + n[2]) * K.cn;
+    cs[17] = -cs[16];
+    cs[18] = -cs[15];
+    // rest population split by mass fraction, moving ones recoloured
+    out_r[0] = f[0] * rr / ri;
+    out_b[0] = f[0] * rb / ri;
+#pragma unroll
+    for (int i = 1; i < 19; i++) {
+      const R w = i < 7 ? ti2 : ti3;
+      out_r[i] = (pcf[i] + K.B * w * cs[i] * rb) * rr / ri;
+      out_b[i] = (pcf[i] - K.B * w * cs[i] * rr) * rb / ri;
+    }
+  }
+}
+
+}  // namespace ps

@@ -1,0 +1,131 @@
+"""GPU parity of the colour-gradient D3Q19 lattice against the FP64 oracle.
+
+The FP64 lattice is compiled without FMA contraction and keeps the
+reference's operation order, so after any number of steps its populations
+must equal the oracle's bit for bit.  The FP32 and 16-bit storage forms are
+compared against the FP64 oracle with the tolerances written in each test.
+"""
+import numpy as np
+import pytest
+
+from porescale_gb300 import PREC_BF16, PREC_F16, PREC_F32, PREC_F64
+from porescale_gb300 import geometry as geo
+from porescale_gb300.lattice import Lattice, make_params
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(n=(20, 18, 24), porosity=0.45, radius=4, seed=7, wet=0.7071067811865476, bf=1e-5, vir=1 / 6, vib=1 / 6,
+          B=0.7, sig=1e-3):
+    ind = geo.sphere_pack(n, porosity, radius, seed)
+    p = make_params(B=B, sig=sig, vir=vir, vib=vib, wet=wet, bfr=(bf, 0, 0), bfb=(bf, 0, 0))
+    return ind, p
+
+
+def test_tables_bit_exact(gpu, oracle_lib):
+    for n, seed in (((20, 18, 24), 7), ((16, 16, 16), 3), ((9, 13, 11), 5)):
+        ind, p = _case(n=n, seed=seed)
+        o = oracle_lib.OracleLattice(p, ind)
+        with Lattice(p, ind, PREC_F64) as L:
+            i = L.info
+            assert (i.nl, i.nps, i.npb2, i.npb4, i.ns) == (o.nl, o.nps, o.npb2, o.npb4, o.ns)
+            icor, ips, ipb2, ipb4 = L.tables()
+            oicor, oips, oipb2, oipb4, _, _ = o.tables()
+            assert np.array_equal(icor, oicor)
+            assert np.array_equal(ips, oips)
+            assert np.array_equal(ipb2, oipb2)
+            assert np.array_equal(ipb4, oipb4)
+
+
+def test_state_roundtrip(gpu, oracle_lib):
+    """set_state/get_state is the identity for every storage precision on FP64 inputs
+    within the storage rounding (exact for FP64)."""
+    ind, p = _case()
+    o = oracle_lib.OracleLattice(p, ind)
+    o.init_random(0.5)
+    o.run(3)
+    fr, fb = o.get_state()
+    for prec, tol in ((PREC_F64, 0.0), (PREC_F32, 1e-7), (PREC_F16, 2e-5), (PREC_BF16, 2e-4)):
+        with Lattice(p, ind, prec) as L:
+            L.set_state(fr, fb)
+            gr, gb = L.get_state()
+            assert np.max(np.abs(gr - fr)) <= tol
+            assert np.max(np.abs(gb - fb)) <= tol
+
+
+@pytest.mark.parametrize("steps", [1, 7, 40])
+def test_f64_bit_exact_vs_oracle(gpu, oracle_lib, steps):
+    ind, p = _case()
+    o = oracle_lib.OracleLattice(p, ind)
+    o.init_random(0.5)
+    with Lattice(p, ind, PREC_F64) as L:
+        L.init_random(0.5)
+        a, b = L.get_state()
+        fr0, fb0 = o.get_state()
+        assert np.array_equal(a, fr0) and np.array_equal(b, fb0)
+        L.step(steps)
+        o.run(steps, 4)
+        gr, gb = L.get_state()
+        fr, fb = o.get_state()
+        nd = int(np.sum(gr != fr) + np.sum(gb != fb))
+        assert nd == 0, f"{nd} populations differ; max |d| = {max(np.abs(gr - fr).max(), np.abs(gb - fb).max())}"
+        rr, rb, cf = L.fields()
+        orr, orb, ocf = o.fields()
+        assert np.array_equal(rr, orr) and np.array_equal(rb, orb) and np.array_equal(cf, ocf)
+
+
+def test_f64_observables_vs_oracle(gpu, oracle_lib):
+    ind, p = _case()
+    o = oracle_lib.OracleLattice(p, ind)
+    o.init_random(0.5)
+    o.run(25, 4)
+    with Lattice(p, ind, PREC_F64) as L:
+        L.init_random(0.5)
+        L.step(25)
+        g = L.observables().as_dict()
+    ob = o.observables()
+    rel = 1e-11
+    for k in ("tmr", "tmb", "tm", "Cpr", "Cpb", "permr", "permb"):
+        if np.isnan(ob[k]):  # e.g. Cpr = cr2*0/0 when no node has cf > 0.99
+            assert np.isnan(g[k]), k
+            continue
+        assert g[k] == pytest.approx(ob[k], rel=rel, abs=1e-14), k
+    for d in range(3):
+        assert g["Qr"][d] == pytest.approx(ob[f"Qr{d}"], rel=rel, abs=1e-16)
+        assert g["Qb"][d] == pytest.approx(ob[f"Qb{d}"], rel=rel, abs=1e-16)
+        assert g["bmt"][d] == pytest.approx(ob[f"bmt{d}"], rel=rel, abs=1e-12)
+        assert g["rmt"][d] == pytest.approx(ob[f"rmt{d}"], rel=rel, abs=1e-12)
+    assert (g["nr"], g["nb"], g["nr_cf"], g["nb_cf"]) == (ob["nr"], ob["nb"], ob["nr_cf"], ob["nb_cf"])
+    assert g["isneg"] == int(ob["isneg"])
+
+
+@pytest.mark.parametrize("prec,tol", [(PREC_F32, 2e-5), (PREC_F16, 5e-4), (PREC_BF16, 3e-3)])
+def test_low_precision_close_to_oracle(gpu, oracle_lib, prec, tol):
+    """Population max-abs error after 20 steps, relative to the rest weight
+    scale (populations are O(0.05)): FP32 2e-5, FP16 5e-4, BF16 3e-3."""
+    ind, p = _case()
+    o = oracle_lib.OracleLattice(p, ind)
+    o.init_random(0.5)
+    o.run(20, 4)
+    fr, fb = o.get_state()
+    with Lattice(p, ind, prec) as L:
+        L.init_random(0.5)
+        L.step(20)
+        gr, gb = L.get_state()
+    err = max(np.abs(gr - fr).max(), np.abs(gb - fb).max())
+    assert err <= tol, err
+
+
+def test_block_sizes_agree(gpu):
+    """Every compiled (collide, density) block-size pair gives the same FP64 result."""
+    ind, p = _case(n=(40, 12, 20))
+    ref = None
+    for tx, ty in ((128, 256), (256, 256)):
+        with Lattice(p, ind, PREC_F64) as L:
+            L.set_tile(tx, ty, 0)
+            L.init_random(0.4)
+            L.step(6)
+            st = L.get_state()
+        if ref is None:
+            ref = st
+        assert np.array_equal(st[0], ref[0]) and np.array_equal(st[1], ref[1]), (tx, ty)
