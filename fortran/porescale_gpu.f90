@@ -1,0 +1,132 @@
+! porescale_gpu.f90 -- ISO_C_BINDING interface of libporescale_gpu.so for the
+! Fortran drivers of porescale (lsm_lbm_static_alpha_beta_multipore.f,
+! alfabeta2solid.f, XX_P.f, YZ_P.f).  Every routine binds one entry point
+! declared in include/porescale.h; arrays are passed in the drivers' own
+! layouts (ind(ncx,ncy,ncz), fr(19,nl), rdat(3,ns)) without copies.
+!
+! Build (with any Fortran 2003 compiler):
+!   gfortran -c porescale_gpu.f90
+!   gfortran driver.f porescale_gpu.o -L<dir> -lporescale_gpu -Wl,-rpath,<dir>
+module porescale_gpu
+  use, intrinsic :: iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: PS_OK = 0
+  integer(c_int), parameter :: PS_PREC_F64 = 0, PS_PREC_F32 = 1, PS_PREC_F16 = 2, PS_PREC_BF16 = 3
+  integer(c_int), parameter :: PS_LOAD_XSTRETCH = 0, PS_LOAD_YZSHEAR = 1
+  integer(c_int), parameter :: PS_LSM_F64 = 0, PS_LSM_MIXED = 1
+
+  ! ps_lbm_params: the LBM block of INPUT_PARAMETERS (S1:435-469)
+  type, bind(c) :: ps_lbm_params
+    real(c_double) :: cr2, rr0, rb0, B, sig, vir, vib, wet, ee, dt
+    real(c_double) :: bfr(3), bfb(3)
+    integer(c_int32_t) :: idir, iipore
+  end type
+
+  type, bind(c) :: ps_lbm_info
+    integer(c_int64_t) :: nl, nps, npb2, npb4, ns, nvox
+    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, zchunk, reserved
+    integer(c_int64_t) :: device_bytes
+  end type
+
+  ! ps_lbm_obs: check_state quantities (S1:2988-3202)
+  type, bind(c) :: ps_lbm_obs
+    real(c_double) :: tmr, tmb, tm, Cpr, Cpb, nr_cf, nb_cf, nr, nb
+    real(c_double) :: Qr(3), Qb(3), um(3), umr(3), umb(3), tfr(3), tfb(3), bmt(3), rmt(3)
+    real(c_double) :: permr, permb, sat_r, sat_b
+    integer(c_int32_t) :: isneg, nneg_rr, nneg_rb, reserved
+  end type
+
+  type, bind(c) :: ps_lsm_params
+    real(c_double) :: alf1, bet1, alf2, bet2, gstrain
+    integer(c_int32_t) :: load, precision
+  end type
+
+  type, bind(c) :: ps_lsm_result
+    real(c_double) :: modulus, sigma(9), strain, relres
+    integer(c_int64_t) :: iterations, inner_iterations, nnode, ncube
+    integer(c_int32_t) :: refinements, converged
+  end type
+
+  interface
+    integer(c_int) function ps_lbm_create(p, ind, nx, ny, nz, precision, handle) bind(c, name='ps_lbm_create')
+      import :: c_int, c_int32_t, c_ptr, ps_lbm_params
+      type(ps_lbm_params), intent(in) :: p
+      integer(c_int32_t), intent(in) :: ind(*)
+      integer(c_int32_t), value :: nx, ny, nz, precision
+      type(c_ptr), intent(out) :: handle
+    end function
+    integer(c_int) function ps_lbm_destroy(handle) bind(c, name='ps_lbm_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: handle
+    end function
+    integer(c_int) function ps_lbm_get_info(handle, info) bind(c, name='ps_lbm_get_info')
+      import :: c_int, c_ptr, ps_lbm_info
+      type(c_ptr), value :: handle
+      type(ps_lbm_info), intent(out) :: info
+    end function
+    integer(c_int) function ps_lbm_tables(handle, icor, ips, ipb2, ipb4) bind(c, name='ps_lbm_tables')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), intent(out) :: icor(*), ips(*), ipb2(*), ipb4(*)
+    end function
+    integer(c_int) function ps_lbm_set_state(handle, fr, fb) bind(c, name='ps_lbm_set_state')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(in) :: fr(*), fb(*)
+    end function
+    integer(c_int) function ps_lbm_get_state(handle, fr, fb) bind(c, name='ps_lbm_get_state')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: fr(*), fb(*)
+    end function
+    integer(c_int) function ps_lbm_init_random(handle, sat) bind(c, name='ps_lbm_init_random')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), value :: sat
+    end function
+    integer(c_int) function ps_lbm_step(handle, nsteps) bind(c, name='ps_lbm_step')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: nsteps
+    end function
+    integer(c_int) function ps_lbm_observables(handle, obs) bind(c, name='ps_lbm_observables')
+      import :: c_int, c_ptr, ps_lbm_obs
+      type(c_ptr), value :: handle
+      type(ps_lbm_obs), intent(out) :: obs
+    end function
+    integer(c_int) function ps_lbm_fields(handle, rr, rb, cf) bind(c, name='ps_lbm_fields')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: rr(*), rb(*), cf(*)
+    end function
+    integer(c_int) function ps_lsm_create(p, ind, nx, ny, nz, handle) bind(c, name='ps_lsm_create')
+      import :: c_int, c_int32_t, c_ptr, ps_lsm_params
+      type(ps_lsm_params), intent(in) :: p
+      integer(c_int32_t), intent(in) :: ind(*)
+      integer(c_int32_t), value :: nx, ny, nz
+      type(c_ptr), intent(out) :: handle
+    end function
+    integer(c_int) function ps_lsm_solve(handle, rtol, maxit, res) bind(c, name='ps_lsm_solve')
+      import :: c_int, c_int32_t, c_double, c_ptr, ps_lsm_result
+      type(c_ptr), value :: handle
+      real(c_double), value :: rtol
+      integer(c_int32_t), value :: maxit
+      type(ps_lsm_result), intent(out) :: res
+    end function
+    integer(c_int) function ps_lsm_get_disp(handle, u) bind(c, name='ps_lsm_get_disp')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: u(*)
+    end function
+    integer(c_int) function ps_lsm_destroy(handle) bind(c, name='ps_lsm_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: handle
+    end function
+    integer(c_int) function ps_last_error(buf, len) bind(c, name='ps_last_error')
+      import :: c_int, c_int32_t, c_char
+      character(kind=c_char), intent(out) :: buf(*)
+      integer(c_int32_t), value :: len
+    end function
+  end interface
+end module porescale_gpu

@@ -121,6 +121,55 @@ int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t zchunk);
  * keeps the fastest; writes the chosen tile to *tx, *ty, *zchunk. */
 int ps_lbm_autotune(void *handle, int32_t steps, int32_t *tx, int32_t *ty, int32_t *zchunk);
 
+/* ---- lattice-spring static solve (hot path b) ---- */
+#define PS_LOAD_XSTRETCH 0 /* x stretch with tied x faces: Cxxxx (XX_P.f) */
+#define PS_LOAD_YZSHEAR 1  /* yz shear with tied y faces: Cyzyz (YZ_P.f)  */
+#define PS_LSM_F64 0       /* FP64 conjugate gradient                                */
+#define PS_LSM_MIXED 1     /* FP32 CG inside FP64 iterative refinement              */
+
+/* Spring constants per solid phase (alf = Em/(5-10nu), bet =
+ * Em(4nu-1)/(20(2nu^2+nu-1)), XX:411-414) and the imposed half jump g:
+ * the loaded faces are tied with a displacement jump 2g (strain 2g/N). */
+typedef struct {
+  double alf1, bet1, alf2, bet2, gstrain;
+  int32_t load, precision;
+} ps_lsm_params;
+
+typedef struct {
+  int64_t nnode;   /* unique solid nodes (the tied planes counted once) */
+  int64_t ncube;   /* solid voxel cubes                                  */
+  int64_t nvox;
+  int32_t nx, ny, nz, load, precision, reserved;
+  int64_t device_bytes;
+} ps_lsm_info;
+
+typedef struct {
+  double modulus;    /* Exxxx = <sigma>(1,1)/(V 2g/N) or Eyzyz = <sigma>(2,3)/(V 2g/N) */
+  double sigma[9];   /* summed cube stress sigma+ (calc_stress asigmap), row = force component */
+  double strain;     /* 2g/N */
+  double relres;     /* final FP64 relative residual |b - A x| / |b| */
+  int64_t iterations;        /* FP64 CG iterations, or outer refinements (mixed) */
+  int64_t inner_iterations;  /* CG iterations in the working precision */
+  int64_t nnode, ncube;
+  int32_t refinements, converged;
+} ps_lsm_result;
+
+/* Builds the spring network of the voxel field ind(nx,ny,nz) (0 = solid
+ * phase 1, 3 = solid phase 2, other values pore).  Replaces the geometry,
+ * bond and angle construction of XX:446-1361 (YZ likewise). */
+int ps_lsm_create(const ps_lsm_params *p, const int32_t *ind, int32_t nx, int32_t ny, int32_t nz, void **handle);
+int ps_lsm_destroy(void *handle);
+int ps_lsm_get_info(void *handle, ps_lsm_info *out);
+/* Static equilibrium to |b - A x| <= rtol |b| and the effective modulus.
+ * Replaces the damped-Verlet loop XX:1377-1545 and calc_stress
+ * XX:1628-1997.  Returns PS_ERR_NOTCONV (result still filled) when the
+ * tolerance is not reached within maxit working-precision iterations. */
+int ps_lsm_solve(void *handle, double rtol, int32_t maxit, ps_lsm_result *out);
+/* Displacements (3, ns) in the reference node order (k-j-i over the padded
+ * grid, duplicate plane included, as LSM_displ_field) after a solve. */
+int ps_lsm_get_disp(void *handle, double *u);
+void *ps_lsm_stream(void *handle);
+
 /* Message of the last error on this thread (always NUL-terminated). */
 int ps_last_error(char *buf, int32_t len);
 /* Library build information ("porescale_gb300 <version> sm_103a"). */

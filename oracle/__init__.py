@@ -138,3 +138,89 @@ class OracleLattice:
         out = np.zeros(41)
         lib().or_lbm_observables(self._h, _d(out))
         return dict(zip(OBS_NAMES, out.tolist()))
+
+
+def _lsm_sigs(L):
+    sig = {
+        "or_lsm_create": (C.c_void_p, [_IP, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_double, C.c_int]),
+        "or_lsm_destroy": (None, [C.c_void_p]),
+        "or_lsm_sizes": (None, [C.c_void_p, _LP]),
+        "or_lsm_tables": (None, [C.c_void_p, _IP, _IP, _DP, _IP, _DP]),
+        "or_lsm_forces": (None, [C.c_void_p, _DP, _DP]),
+        "or_lsm_relax": (C.c_int64, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double]),
+        "or_lsm_cg": (C.c_int64, [C.c_void_p, C.c_double, C.c_int64, _DP]),
+        "or_lsm_get_disp": (None, [C.c_void_p, _DP]),
+        "or_lsm_set_disp": (None, [C.c_void_p, _DP]),
+        "or_lsm_stress": (None, [C.c_void_p, _DP]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+class OracleSprings:
+    """FP64 CPU restatement of the two-solid lattice-spring model
+    (load 0 = x-stretch as XX_P.f, 1 = yz-shear as YZ_P.f)."""
+
+    def __init__(self, ind: np.ndarray, alf1, bet1, alf2, bet2, gstrain, load=0):
+        L = lib()
+        if not getattr(L, "_lsm_ready", False):
+            _lsm_sigs(L)
+            L._lsm_ready = True
+        ind = np.ascontiguousarray(ind, np.int32)
+        nz, ny, nx = ind.shape
+        self.shape = (nz, ny, nx)
+        self._h = C.c_void_p(L.or_lsm_create(_i(ind), nx, ny, nz, alf1, bet1, alf2, bet2, gstrain, load))
+        s = np.zeros(4, np.int64)
+        L.or_lsm_sizes(self._h, s.ctypes.data_as(_LP))
+        self.ns, self.nbo, self.nna, self.nunique = (int(v) for v in s)
+
+    def close(self):
+        if self._h:
+            lib().or_lsm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tables(self):
+        icors = np.zeros((self.ns, 3), np.int32)
+        bon = np.zeros((self.nbo, 3), np.int32)
+        sbond = np.zeros(self.nbo)
+        ang = np.zeros((self.nna, 6), np.int32)
+        abond = np.zeros(self.nna)
+        lib().or_lsm_tables(self._h, _i(icors), _i(bon), _d(sbond), _i(ang), _d(abond))
+        return icors, bon, sbond, ang, abond
+
+    def forces(self, u):
+        u = np.ascontiguousarray(u, np.float64)
+        a = np.zeros_like(u)
+        lib().or_lsm_forces(self._h, _d(u), _d(a))
+        return a
+
+    def relax(self, dt, rs, damp, maxsteps, ftol):
+        return int(lib().or_lsm_relax(self._h, dt, rs, damp, int(maxsteps), ftol))
+
+    def cg(self, rtol=1e-10, maxit=100000):
+        rel = C.c_double()
+        it = int(lib().or_lsm_cg(self._h, rtol, int(maxit), C.byref(rel)))
+        return it, rel.value
+
+    def disp(self):
+        u = np.zeros((self.ns, 3))
+        lib().or_lsm_get_disp(self._h, _d(u))
+        return u
+
+    def set_disp(self, u):
+        u = np.ascontiguousarray(u, np.float64)
+        lib().or_lsm_set_disp(self._h, _d(u))
+
+    def stress(self):
+        out = np.zeros(12)
+        lib().or_lsm_stress(self._h, _d(out))
+        return {"sigma": out[:9].reshape(3, 3), "modulus": out[9], "strain": out[10], "ncube": int(out[11])}

@@ -17,8 +17,9 @@ from __future__ import annotations
 from ._lib import (PREC_BF16, PREC_F16, PREC_F32, PREC_F64, PREC_NAMES, LbmInfo, LbmObs, LbmParams, PorescaleError,
                    library, library_path)
 from .lattice import Lattice
+from .springs import SpringNetwork, spring_constants
 
 __all__ = [
-    "Lattice", "LbmParams", "LbmInfo", "LbmObs", "PorescaleError", "library", "library_path",
+    "Lattice", "SpringNetwork", "spring_constants", "LbmParams", "LbmInfo", "LbmObs", "PorescaleError", "library", "library_path",
     "PREC_F64", "PREC_F32", "PREC_F16", "PREC_BF16", "PREC_NAMES",
 ]

@@ -224,6 +224,12 @@ void build_geometry(Lattice* L, std::vector<uint32_t>& mask, std::vector<int32_t
     const long long v = L->fvox[i];
     const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long long)nx * ny));
     uint32_t m = kFluidBit;
+    if (x == 0) m |= 1u << (kWrapShift + 0);
+    if (x == nx - 1) m |= 1u << (kWrapShift + 1);
+    if (y == 0) m |= 1u << (kWrapShift + 2);
+    if (y == ny - 1) m |= 1u << (kWrapShift + 3);
+    if (z == 0) m |= 1u << (kWrapShift + 4);
+    if (z == nz - 1) m |= 1u << (kWrapShift + 5);
     // incoming link d is open when the outgoing link d of x - c_d streams;
     // by symmetry that is the outgoing link opp(d) of x itself
     for (int d = 1; d < 19; d++) {

@@ -10,7 +10,9 @@
 //     bounce-back).  This is the reference's push streaming (ips) and
 //     bounce-back (ipb2, ipb4) seen from the receiving node;
 //   * mask[v]: bit 31 = fluid node, bit d-1 (d = 1..18) = incoming link d
-//     open (the link from x - c_d is one of the reference's ips entries);
+//     open (the link from x - c_d is one of the reference's ips entries),
+//     bits 18..23 = node on the low/high x, y, z face of the box (periodic
+//     wrap), so neighbour addresses need no division;
 //   * pvox[i]: the fluid voxels in ascending voxel order -- every thread of
 //     the step kernels owns one fluid node, so no lane idles on solid voxels
 //     and consecutive lanes read consecutive voxels;
@@ -68,6 +70,28 @@ static_assert(opp(7) == 10 && opp(8) == 9 && opp(11) == 14 && opp(12) == 13, "op
 static_assert(opp(15) == 18 && opp(16) == 17 && opp(1) == 2 && opp(5) == 6, "opposites");
 
 constexpr uint32_t kFluidBit = 1u << 31;
+constexpr int kWrapShift = 18;  // bits 18..23: x==0, x==nx-1, y==0, y==ny-1, z==0, z==nz-1
+
+// voxel-index offsets of the neighbours at -1, 0, +1 along each axis,
+// periodic wrap taken from the mask's face bits
+struct NbOff {
+  int x[3], y[3], z[3];
+};
+__device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int nz)
+{
+  NbOff o;
+  const int ny_nx = nxy;  // nx*ny
+  o.x[0] = (m & (1u << (kWrapShift + 0))) ? nx - 1 : -1;
+  o.x[1] = 0;
+  o.x[2] = (m & (1u << (kWrapShift + 1))) ? 1 - nx : 1;
+  o.y[0] = (m & (1u << (kWrapShift + 2))) ? ny_nx - nx : -nx;
+  o.y[1] = 0;
+  o.y[2] = (m & (1u << (kWrapShift + 3))) ? nx - ny_nx : nx;
+  o.z[0] = (m & (1u << (kWrapShift + 4))) ? (nz - 1) * ny_nx : -ny_nx;
+  o.z[1] = 0;
+  o.z[2] = (m & (1u << (kWrapShift + 5))) ? (1 - nz) * ny_nx : ny_nx;
+  return o;
+}
 
 struct GeomDev {
   int nx, ny, nz;
@@ -209,6 +233,27 @@ __device__ __forceinline__ void pull_node(const LbmConst<typename Store<PREC>::R
   }
 }
 
+// Pull by voxel index and mask only (32-bit addressing): the step kernels'
+// form of pull_node.
+template <int PREC>
+__device__ __forceinline__ void pull_fast(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, int v, uint32_t m, const NbOff& o,
+                                          typename Store<PREC>::R* f)
+{
+  const long long nv = G.nvox;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    f[19 * k] = Pop<PREC>::load(K, src, k, 0, v, nv);
+#pragma unroll
+    for (int d = 1; d < 19; d++) {
+      const bool open = m & (1u << (d - 1));
+      const int vs = open ? v + o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : v;
+      const int ds = open ? d : opp(d);
+      f[19 * k + d] = Pop<PREC>::load(K, src, k, ds, vs, nv);
+    }
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ void densities(const R* f, R& rr, R& rb)
 {
@@ -238,12 +283,13 @@ __global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmCon
                                                   const BufDev dst, typename Store<PREC>::R* __restrict__ cc)
 {
   using R = typename Store<PREC>::R;
-  const long long i = blockIdx.x * (long long)BLK + threadIdx.x;
+  const int i = blockIdx.x * BLK + threadIdx.x;
   if (i >= G.nl) return;
-  const long long v = __ldg(G.pvox + i);
-  const int x = (int)(v % G.nx), y = (int)((v / G.nx) % G.ny), z = (int)(v / ((long long)G.nx * G.ny));
+  const int v = __ldg(G.pvox + i);
+  const uint32_t m = __ldg(G.mask + v);
+  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.nz);
   R f[38];
-  pull_node<PREC>(K, G, src, x, y, z, __ldg(G.mask + v), f);
+  pull_fast<PREC>(K, G, src, v, m, o, f);
   R rr, rb;
   densities(f, rr, rb);
   cc[v] = stencil_colour(rr, rb, K.wet);
@@ -260,20 +306,16 @@ __global__ void __launch_bounds__(BLK) k_lbm_coll(const __grid_constant__ LbmCon
                                                   const BufDev dst, const typename Store<PREC>::R* __restrict__ cc)
 {
   using R = typename Store<PREC>::R;
-  const long long i = blockIdx.x * (long long)BLK + threadIdx.x;
+  const int i = blockIdx.x * BLK + threadIdx.x;
   if (i >= G.nl) return;
-  const long long v = __ldg(G.pvox + i);
-  const int x = (int)(v % G.nx), y = (int)((v / G.nx) % G.ny), z = (int)(v / ((long long)G.nx * G.ny));
+  const int v = __ldg(G.pvox + i);
+  const uint32_t m = __ldg(G.mask + v);
+  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.nz);
   R f[38];
-  pull_node<PREC>(K, G, src, x, y, z, __ldg(G.mask + v), f);
+  pull_fast<PREC>(K, G, src, v, m, o, f);
   R rr, rb;
   densities(f, rr, rb);
-  int xs[3], ys[3], zs[3];
-  nb3(x, G.nx, xs);
-  nb3(y, G.ny, ys);
-  nb3(z, G.nz, zs);
-  const long long nxl = G.nx, nxy = (long long)G.nx * G.ny;
-  auto col = [&](int a, int b, int c) -> R { return cc[xs[a] + nxl * ys[b] + nxy * zs[c]]; };
+  auto col = [&](int a, int b, int c) -> R { return cc[v + o.x[a] + o.y[b] + o.z[c]]; };
   R outr[19], outb[19];
   node_update(K, f, f + 19, rr, rb, col, outr, outb);
   Pop<PREC>::store(K, dst, 0, v, G.nvox, outr, rr);

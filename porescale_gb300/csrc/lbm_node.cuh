@@ -220,60 +220,81 @@ PS_HD void csf_force(const LbmConst<R>& K, CC cc, R* n, R* Fs)
 }
 
 // One node of the majority-rule step.  fr, fb: post-streaming populations
-// (19 each, modified); out_r/out_b receive all 19 post-collision populations
-// (index 0 = rest).  rr, rb are the component densities of fr, fb.
+// (19 each); out_r/out_b receive all 19 post-collision populations (index
+// 0 = rest).  rr, rb are the component densities of fr, fb.
+//
+// The three branches of the reference (bulk red, bulk blue, interface) all
+// reduce to one forced collision with branch-dependent inputs, so the
+// collision is evaluated once per node: a warp holding nodes of all three
+// kinds executes it once instead of three times.  Per node the arithmetic is
+// exactly the reference's.
 template <typename R, typename CC>
-PS_HD void node_update(const LbmConst<R>& K, R* fr, R* fb, R rr, R rb, CC cc, R* out_r, R* out_b)
+PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R rb, CC cc, R* out_r, R* out_b)
 {
-  if (rb <= K.ee) {  // bulk red
-    mrt_collide(K, K.t[0][0], K.t[0][1], K.t[0][2], fr, out_r, rr, K.bf[0], K.Fp[0], K.S[0]);
-    out_r[0] = fr[0];
-    out_b[0] = K.t[1][0] * rb;
-#pragma unroll
-    for (int i = 1; i < 19; i++) out_b[i] = K.t[1][i < 7 ? 1 : 2] * rb;
-  } else if (rr <= K.ee) {  // bulk blue
-    mrt_collide(K, K.t[1][0], K.t[1][1], K.t[1][2], fb, out_b, rb, K.bf[1], K.Fp[1], K.S[1]);
-    out_b[0] = fb[0];
-    out_r[0] = K.t[0][0] * rr;
-#pragma unroll
-    for (int i = 1; i < 19; i++) out_r[i] = K.t[0][i < 7 ? 1 : 2] * rr;
-  } else {  // interface: collide the mixture with the majority phase's rates
-    R n[3], Fs[3];
+  constexpr bool kExact = sizeof(R) == 8;  // FP64: keep every division as written
+  const bool bulk_r = rb <= K.ee;
+  const bool bulk_b = !bulk_r && rr <= K.ee;
+  const bool iface = !bulk_r && !bulk_b;
+  // collision inputs
+  R f[19], pcf[19], Fp[19], S[19], bf[3], n[3] = {R(0), R(0), R(0)};
+  R t1, t2, t3, r, ti2 = R(0), ti3 = R(0);
+  if (iface) {
+    R Fs[3];
     csf_force(K, cc, n, Fs);
-    R f[19], pcf[19];
 #pragma unroll
     for (int i = 0; i < 19; i++) f[i] = fr[i] + fb[i];
     const R ri = rr + rb;
     const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / ri;
-    const R ti1 = R(1) - R(2) * ci2 * K.dt2;
-    const R ti2 = ci2 * K.c1d6 * K.dt2;
-    const R ti3 = ci2 * K.c1d12 * K.dt2;
+    t1 = R(1) - R(2) * ci2 * K.dt2;
+    ti2 = ci2 * K.c1d6 * K.dt2;
+    ti3 = ci2 * K.c1d12 * K.dt2;
+    t2 = ti2;
+    t3 = ti3;
+    r = ri;
     const int ph = rr >= rb ? 0 : 1;
-    R bfi[3], Fpi[19];
-    bfi[0] = K.bf[ph][0] + Fs[0];
-    bfi[1] = K.bf[ph][1] + Fs[1];
-    bfi[2] = K.bf[ph][2] + Fs[2];
+    bf[0] = K.bf[ph][0] + Fs[0];
+    bf[1] = K.bf[ph][1] + Fs[1];
+    bf[2] = K.bf[ph][2] + Fs[2];
+#pragma unroll
+    for (int i = 0; i < 19; i++) S[i] = K.S[ph][i];
     const R dt2 = K.dt2;
-    Fpi[0] = R(0);
-    Fpi[1] = K.c1d6 * bfi[0] * dt2;
-    Fpi[2] = -Fpi[1];
-    Fpi[3] = K.c1d6 * bfi[1] * dt2;
-    Fpi[4] = -Fpi[3];
-    Fpi[5] = K.c1d6 * bfi[2] * dt2;
-    Fpi[6] = -Fpi[5];
-    Fpi[7] = K.c1d12 * (bfi[0] + bfi[1]) * dt2;
-    Fpi[8] = K.c1d12 * (-bfi[0] + bfi[1]) * dt2;
-    Fpi[9] = -Fpi[8];
-    Fpi[10] = -Fpi[7];
-    Fpi[11] = K.c1d12 * (bfi[0] + bfi[2]) * dt2;
-    Fpi[12] = K.c1d12 * (-bfi[0] + bfi[2]) * dt2;
-    Fpi[13] = -Fpi[12];
-    Fpi[14] = -Fpi[11];
-    Fpi[15] = K.c1d12 * (bfi[1] + bfi[2]) * dt2;
-    Fpi[16] = K.c1d12 * (-bfi[1] + bfi[2]) * dt2;
-    Fpi[17] = -Fpi[16];
-    Fpi[18] = -Fpi[15];
-    mrt_collide(K, ti1, ti2, ti3, f, pcf, ri, bfi, Fpi, K.S[ph]);
+    Fp[0] = R(0);
+    Fp[1] = K.c1d6 * bf[0] * dt2;
+    Fp[2] = -Fp[1];
+    Fp[3] = K.c1d6 * bf[1] * dt2;
+    Fp[4] = -Fp[3];
+    Fp[5] = K.c1d6 * bf[2] * dt2;
+    Fp[6] = -Fp[5];
+    Fp[7] = K.c1d12 * (bf[0] + bf[1]) * dt2;
+    Fp[8] = K.c1d12 * (-bf[0] + bf[1]) * dt2;
+    Fp[9] = -Fp[8];
+    Fp[10] = -Fp[7];
+    Fp[11] = K.c1d12 * (bf[0] + bf[2]) * dt2;
+    Fp[12] = K.c1d12 * (-bf[0] + bf[2]) * dt2;
+    Fp[13] = -Fp[12];
+    Fp[14] = -Fp[11];
+    Fp[15] = K.c1d12 * (bf[1] + bf[2]) * dt2;
+    Fp[16] = K.c1d12 * (-bf[1] + bf[2]) * dt2;
+    Fp[17] = -Fp[16];
+    Fp[18] = -Fp[15];
+  } else {
+    const int k = bulk_r ? 0 : 1;
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      f[i] = bulk_r ? fr[i] : fb[i];
+      Fp[i] = K.Fp[k][i];
+      S[i] = K.S[k][i];
+    }
+    t1 = K.t[k][0];
+    t2 = K.t[k][1];
+    t3 = K.t[k][2];
+    r = bulk_r ? rr : rb;
+    bf[0] = K.bf[k][0];
+    bf[1] = K.bf[k][1];
+    bf[2] = K.bf[k][2];
+  }
+  mrt_collide(K, t1, t2, t3, f, pcf, r, bf, Fp, S);
+  if (iface) {
     // cosine between the colour normal and each direction
     R cs[19];
     cs[1] = n[0];
@@ -295,13 +316,35 @@ PS_HD void node_update(const LbmConst<R>& K, R* fr, R* fb, R rr, R rb, CC cc, R*
     cs[17] = -cs[16];
     cs[18] = -cs[15];
     // rest population split by mass fraction, moving ones recoloured
-    out_r[0] = f[0] * rr / ri;
-    out_b[0] = f[0] * rb / ri;
+    // (Latva-Kokko), S1:3797-3817
+    if constexpr (kExact) {
+      out_r[0] = f[0] * rr / r;
+      out_b[0] = f[0] * rb / r;
 #pragma unroll
-    for (int i = 1; i < 19; i++) {
-      const R w = i < 7 ? ti2 : ti3;
-      out_r[i] = (pcf[i] + K.B * w * cs[i] * rb) * rr / ri;
-      out_b[i] = (pcf[i] - K.B * w * cs[i] * rr) * rb / ri;
+      for (int i = 1; i < 19; i++) {
+        const R w = i < 7 ? ti2 : ti3;
+        out_r[i] = (pcf[i] + K.B * w * cs[i] * rb) * rr / r;
+        out_b[i] = (pcf[i] - K.B * w * cs[i] * rr) * rb / r;
+      }
+    } else {
+      const R inv = R(1) / r, qr = rr * inv, qb = rb * inv;
+      out_r[0] = f[0] * qr;
+      out_b[0] = f[0] * qb;
+#pragma unroll
+      for (int i = 1; i < 19; i++) {
+        const R w = K.B * (i < 7 ? ti2 : ti3) * cs[i];
+        out_r[i] = (pcf[i] + w * rb) * qr;
+        out_b[i] = (pcf[i] - w * rr) * qb;
+      }
+    }
+  } else {
+    // collided component, and the other one at its rest equilibrium
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      const R c = i == 0 ? f[0] : pcf[i];
+      const int w = i == 0 ? 0 : (i < 7 ? 1 : 2);
+      out_r[i] = bulk_r ? c : K.t[0][w] * rr;
+      out_b[i] = bulk_r ? K.t[1][w] * rb : c;
     }
   }
 }

@@ -1,0 +1,514 @@
+// lsm_api.cu -- C ABI of the lattice-spring static solve (include/porescale.h).
+//
+// Replaces the reference's damped-Verlet relaxation and calc_stress
+// (XX_P.f:1377-1545, 1628-1997; YZ_P.f likewise) by a conjugate-gradient
+// solve of the same linear spring network: the tied node planes of the
+// loaded axis become one periodic plane with a displacement jump, the
+// unknowns are the unique solid nodes, and the operator is applied
+// matrix-free from per-material cube matrices (lsm_cube.h).  Precisions:
+//   PS_LSM_F64    FP64 CG;
+//   PS_LSM_MIXED  FP32 CG inside FP64 iterative refinement: the residual,
+//                 dot products and solution update are FP64, the inner
+//                 operator products and vectors FP32.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "lsm_cube.h"
+#include "lsm_kernels.cuh"
+#include "ps_common.h"
+
+namespace ps {
+namespace {
+
+using lsm::LsmGeom;
+
+constexpr int kBlk = 256;
+
+struct Springs {
+  ps_lsm_params p{};
+  int nx = 0, ny = 0, nz = 0, nvox = 0, pa = 0, jc = 0;
+  long long nnode = 0, ncube = 0, ns_ref = 0;
+  std::vector<uint8_t> mat, node;
+  cudaStream_t stream = nullptr;
+  uint8_t *d_mat = nullptr, *d_node = nullptr;
+  double *d_K64 = nullptr, *d_S64 = nullptr;  // per-material cube matrices of this handle
+  float* d_K32 = nullptr;
+  // FP64 vectors (3*nvox each)
+  double *b = nullptr, *x = nullptr, *r = nullptr, *p64 = nullptr, *q64 = nullptr;
+  // FP32 inner vectors
+  float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  double *part = nullptr, *scal = nullptr;
+  int nblk = 0;
+  bool solved = false;
+  ps_lsm_result last{};
+  long long dev_bytes = 0;
+
+  LsmGeom geom() const { return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_K32, d_S64}; }
+};
+
+void free_springs(Springs* S)
+{
+  if (!S) return;
+  cudaFree(S->d_mat);
+  cudaFree(S->d_node);
+  cudaFree(S->d_K64);
+  cudaFree(S->d_K32);
+  cudaFree(S->d_S64);
+  cudaFree(S->b);
+  cudaFree(S->x);
+  cudaFree(S->r);
+  cudaFree(S->p64);
+  cudaFree(S->q64);
+  cudaFree(S->x32);
+  cudaFree(S->r32);
+  cudaFree(S->p32);
+  cudaFree(S->q32);
+  cudaFree(S->part);
+  cudaFree(S->scal);
+  if (S->stream) cudaStreamDestroy(S->stream);
+  delete S;
+}
+
+template <typename T>
+int dalloc(Springs* S, T** p, size_t bytes)
+{
+  cudaError_t e = cudaMalloc((void**)p, bytes > 0 ? bytes : 16);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  S->dev_bytes += (long long)bytes;
+  return PS_OK;
+}
+
+// ---- small device helpers -------------------------------------------------
+__global__ void k_masked_sum3(int nv, const uint8_t* node, const double* u, double* part)
+{
+  __shared__ double red[3][kBlk / 32];
+  const int v = blockIdx.x * kBlk + threadIdx.x;
+  double s[3] = {0.0, 0.0, 0.0};
+  if (v < nv && node[v])
+    for (int c = 0; c < 3; c++) s[c] = u[c * nv + v];
+  for (int c = 0; c < 3; c++) {
+    double t = s[c];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[c][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int w = 0; w < kBlk / 32; w++) t += red[threadIdx.x][w];
+    part[blockIdx.x * 3 + threadIdx.x] = t;
+  }
+}
+__global__ void k_sum3(const double* part, int n, double inv_count, double* out)
+{
+  if (threadIdx.x >= 3) return;
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s += part[3 * i + threadIdx.x];
+  out[threadIdx.x] = s * inv_count;
+}
+// u -= mean on existing nodes (removes the rigid translation component)
+__global__ void k_sub_mean(int nv, const uint8_t* node, const double* mean, double* u)
+{
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv || !node[v]) return;
+  for (int c = 0; c < 3; c++) u[c * nv + v] -= mean[c];
+}
+__global__ void k_axpy_res(int n3, const double* b, const double* q, double* r, double* part)
+{
+  __shared__ double red[kBlk / 32];
+  const int i = blockIdx.x * kBlk + threadIdx.x;
+  double t = 0.0;
+  if (i < n3) {
+    const double ri = b[i] - q[i];
+    r[i] = ri;
+    t = ri * ri;
+  }
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kBlk / 32; w++) s += red[w];
+    part[blockIdx.x] = s;
+  }
+}
+__global__ void k_sq_norm(int n3, const double* r, double* part)
+{
+  __shared__ double red[kBlk / 32];
+  const int i = blockIdx.x * kBlk + threadIdx.x;
+  double t = i < n3 ? r[i] * r[i] : 0.0;
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kBlk / 32; w++) s += red[w];
+    part[blockIdx.x] = s;
+  }
+}
+// inner start: r32 = r64 * s, p32 = r32, x32 = 0
+__global__ void k_ir_start(int n3, double s, const double* r64, float* r32, float* p32, float* x32)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  const float v = (float)(r64[i] * s);
+  r32[i] = v;
+  p32[i] = v;
+  x32[i] = 0.f;
+}
+// refinement update x64 += s * x32
+__global__ void k_ir_update(int n3, double s, const float* x32, double* x)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  x[i] += s * (double)x32[i];
+}
+__global__ void k_set_scal(double* scal, double rr, double bb)
+{
+  scal[0] = rr;
+  scal[5] = bb;
+  scal[6] = 0.0;
+  scal[7] = 0.0;
+}
+
+int blocks_for(long long n) { return (int)((n + kBlk - 1) / kBlk); }
+
+// ---- host-side solve ---------------------------------------------------------
+int sum_parts(Springs* S, int n, double* d_out)
+{
+  lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, n, d_out);
+  return cudaGetLastError() == cudaSuccess ? PS_OK : cuda_fail(cudaGetLastError(), "k_sum");
+}
+
+int project_mean(Springs* S, double* u)
+{
+  const int nb = blocks_for(S->nvox);
+  k_masked_sum3<<<nb, kBlk, 0, S->stream>>>(S->nvox, S->d_node, u, S->part);
+  k_sum3<<<1, 32, 0, S->stream>>>(S->part, nb, 1.0 / (double)std::max(1LL, S->nnode), S->scal + 8);
+  k_sub_mean<<<nb, kBlk, 0, S->stream>>>(S->nvox, S->d_node, S->scal + 8, u);
+  PS_CUDA(cudaGetLastError());
+  return PS_OK;
+}
+
+int read_scal(Springs* S, double* h, int n)
+{
+  PS_CUDA(cudaMemcpyAsync(h, S->scal, sizeof(double) * n, cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  return PS_OK;
+}
+
+// CG on A x = r0 from x = 0 (T = double: x,r,p,q are the FP64 vectors; T =
+// float: the FP32 inner vectors).  Stops at |r| <= tol |r0| or maxit.
+// Returns iterations in *its and the final |r|^2 / |r0|^2 in *rel2.
+template <typename T>
+int cg(Springs* S, T* x, T* r, T* p, T* q, double tol, long long maxit, long long* its, double* rel2)
+{
+  const int n3 = 3 * S->nvox;
+  const int nb = blocks_for(S->nvox), nb3 = blocks_for(n3);
+  const LsmGeom G = S->geom();
+  // |r0|^2 (x = 0 and p = r0 set by the caller)
+  lsm::k_sq_norm_t<T, kBlk><<<nb3, kBlk, 0, S->stream>>>(n3, r, S->part);
+  if (int e = sum_parts(S, nb3, S->scal + 0)) return e;
+  double h[8];
+  if (int e = read_scal(S, h, 1)) return e;
+  const double rr0 = h[0];
+  k_set_scal<<<1, 1, 0, S->stream>>>(S->scal, rr0, rr0);
+  PS_CUDA(cudaGetLastError());
+  long long it = 0;
+  const double tol2 = tol * tol;
+  const int batch = 16;
+  bool done = rr0 == 0.0;
+  while (!done && it < maxit) {
+    for (int k = 0; k < batch; k++) {
+      lsm::k_lsm_matvec<T, kBlk><<<nb, kBlk, 0, S->stream>>>(G, p, q, S->part);
+      lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, nb, S->scal + 1);
+      lsm::k_cg_alpha<<<1, 1, 0, S->stream>>>(S->scal, tol2);
+      lsm::k_cg_xr<T, kBlk><<<nb3, kBlk, 0, S->stream>>>(n3, S->scal, x, r, p, q, S->part);
+      lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, nb3, S->scal + 4);
+      lsm::k_cg_beta<<<1, 1, 0, S->stream>>>(S->scal);
+      lsm::k_cg_p<T><<<nb3, kBlk, 0, S->stream>>>(n3, S->scal, r, p);
+    }
+    PS_CUDA(cudaGetLastError());
+    if (int e = read_scal(S, h, 7)) return e;
+    done = h[6] > 0.0;
+    it += batch;
+  }
+  if (int e = read_scal(S, h, 8)) return e;
+  *its = (long long)h[7];
+  *rel2 = rr0 > 0 ? h[0] / rr0 : 0.0;
+  return PS_OK;
+}
+
+int residual(Springs* S, double* rnorm2)
+{
+  const int n3 = 3 * S->nvox;
+  const int nb = blocks_for(S->nvox), nb3 = blocks_for(n3);
+  lsm::k_lsm_matvec<double, kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
+  k_axpy_res<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->q64, S->r, S->part);
+  PS_CUDA(cudaGetLastError());
+  if (int e = project_mean(S, S->r)) return e;
+  k_sq_norm<<<nb3, kBlk, 0, S->stream>>>(n3, S->r, S->part);
+  if (int e = sum_parts(S, nb3, S->scal + 16)) return e;
+  PS_CUDA(cudaMemcpyAsync(rnorm2, S->scal + 16, sizeof(double), cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  return PS_OK;
+}
+
+int compute_stress(Springs* S, ps_lsm_result* out)
+{
+  const int nb = blocks_for(S->nvox);
+  const double jump = 2.0 * S->p.gstrain;
+  lsm::k_lsm_stress<kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->pa, S->jc, jump, S->x, S->part);
+  PS_CUDA(cudaGetLastError());
+  std::vector<double> h((size_t)nb * 9);
+  PS_CUDA(cudaMemcpyAsync(h.data(), S->part, sizeof(double) * 9 * nb, cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  double sig[9] = {0};
+  for (int b = 0; b < nb; b++)
+    for (int i = 0; i < 9; i++) sig[i] += h[(size_t)b * 9 + i];
+  for (int i = 0; i < 9; i++) out->sigma[i] = sig[i];
+  const double vcell = (double)S->nx * S->ny * S->nz;
+  const double nax = S->pa == 0 ? S->nx : S->ny;
+  const double s = S->pa == 0 ? sig[0] : sig[5];  // asigmap(1,1) or asigmap(2,3)
+  out->strain = jump / nax;
+  out->modulus = s / (vcell * jump / nax);
+  return PS_OK;
+}
+
+}  // namespace
+}  // namespace ps
+
+using namespace ps;
+
+extern "C" {
+
+int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_t ny, int32_t nz, void** handle)
+{
+  if (!p || !ind || !handle) return fail(PS_ERR_ARG, "ps_lsm_create: null argument");
+  *handle = nullptr;
+  if (nx < 2 || ny < 2 || nz < 2) return fail(PS_ERR_ARG, "ps_lsm_create: box %d x %d x %d too small", nx, ny, nz);
+  if ((long long)nx * ny * nz * 3 > (1LL << 31) - 1) return fail(PS_ERR_ARG, "ps_lsm_create: box too large");
+  if (p->load != PS_LOAD_XSTRETCH && p->load != PS_LOAD_YZSHEAR) return fail(PS_ERR_ARG, "ps_lsm_create: bad load %d", p->load);
+  if (p->precision != PS_LSM_F64 && p->precision != PS_LSM_MIXED)
+    return fail(PS_ERR_ARG, "ps_lsm_create: bad precision %d", p->precision);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PS_ERR_NODEVICE, "ps_lsm_create: no CUDA device");
+  std::unique_ptr<Springs, void (*)(Springs*)> S(new Springs, free_springs);
+  S->p = *p;
+  S->nx = nx;
+  S->ny = ny;
+  S->nz = nz;
+  S->nvox = nx * ny * nz;
+  S->pa = p->load == PS_LOAD_XSTRETCH ? 0 : 1;
+  S->jc = p->load == PS_LOAD_XSTRETCH ? 0 : 2;
+  const int nv = S->nvox;
+  S->mat.assign(nv, 0);
+  S->node.assign(nv, 0);
+  for (int v = 0; v < nv; v++) S->mat[v] = ind[v] == 0 ? 1 : (ind[v] == 3 ? 2 : 0);
+  long long nn = 0, nc = 0;
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        const int v = x + nx * (y + ny * z);
+        if (S->mat[v]) nc++;
+        bool solid = false;  // a node exists when one of its 8 cubes is solid
+        for (int e = 0; e < 8 && !solid; e++) {
+          const int cx = (x - (e & 1) + nx) % nx, cy = (y - ((e >> 1) & 1) + ny) % ny, cz = (z - (e >> 2) + nz) % nz;
+          solid = S->mat[cx + nx * (cy + ny * cz)] != 0;
+        }
+        S->node[v] = solid;
+        nn += solid;
+      }
+  S->nnode = nn;
+  S->ncube = nc;
+  // cube matrices, per material
+  static lsm::CubeMatrices M;
+  static bool built = false;
+  if (!built) {
+    lsm::build_cube_matrices(M);
+    built = true;
+  }
+  std::vector<double> K64(2 * 24 * 24), S64(2 * 9 * 24);
+  std::vector<float> K32(2 * 24 * 24);
+  const double al[2] = {p->alf1, p->alf2}, be[2] = {p->bet1, p->bet2};
+  for (int m = 0; m < 2; m++) {
+    for (int i = 0; i < 24; i++)
+      for (int j = 0; j < 24; j++) {
+        K64[(m * 24 + i) * 24 + j] = al[m] * M.Ka[i][j] + be[m] * M.Kb[i][j];
+        K32[(m * 24 + i) * 24 + j] = (float)K64[(m * 24 + i) * 24 + j];
+      }
+    for (int i = 0; i < 9; i++)
+      for (int j = 0; j < 24; j++) S64[(m * 9 + i) * 24 + j] = al[m] * M.Sa[i][j] + be[m] * M.Sb[i][j];
+  }
+  PS_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  S->nblk = blocks_for(3LL * nv);
+  if (int r = dalloc(S.get(), &S->d_mat, nv)) return r;
+  if (int r = dalloc(S.get(), &S->d_node, nv)) return r;
+  PS_CUDA(cudaMemcpyAsync(S->d_mat, S->mat.data(), nv, cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaMemcpyAsync(S->d_node, S->node.data(), nv, cudaMemcpyHostToDevice, S->stream));
+  const size_t b64 = sizeof(double) * 3 * (size_t)nv, b32 = sizeof(float) * 3 * (size_t)nv;
+  for (double** v : {&S->b, &S->x, &S->r, &S->p64, &S->q64})
+    if (int r = dalloc(S.get(), v, b64)) return r;
+  if (p->precision == PS_LSM_MIXED)
+    for (float** v : {&S->x32, &S->r32, &S->p32, &S->q32})
+      if (int r = dalloc(S.get(), v, b32)) return r;
+  if (int r = dalloc(S.get(), &S->part, sizeof(double) * 9 * (size_t)(S->nblk + 1))) return r;
+  if (int r = dalloc(S.get(), &S->scal, sizeof(double) * 32)) return r;
+  PS_CUDA(cudaMemsetAsync(S->scal, 0, sizeof(double) * 32, S->stream));
+  if (int r = dalloc(S.get(), &S->d_K64, sizeof(double) * K64.size())) return r;
+  if (int r = dalloc(S.get(), &S->d_K32, sizeof(float) * K32.size())) return r;
+  if (int r = dalloc(S.get(), &S->d_S64, sizeof(double) * S64.size())) return r;
+  PS_CUDA(cudaMemcpyAsync(S->d_K64, K64.data(), sizeof(double) * K64.size(), cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaMemcpyAsync(S->d_K32, K32.data(), sizeof(float) * K32.size(), cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaMemcpyAsync(S->d_S64, S64.data(), sizeof(double) * S64.size(), cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  *handle = S.release();
+  return PS_OK;
+}
+
+int ps_lsm_destroy(void* h)
+{
+  if (!h) return PS_OK;
+  Springs* S = static_cast<Springs*>(h);
+  if (S->stream) cudaStreamSynchronize(S->stream);
+  free_springs(S);
+  return PS_OK;
+}
+
+int ps_lsm_get_info(void* h, ps_lsm_info* o)
+{
+  if (!h || !o) return fail(PS_ERR_ARG, "ps_lsm_get_info: null argument");
+  Springs* S = static_cast<Springs*>(h);
+  memset(o, 0, sizeof *o);
+  o->nnode = S->nnode;
+  o->ncube = S->ncube;
+  o->nvox = S->nvox;
+  o->nx = S->nx;
+  o->ny = S->ny;
+  o->nz = S->nz;
+  o->load = S->p.load;
+  o->precision = S->p.precision;
+  o->device_bytes = S->dev_bytes;
+  return PS_OK;
+}
+
+int ps_lsm_solve(void* h, double rtol, int32_t maxit, ps_lsm_result* out)
+{
+  if (!h || !out) return fail(PS_ERR_ARG, "ps_lsm_solve: null argument");
+  if (!(rtol > 0.0) || maxit < 1) return fail(PS_ERR_ARG, "ps_lsm_solve: need rtol > 0 and maxit >= 1");
+  Springs* S = static_cast<Springs*>(h);
+  memset(out, 0, sizeof *out);
+  const int nv = S->nvox, n3 = 3 * nv;
+  const int nb = blocks_for(nv), nb3 = blocks_for(n3);
+  const LsmGeom G = S->geom();
+  // right-hand side of the tied system, without its translation component
+  lsm::k_lsm_rhs<<<nb, kBlk, 0, S->stream>>>(G, S->pa, S->jc, 2.0 * S->p.gstrain, S->b);
+  PS_CUDA(cudaGetLastError());
+  if (int e = project_mean(S, S->b)) return e;
+  k_sq_norm<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->part);
+  if (int e = sum_parts(S, nb3, S->scal + 17)) return e;
+  double bb = 0.0;
+  PS_CUDA(cudaMemcpyAsync(&bb, S->scal + 17, sizeof(double), cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaMemsetAsync(S->x, 0, sizeof(double) * n3, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  long long iters = 0, inner = 0;
+  double rel = 0.0;
+  int refinements = 0;
+  if (S->p.precision == PS_LSM_F64) {
+    PS_CUDA(cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream));
+    PS_CUDA(cudaMemcpyAsync(S->p64, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream));
+    double rel2 = 0.0;
+    if (int e = cg<double>(S, S->x, S->r, S->p64, S->q64, rtol, maxit, &iters, &rel2)) return e;
+    inner = iters;
+  } else {
+    // FP64 iterative refinement around FP32 CG
+    const double inner_tol = 1e-4;
+    long long budget = maxit;
+    for (refinements = 0; refinements < 60; refinements++) {
+      double rn2 = 0.0;
+      if (refinements == 0) {
+        PS_CUDA(cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream));
+        rn2 = bb;
+      } else if (int e = residual(S, &rn2)) {
+        return e;
+      }
+      if (!(bb > 0.0) || rn2 <= rtol * rtol * bb || budget <= 0) break;
+      const double rn = std::sqrt(rn2);
+      k_ir_start<<<nb3, kBlk, 0, S->stream>>>(n3, 1.0 / rn, S->r, S->r32, S->p32, S->x32);
+      PS_CUDA(cudaGetLastError());
+      long long it = 0;
+      double rel2 = 0.0;
+      if (int e = cg<float>(S, S->x32, S->r32, S->p32, S->q32, inner_tol, budget, &it, &rel2)) return e;
+      inner += it;
+      budget -= it;
+      k_ir_update<<<nb3, kBlk, 0, S->stream>>>(n3, rn, S->x32, S->x);
+      PS_CUDA(cudaGetLastError());
+      iters++;
+    }
+  }
+  // true FP64 residual of the final solution
+  double rn2 = 0.0;
+  if (int e = residual(S, &rn2)) return e;
+  rel = bb > 0.0 ? std::sqrt(rn2 / bb) : 0.0;
+  out->iterations = iters;
+  out->inner_iterations = inner;
+  out->refinements = refinements;
+  out->relres = rel;
+  out->converged = rel <= rtol * 1.0000001 ? 1 : 0;
+  out->nnode = S->nnode;
+  out->ncube = S->ncube;
+  if (int e = compute_stress(S, out)) return e;
+  S->solved = true;
+  S->last = *out;
+  return out->converged ? PS_OK : fail(PS_ERR_NOTCONV, "ps_lsm_solve: relative residual %.3e above %.3e", rel, rtol);
+}
+
+int ps_lsm_get_disp(void* h, double* u)
+{
+  if (!h || !u) return fail(PS_ERR_ARG, "ps_lsm_get_disp: null argument");
+  Springs* S = static_cast<Springs*>(h);
+  if (!S->solved) return fail(PS_ERR_STATE, "ps_lsm_get_disp: no solution yet");
+  const int nv = S->nvox;
+  std::vector<double> x((size_t)3 * nv);
+  PS_CUDA(cudaMemcpyAsync(x.data(), S->x, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  // reference node order: k-j-i over the padded node grid, the loaded axis
+  // having node planes 1..N+1 (plane N+1 = plane 1 + jump)
+  const int M[3] = {S->nx + (S->pa == 0 ? 1 : 0), S->ny + (S->pa == 1 ? 1 : 0), S->nz};
+  const int n3[3] = {S->nx, S->ny, S->nz};
+  long long k = 0;
+  for (int z = 0; z < M[2]; z++)
+    for (int y = 0; y < M[1]; y++)
+      for (int xx = 0; xx < M[0]; xx++) {
+        const int c[3] = {xx, y, z};
+        int w[3];
+        for (int d = 0; d < 3; d++) w[d] = c[d] % n3[d];
+        const int v = w[0] + S->nx * (w[1] + S->ny * w[2]);
+        // the reference's node exists when one of its cubes is solid, cubes
+        // beyond the ends of the loaded axis being pore (no wrap there)
+        bool exists = false;
+        for (int e = 0; e < 8 && !exists; e++) {
+          int cc[3];
+          bool ok = true;
+          for (int d = 0; d < 3; d++) {
+            cc[d] = c[d] - ((e >> d) & 1);
+            if (d == S->pa) ok = ok && cc[d] >= 0 && cc[d] < n3[d];
+            else cc[d] = (cc[d] + n3[d]) % n3[d];
+          }
+          exists = ok && S->mat[cc[0] + S->nx * (cc[1] + S->ny * cc[2])] != 0;
+        }
+        if (!exists) continue;
+        const bool dup = c[S->pa] == n3[S->pa];
+        for (int d = 0; d < 3; d++) u[3 * k + d] = x[(size_t)d * nv + v] + (dup && d == S->jc ? 2.0 * S->p.gstrain : 0.0);
+        k++;
+      }
+  return PS_OK;
+}
+
+void* ps_lsm_stream(void* h) { return h ? (void*)static_cast<Springs*>(h)->stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,260 @@
+// lsm_kernels.cuh -- device side of the lattice-spring static solve.
+//
+// Layout in HBM: the unique solid nodes live on the nx*ny*nz node box (the
+// reference's duplicate node plane N+1 of the loaded axis is the box's plane
+// 0 plus the displacement jump), displacement components as three planes
+// u[c*nvox + v] (structure of arrays), v = x + nx*(y + ny*z).  mat[v] is the
+// material of the voxel cube whose low corner is node v (0 pore, 1 or 2).
+// The stiffness operator is applied matrix-free: each node gathers the
+// rows of its corner from the (at most 8) solid cubes around it; nodes
+// outside the solid return 0.  Nothing is scattered, so the product is
+// deterministic and needs no atomics.
+#pragma once
+#include <stdint.h>
+
+namespace ps {
+namespace lsm {
+
+struct LsmGeom {
+  int nx, ny, nz, nvox;
+  const uint8_t* mat;   // cube material per voxel (0 pore)
+  const uint8_t* node;  // 1 where the node exists
+  const double* K64;    // per-material cube stiffness [2][24][24]
+  const float* K32;
+  const double* S64;    // per-material cube stress rows [2][9][24]
+};
+
+template <typename T>
+__device__ __forceinline__ T kval(const LsmGeom& G, int m, int r, int c);
+template <>
+__device__ __forceinline__ double kval<double>(const LsmGeom& G, int m, int r, int c)
+{
+  return __ldg(G.K64 + (m * 24 + r) * 24 + c);
+}
+template <>
+__device__ __forceinline__ float kval<float>(const LsmGeom& G, int m, int r, int c)
+{
+  return __ldg(G.K32 + (m * 24 + r) * 24 + c);
+}
+
+__device__ __forceinline__ int wrap_add(int c, int d, int n) { return c + d < 0 ? c + d + n : (c + d >= n ? c + d - n : c + d); }
+
+// q = A p on every node, with the FP64 partial sums of p.q per block
+// (dot[blockIdx]).  T = storage / arithmetic type of p and q.
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __restrict__ p, T* __restrict__ q,
+                                                    double* __restrict__ dot)
+{
+  const int v = blockIdx.x * BLK + threadIdx.x;
+  double pq = 0.0;
+  if (v < G.nvox) {
+    const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
+    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    T acc[3] = {T(0), T(0), T(0)};
+    if (G.node[v]) {
+      const int xs[3] = {wrap_add(x, -1, nx), x, wrap_add(x, 1, nx)};
+      const int ys[3] = {wrap_add(y, -1, ny), y, wrap_add(y, 1, ny)};
+      const int zs[3] = {wrap_add(z, -1, nz), z, wrap_add(z, 1, nz)};
+#pragma unroll
+      for (int e = 0; e < 8; e++) {  // cube with low corner at node - e; this node is its corner e
+        const int ex = e & 1, ey = (e >> 1) & 1, ez = e >> 2;
+        const int cv = xs[1 - ex] + nx * (ys[1 - ey] + ny * zs[1 - ez]);
+        const int m = G.mat[cv];
+        if (m == 0) continue;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+          if (b == (e ^ 7)) continue;  // no spring couples opposite corners
+          const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
+          const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
+          const T u0 = p[nvb], u1 = p[nv + nvb], u2 = p[2 * nv + nvb];
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+            acc[r] += kval<T>(G, m - 1, 3 * e + r, 3 * b) * u0 + kval<T>(G, m - 1, 3 * e + r, 3 * b + 1) * u1 +
+                      kval<T>(G, m - 1, 3 * e + r, 3 * b + 2) * u2;
+        }
+      }
+      pq = (double)p[v] * (double)acc[0] + (double)p[nv + v] * (double)acc[1] + (double)p[2 * nv + v] * (double)acc[2];
+    }
+    q[v] = acc[0];
+    q[nv + v] = acc[1];
+    q[2 * nv + v] = acc[2];
+  }
+  // block sum of p.q
+  __shared__ double red[BLK / 32];
+  for (int o = 16; o > 0; o >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = pq;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < BLK / 32; w++) s += red[w];
+    dot[blockIdx.x] = s;
+  }
+}
+
+// b = -sum over cubes of K * (jump of the cube's corners): the right-hand
+// side of the tied system.  Cubes whose low corner is on the last plane of
+// the loaded axis see their far corners across the tie, shifted by `jump`
+// in displacement component jc.
+__global__ void k_lsm_rhs(const LsmGeom G, int pa, int jc, double jump, double* __restrict__ b)
+{
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= G.nvox) return;
+  const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
+  const int c3[3] = {v % nx, (v / nx) % ny, v / (nx * ny)};
+  const int n3[3] = {nx, ny, nz};
+  double acc[3] = {0.0, 0.0, 0.0};
+  if (G.node[v]) {
+    for (int e = 0; e < 8; e++) {
+      const int ee[3] = {e & 1, (e >> 1) & 1, e >> 2};
+      int cc[3];
+      for (int d = 0; d < 3; d++) cc[d] = wrap_add(c3[d], -ee[d], n3[d]);
+      const int m = G.mat[cc[0] + nx * (cc[1] + ny * cc[2])];
+      if (m == 0 || cc[pa] != n3[pa] - 1) continue;
+      // corners b with bit pa set sit across the tie
+      for (int b = 0; b < 8; b++) {
+        if (!((b >> pa) & 1)) continue;
+        for (int r = 0; r < 3; r++) acc[r] -= kval<double>(G, m - 1, 3 * e + r, 3 * b + jc) * jump;
+      }
+    }
+  }
+  b[v] = acc[0];
+  b[nv + v] = acc[1];
+  b[2 * nv + v] = acc[2];
+}
+
+// per-block FP64 sums of sigma+ (9 components) over solid cubes at the
+// displacement u (+ the jump across the tie); the strain contribution is
+// not needed for the moduli
+template <int BLK>
+__global__ void __launch_bounds__(BLK) k_lsm_stress(const LsmGeom G, int pa, int jc, double jump,
+                                                    const double* __restrict__ u, double* __restrict__ part)
+{
+  const int v = blockIdx.x * BLK + threadIdx.x;
+  double s[9];
+  for (int i = 0; i < 9; i++) s[i] = 0.0;
+  if (v < G.nvox) {
+    const int m = G.mat[v];
+    if (m) {
+      const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
+      const int c3[3] = {v % nx, (v / nx) % ny, v / (nx * ny)};
+      const int n3[3] = {nx, ny, nz};
+      double ul[24];
+      for (int b = 0; b < 8; b++) {
+        const int bb[3] = {b & 1, (b >> 1) & 1, b >> 2};
+        int w[3];
+        for (int d = 0; d < 3; d++) w[d] = wrap_add(c3[d], bb[d], n3[d]);
+        const int nb = w[0] + nx * (w[1] + ny * w[2]);
+        for (int d = 0; d < 3; d++) ul[3 * b + d] = u[d * nv + nb];
+        if (bb[pa] && c3[pa] == n3[pa] - 1) ul[3 * b + jc] += jump;
+      }
+      for (int r = 0; r < 9; r++) {
+        double a = 0.0;
+        for (int c = 0; c < 24; c++) a += __ldg(G.S64 + ((m - 1) * 9 + r) * 24 + c) * ul[c];
+        s[r] = a;
+      }
+    }
+  }
+  __shared__ double red[9][BLK / 32];
+  for (int i = 0; i < 9; i++) {
+    double t = s[i];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 9) {
+    double t = 0.0;
+    for (int w = 0; w < BLK / 32; w++) t += red[threadIdx.x][w];
+    part[(long long)blockIdx.x * 9 + threadIdx.x] = t;
+  }
+}
+
+// ---- CG vector kernels (device-resident scalars, no host round trips) ----
+// scal[]: 0 rr, 1 pq, 2 alpha, 3 beta, 4 rr_new, 5 bb (|b|^2), 6 done flag
+__global__ void k_sum(const double* __restrict__ part, int n, double* __restrict__ out)
+{
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) t += red[w];
+    *out = t;
+  }
+}
+
+// alpha = rr / pq (0 once converged); scal[7] counts the iterations taken
+__global__ void k_cg_alpha(double* scal, double tol2)
+{
+  const double rr = scal[0], pq = scal[1];
+  const bool done = scal[6] > 0.0 || rr <= tol2 * scal[5] || !(pq > 0.0);
+  scal[6] = done ? 1.0 : 0.0;
+  scal[2] = done ? 0.0 : rr / pq;
+  if (!done) scal[7] += 1.0;
+}
+
+// per-block partial sums of |r|^2
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_sq_norm_t(int n3, const T* __restrict__ r, double* __restrict__ part)
+{
+  const int i = blockIdx.x * BLK + threadIdx.x;
+  double t = i < n3 ? (double)r[i] * (double)r[i] : 0.0;
+  __shared__ double red[BLK / 32];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < BLK / 32; w++) s += red[w];
+    part[blockIdx.x] = s;
+  }
+}
+
+// x += alpha p; r -= alpha q; partial |r|^2
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_cg_xr(int n3, const double* __restrict__ scal, T* __restrict__ x,
+                                               T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
+                                               double* __restrict__ part)
+{
+  const int i = blockIdx.x * BLK + threadIdx.x;
+  const T al = (T)scal[2];
+  double rr = 0.0;
+  if (i < n3) {
+    const T xi = x[i] + al * p[i];
+    const T ri = r[i] - al * q[i];
+    x[i] = xi;
+    r[i] = ri;
+    rr = (double)ri * (double)ri;
+  }
+  __shared__ double red[BLK / 32];
+  for (int o = 16; o > 0; o >>= 1) rr += __shfl_xor_sync(0xffffffffu, rr, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = rr;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < BLK / 32; w++) s += red[w];
+    part[blockIdx.x] = s;
+  }
+}
+
+// beta = rr_new / rr; rr = rr_new
+__global__ void k_cg_beta(double* scal)
+{
+  const double rn = scal[4], ro = scal[0];
+  scal[3] = scal[6] > 0.0 || !(ro > 0.0) ? 0.0 : rn / ro;
+  if (scal[6] == 0.0) scal[0] = rn;
+}
+
+// p = r + beta p (p unchanged once converged)
+template <typename T>
+__global__ void k_cg_p(int n3, const double* __restrict__ scal, const T* __restrict__ r, T* __restrict__ p)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3 || scal[6] > 0.0) return;
+  p[i] = r[i] + (T)scal[3] * p[i];
+}
+
+}  // namespace lsm
+}  // namespace ps
