@@ -187,6 +187,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the FP64/FP32 comparison legs")
     ap.add_argument("--accuracy-steps", type=int, default=0)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default step configuration")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -242,6 +243,9 @@ def main():
         L = Lattice(p, ind, PREC_ID[q])
         nl = L.nl
         L.set_state(fr, fb)
+        if not args.no_autotune:
+            L.autotune(4 if q != "f64" else 2)
+            L.set_state(fr, fb)
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()

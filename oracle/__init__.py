@@ -153,6 +153,8 @@ def _lsm_sigs(L):
         "or_lsm_get_disp": (None, [C.c_void_p, _DP]),
         "or_lsm_set_disp": (None, [C.c_void_p, _DP]),
         "or_lsm_stress": (None, [C.c_void_p, _DP]),
+        "or_lsm_anf": (None, [_DP]),
+        "or_lsm_cube_tables": (None, [_IP, _DP, _IP, _DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -224,3 +226,20 @@ class OracleSprings:
         out = np.zeros(12)
         lib().or_lsm_stress(self._h, _d(out))
         return {"sigma": out[:9].reshape(3, 3), "modulus": out[9], "strain": out[10], "ncube": int(out[11])}
+
+
+def lsm_constant_tables():
+    """(anf[48,9], cube bonds[24,3], sbond[24], cube angles[72,6], abond[72])
+    as derived / generated by the oracle (1-based corner and direction ids)."""
+    L = lib()
+    if not getattr(L, "_lsm_ready", False):
+        _lsm_sigs(L)
+        L._lsm_ready = True
+    anf = np.zeros((48, 9))
+    b = np.zeros((24, 3), np.int32)
+    sb = np.zeros(24)
+    a = np.zeros((72, 6), np.int32)
+    ab = np.zeros(72)
+    L.or_lsm_anf(_d(anf))
+    L.or_lsm_cube_tables(_i(b), _d(sb), _i(a), _d(ab))
+    return anf, b, sb, a, ab

@@ -85,6 +85,10 @@ void or_lsm_set_disp(or_lsm *o, const double *u);
 /* calc_stress XX:1628-1997: out[0..8] = <sigma> (3x3, row major),
  * out[9] = modulus (Exxxx or Eyzyz), out[10] = strain used */
 void or_lsm_stress(const or_lsm *o, double *out);
+/* derived anf(9,48) table (row per angle) and the generated cube-local
+ * bond (24 x 3) / angle (72 x 6) tables with their unit constants */
+void or_lsm_anf(double *out);
+void or_lsm_cube_tables(int32_t *bonds, double *sb, int32_t *angs, double *ab);
 
 #ifdef __cplusplus
 }

@@ -481,6 +481,49 @@ int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres)
   return it;
 }
 
+/* the derived angle table (48 x 9) and the cube-local tables as generated
+ * for calc_stress, for comparison with the reference's literal ones */
+void or_lsm_anf(double *out)
+{
+  or_lsm tmp;
+  memset(&tmp, 0, sizeof tmp);
+  lsm_constants(&tmp);
+  memcpy(out, tmp.anf, sizeof tmp.anf);
+}
+
+void or_lsm_cube_tables(int32_t *bonds, double *sb, int32_t *angs, double *ab)
+{
+  int nb = 0, na = 0;
+  for (int a = 0; a < 8; a++)
+    for (int j = 0; j < 9; j++) {
+      int c[3] = {(a & 1) + IB[j][0], ((a >> 1) & 1) + IB[j][1], ((a >> 2) & 1) + IB[j][2]};
+      if (c[0] < 0 || c[0] > 1 || c[1] < 0 || c[1] > 1 || c[2] < 0 || c[2] > 1) continue;
+      bonds[3 * nb] = a + 1; /* reference corner numbering is 1-based */
+      bonds[3 * nb + 1] = c[0] + 2 * c[1] + 4 * c[2] + 1;
+      bonds[3 * nb + 2] = j + 1;
+      sb[nb] = j < 3 ? 0.25 : 0.5;
+      nb++;
+    }
+  for (int a = 0; a < 8; a++)
+    for (int j = 0; j < 48; j++) {
+      const int *cj = CV[NTA[j][0] - 1], *ck = CV[NTA[j][1] - 1];
+      int p[3] = {a & 1, (a >> 1) & 1, (a >> 2) & 1};
+      int qj[3] = {p[0] + cj[0], p[1] + cj[1], p[2] + cj[2]}, qk[3] = {p[0] + ck[0], p[1] + ck[1], p[2] + ck[2]};
+      int ok = 1;
+      for (int d = 0; d < 3; d++) ok &= qj[d] >= 0 && qj[d] <= 1 && qk[d] >= 0 && qk[d] <= 1;
+      if (!ok) continue;
+      int32_t *r = angs + 6 * na;
+      r[0] = a + 1;
+      r[1] = qj[0] + 2 * qj[1] + 4 * qj[2] + 1;
+      r[2] = qk[0] + 2 * qk[1] + 4 * qk[2] + 1;
+      r[3] = NTA[j][0];
+      r[4] = NTA[j][1];
+      r[5] = j + 1;
+      ab[na] = j >= 24 ? 1.0 : 0.5;
+      na++;
+    }
+}
+
 void or_lsm_get_disp(const or_lsm *o, double *u) { memcpy(u, o->r, sizeof(double) * 3 * o->ns); }
 void or_lsm_set_disp(or_lsm *o, const double *u) { memcpy(o->r, u, sizeof(double) * 3 * o->ns); }
 

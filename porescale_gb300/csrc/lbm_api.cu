@@ -37,16 +37,18 @@ struct Lattice {
   int nx = 0, ny = 0, nz = 0, prec = 0;
   long long nvox = 0, nl = 0, nps = 0, npb2 = 0, npb4 = 0, ns = 0;
   std::vector<int32_t> ind;   // as given
-  std::vector<int32_t> fvox;  // fluid index -> voxel (reference order)
-  std::vector<int32_t> pvox;  // fluid voxels in ascending order (processing order)
+  std::vector<int32_t> fvox;  // reference fluid index -> voxel (i outer, k inner)
+  long long pitch = 0;        // elements per direction array of the compact state
+  int nwords = 0;             // 32-voxel words per row
   LbmConst<double> Kd{};
   LbmConst<float> Kf{};
   // device
   cudaStream_t stream = nullptr;
-  uint32_t* d_mask = nullptr;
-  int32_t* d_fid = nullptr;
-  int32_t* d_fvox = nullptr;
-  int32_t* d_pvox = nullptr;
+  uint32_t* d_coord = nullptr;  // compact node -> packed coordinates
+  uint32_t* d_mask = nullptr;   // compact node -> link and face bits
+  int32_t* d_ref = nullptr;     // compact node -> reference fluid index
+  int32_t* d_rowstart = nullptr;
+  uint2* d_rowbits = nullptr;
   void* d_col = nullptr;  // colour field of the step kernels (R per voxel)
   void* d_pop[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer][component]
   float* d_rho[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
@@ -67,12 +69,15 @@ struct Lattice {
     g.nx = nx;
     g.ny = ny;
     g.nz = nz;
+    g.nwords = nwords;
     g.nvox = nvox;
-    g.mask = d_mask;
-    g.fid = d_fid;
-    g.fvox = d_fvox;
-    g.pvox = d_pvox;
     g.nl = nl;
+    g.pitch = pitch;
+    g.coord = d_coord;
+    g.mask = d_mask;
+    g.ref = d_ref;
+    g.rowstart = d_rowstart;
+    g.rowbits = d_rowbits;
     return g;
   }
   BufDev buf(int b) const
@@ -111,10 +116,11 @@ int dalloc(Lattice* L, T** p, size_t bytes)
 void free_lattice(Lattice* L)
 {
   if (!L) return;
+  cudaFree(L->d_coord);
   cudaFree(L->d_mask);
-  cudaFree(L->d_fid);
-  cudaFree(L->d_fvox);
-  cudaFree(L->d_pvox);
+  cudaFree(L->d_ref);
+  cudaFree(L->d_rowstart);
+  cudaFree(L->d_rowbits);
   cudaFree(L->d_col);
   for (int b = 0; b < 2; b++)
     for (int k = 0; k < 2; k++) {
@@ -194,65 +200,96 @@ void make_constants(Lattice* L)
 
 inline int wrapc(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
 
-// Fluid list (S1:1036-1072, i outer, k inner), link mask and link counts
+// Fluid list (S1:1036-1072, i outer, k inner) for the reference layout of
+// the state; compact node order (ascending voxel index), per-node packed
+// coordinates and link/face mask, row tables, and link counts
 // (S1:1077-1134).  A diagonal link streams only when its target and both
 // axis-intermediate voxels are fluid.
-void build_geometry(Lattice* L, std::vector<uint32_t>& mask, std::vector<int32_t>& fid)
+struct HostGeom {
+  std::vector<uint32_t> coord, mask;
+  std::vector<int32_t> ref, rowstart;
+  std::vector<uint2> rowbits;
+};
+
+void build_geometry(Lattice* L, HostGeom& H)
 {
   const int nx = L->nx, ny = L->ny, nz = L->nz;
   const long long nv = L->nvox;
   const int32_t pore = L->p.iipore;
   auto V = [&](int x, int y, int z) -> long long { return x + (long long)nx * (y + (long long)ny * z); };
-  fid.assign(nv, -1);
+  std::vector<int32_t> fref(nv, -1);  // voxel -> reference fluid index
   L->fvox.clear();
   for (int x = 0; x < nx; x++)
     for (int y = 0; y < ny; y++)
       for (int z = 0; z < nz; z++) {
         const long long v = V(x, y, z);
         if (L->ind[v] == pore) {
-          fid[v] = (int32_t)L->fvox.size();
+          fref[v] = (int32_t)L->fvox.size();
           L->fvox.push_back((int32_t)v);
         }
       }
   L->nl = (long long)L->fvox.size();
-  L->pvox = L->fvox;
-  std::sort(L->pvox.begin(), L->pvox.end());
-  mask.assign(nv, 0u);
-  long long nps = 0, npb2 = 0, npb4 = 0;
-  auto fl = [&](int x, int y, int z) { return fid[V(wrapc(x, nx), wrapc(y, ny), wrapc(z, nz))] >= 0; };
-  for (long long i = 0; i < L->nl; i++) {
-    const long long v = L->fvox[i];
-    const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long long)nx * ny));
-    uint32_t m = kFluidBit;
-    if (x == 0) m |= 1u << (kWrapShift + 0);
-    if (x == nx - 1) m |= 1u << (kWrapShift + 1);
-    if (y == 0) m |= 1u << (kWrapShift + 2);
-    if (y == ny - 1) m |= 1u << (kWrapShift + 3);
-    if (z == 0) m |= 1u << (kWrapShift + 4);
-    if (z == nz - 1) m |= 1u << (kWrapShift + 5);
-    // incoming link d is open when the outgoing link d of x - c_d streams;
-    // by symmetry that is the outgoing link opp(d) of x itself
-    for (int d = 1; d < 19; d++) {
-      const int* c = kC[d];
-      bool stream = fl(x + c[0], y + c[1], z + c[2]);
-      if (stream && d >= 7) stream = fl(x + c[0], y, z) && fl(x, y + c[1], z) && fl(x, y, z + c[2]);
-      if (stream)
-        nps++;
-      else if (d < 7)
-        npb4++;
-      else
-        npb2++;
-      // outgoing d of x is incoming opp(d)... recorded below on the target
+  L->pitch = (L->nl + 63) / 64 * 64;
+  L->nwords = (nx + 31) / 32;
+  const long long nrows = (long long)ny * nz;
+  H.rowstart.assign(nrows + 1, 0);
+  H.rowbits.assign(nrows * L->nwords, make_uint2(0u, 0u));
+  H.coord.clear();
+  H.mask.clear();
+  H.ref.clear();
+  H.coord.reserve(L->nl);
+  H.mask.reserve(L->nl);
+  H.ref.reserve(L->nl);
+  auto fl = [&](int x, int y, int z) { return fref[V(wrapc(x, nx), wrapc(y, ny), wrapc(z, nz))] >= 0; };
+  long long nps = 0, npb2 = 0, npb4 = 0, n = 0;
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++) {
+      const long long row = y + (long long)ny * z;
+      H.rowstart[row] = (int32_t)n;
+      int before = 0;
+      for (int w = 0; w < L->nwords; w++) {
+        uint32_t bits = 0;
+        for (int b = 0; b < 32; b++) {
+          const int x = 32 * w + b;
+          if (x < nx && fref[V(x, y, z)] >= 0) bits |= 1u << b;
+        }
+        H.rowbits[row * L->nwords + w] = make_uint2(bits, (uint32_t)before);
+        before += __builtin_popcount(bits);
+      }
+      for (int x = 0; x < nx; x++) {
+        const long long v = V(x, y, z);
+        if (fref[v] < 0) continue;
+        uint32_t m = 0;
+        if (x == 0) m |= 1u << (kWrapShift + 0);
+        if (x == nx - 1) m |= 1u << (kWrapShift + 1);
+        if (y == 0) m |= 1u << (kWrapShift + 2);
+        if (y == ny - 1) m |= 1u << (kWrapShift + 3);
+        if (z == 0) m |= 1u << (kWrapShift + 4);
+        if (z == nz - 1) m |= 1u << (kWrapShift + 5);
+        for (int d = 1; d < 19; d++) {
+          const int* c = kC[d];
+          // outgoing link d of this node (the reference's ips / ipb tables)
+          bool stream = fl(x + c[0], y + c[1], z + c[2]);
+          if (stream && d >= 7) stream = fl(x + c[0], y, z) && fl(x, y + c[1], z) && fl(x, y, z + c[2]);
+          if (stream)
+            nps++;
+          else if (d < 7)
+            npb4++;
+          else
+            npb2++;
+          // incoming link d: the outgoing link d of x - c_d streams
+          const int sx = x - c[0], sy = y - c[1], sz = z - c[2];
+          bool open = fl(sx, sy, sz);
+          if (open && d >= 7) open = fl(sx + c[0], sy, sz) && fl(sx, sy + c[1], sz) && fl(sx, sy, sz + c[2]);
+          if (open) m |= 1u << (d - 1);
+        }
+        H.coord.push_back((uint32_t)x | ((uint32_t)y << kCoordBits) | ((uint32_t)z << (2 * kCoordBits)));
+        H.mask.push_back(m);
+        H.ref.push_back(fref[v]);
+        n++;
+      }
     }
-    for (int d = 1; d < 19; d++) {
-      const int* c = kC[d];
-      const int sx = x - c[0], sy = y - c[1], sz = z - c[2];
-      bool open = fl(sx, sy, sz);
-      if (open && d >= 7) open = fl(sx + c[0], sy, sz) && fl(sx, sy + c[1], sz) && fl(sx, sy, sz + c[2]);
-      if (open) m |= 1u << (d - 1);
-    }
-    mask[v] = m;
-  }
+  H.rowstart[nrows] = (int32_t)n;
   L->nps = nps;
   L->npb2 = npb2;
   L->npb4 = npb4;
@@ -297,11 +334,14 @@ int ensure_staging(Lattice* L)
 int ensure_fields(Lattice* L)
 {
   if (!L->d_cc) {
-    const size_t b = sizeof(double) * (size_t)L->nvox;
+    const size_t b = sizeof(double) * (size_t)std::max(1LL, L->nl);
     if (int r = dalloc(L, &L->d_rr, b)) return r;
     if (int r = dalloc(L, &L->d_rb, b)) return r;
     if (int r = dalloc(L, &L->d_cf, b)) return r;
-    if (int r = dalloc(L, &L->d_cc, b)) return r;
+    if (int r = dalloc(L, &L->d_cc, sizeof(double) * (size_t)L->nvox)) return r;
+    std::vector<double> w((size_t)L->nvox, L->p.wet);  // non-fluid voxels keep the wetting colour
+    PS_CUDA(cudaMemcpyAsync(L->d_cc, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, L->stream));
+    PS_CUDA(cudaStreamSynchronize(L->stream));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -324,11 +364,44 @@ int launch_steps(Lattice* L, int n)
 {
   for (int s = 0; s < n; s++) {
     LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
-    cudaError_t e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, 0, a);
+    cudaError_t e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, L->zchunk, a);
     if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
     L->cur = 1 - L->cur;
   }
   return PS_OK;
+}
+
+constexpr size_t kMaxFusedSmem = 227 * 1024;
+
+int sm_count()
+{
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+// planes per CTA so that the fused grid holds about `waves` CTAs per SM
+int default_zchunk(const Lattice* L, int ty, int waves = 4)
+{
+  const long long tiles = (L->ny + ty - 1) / ty;
+  const long long want = (long long)waves * sm_count();
+  const long long nch = std::max(1LL, (want + tiles - 1) / tiles);
+  return (int)std::max(4LL, std::min<long long>(L->nz, (L->nz + nch - 1) / nch));
+}
+
+// default step configuration: the fused kernel with the largest row count
+// up to 8 whose shared-memory ring stays under 96 KB, else two launches
+void default_config(Lattice* L)
+{
+  L->tx = 256;
+  L->ty = 0;
+  for (int ty = 8; ty >= 1; ty /= 2)
+    if (lbm_step_smem(L->prec, 256, ty, L->nx) <= 96 * 1024) {
+      L->ty = ty;
+      break;
+    }
+  L->zchunk = L->ty ? default_zchunk(L, L->ty) : 0;
 }
 
 }  // namespace
@@ -338,8 +411,7 @@ cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunc
 {
   return PREC_DISPATCH(lbm_step_launch, prec, tx, ty, zchunk, a);
 }
-int lbm_tiles(int prec, TileCfg* out, int cap) { return PREC_DISPATCH(lbm_tiles, prec, out, cap); }
-size_t lbm_step_smem(int prec, int tx, int ty) { return PREC_DISPATCH(lbm_step_smem, prec, tx, ty); }
+size_t lbm_step_smem(int prec, int tx, int ty, int nx) { return PREC_DISPATCH(lbm_step_smem, prec, tx, ty, nx); }
 
 }  // namespace ps
 
@@ -366,6 +438,8 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   *handle = nullptr;
   if (nx < 1 || ny < 1 || nz < 1) return fail(PS_ERR_ARG, "ps_lbm_create: bad box %d x %d x %d", nx, ny, nz);
   if ((long long)nx * ny * nz > (1LL << 31) - 1) return fail(PS_ERR_ARG, "ps_lbm_create: box too large for int32 voxel ids");
+  if (nx > 1024 || ny > 1024 || nz > 4096)
+    return fail(PS_ERR_ARG, "ps_lbm_create: box %d x %d x %d exceeds 1024 x 1024 x 4096", nx, ny, nz);
   if (precision < 0 || precision > 3) return fail(PS_ERR_ARG, "ps_lbm_create: precision %d not in 0..3", precision);
   if (!(p->dt > 0.0) || !(p->rb0 != 0.0)) return fail(PS_ERR_ARG, "ps_lbm_create: dt must be > 0 and rb0 != 0");
   if (p->idir < 1 || p->idir > 3) return fail(PS_ERR_ARG, "ps_lbm_create: idir %d not in 1..3", p->idir);
@@ -379,23 +453,24 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   L->prec = precision;
   L->nvox = (long long)nx * ny * nz;
   L->ind.assign(ind, ind + L->nvox);
-  std::vector<uint32_t> mask;
-  std::vector<int32_t> fid;
-  build_geometry(L.get(), mask, fid);
+  HostGeom H;
+  build_geometry(L.get(), H);
   lsm_node_numbers(L.get(), &L->ns);
   make_constants(L.get());
   PS_CUDA(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
-  const size_t nv = (size_t)L->nvox;
-  if (int r = dalloc(L.get(), &L->d_mask, sizeof(uint32_t) * nv)) return r;
-  if (int r = dalloc(L.get(), &L->d_fid, sizeof(int32_t) * nv)) return r;
-  if (int r = dalloc(L.get(), &L->d_fvox, sizeof(int32_t) * std::max<size_t>(1, L->fvox.size()))) return r;
-  PS_CUDA(cudaMemcpyAsync(L->d_mask, mask.data(), sizeof(uint32_t) * nv, cudaMemcpyHostToDevice, L->stream));
-  PS_CUDA(cudaMemcpyAsync(L->d_fid, fid.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice, L->stream));
-  if (int r = dalloc(L.get(), &L->d_pvox, sizeof(int32_t) * std::max<size_t>(1, L->pvox.size()))) return r;
-  if (!L->fvox.empty()) {
-    PS_CUDA(cudaMemcpyAsync(L->d_fvox, L->fvox.data(), sizeof(int32_t) * L->fvox.size(), cudaMemcpyHostToDevice, L->stream));
-    PS_CUDA(cudaMemcpyAsync(L->d_pvox, L->pvox.data(), sizeof(int32_t) * L->pvox.size(), cudaMemcpyHostToDevice, L->stream));
+  const size_t nv = (size_t)L->nvox, nlc = (size_t)std::max(1LL, L->nl);
+  if (int r = dalloc(L.get(), &L->d_coord, sizeof(uint32_t) * nlc)) return r;
+  if (int r = dalloc(L.get(), &L->d_mask, sizeof(uint32_t) * nlc)) return r;
+  if (int r = dalloc(L.get(), &L->d_ref, sizeof(int32_t) * nlc)) return r;
+  if (int r = dalloc(L.get(), &L->d_rowstart, sizeof(int32_t) * H.rowstart.size())) return r;
+  if (int r = dalloc(L.get(), &L->d_rowbits, sizeof(uint2) * H.rowbits.size())) return r;
+  if (L->nl > 0) {
+    PS_CUDA(cudaMemcpyAsync(L->d_coord, H.coord.data(), sizeof(uint32_t) * L->nl, cudaMemcpyHostToDevice, L->stream));
+    PS_CUDA(cudaMemcpyAsync(L->d_mask, H.mask.data(), sizeof(uint32_t) * L->nl, cudaMemcpyHostToDevice, L->stream));
+    PS_CUDA(cudaMemcpyAsync(L->d_ref, H.ref.data(), sizeof(int32_t) * L->nl, cudaMemcpyHostToDevice, L->stream));
   }
+  PS_CUDA(cudaMemcpyAsync(L->d_rowstart, H.rowstart.data(), sizeof(int32_t) * H.rowstart.size(), cudaMemcpyHostToDevice, L->stream));
+  PS_CUDA(cudaMemcpyAsync(L->d_rowbits, H.rowbits.data(), sizeof(uint2) * H.rowbits.size(), cudaMemcpyHostToDevice, L->stream));
   // colour field: the wetting colour everywhere; fluid voxels are rewritten
   // by every step before they are read
   {
@@ -411,21 +486,20 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
       PS_CUDA(cudaStreamSynchronize(L->stream));
     }
   }
-  const size_t popb = L->elem() * 19 * nv;
+  const size_t pitch = (size_t)std::max(64LL, L->pitch);
+  const size_t popb = L->elem() * 19 * pitch;
   for (int b = 0; b < 2; b++)
     for (int k = 0; k < 2; k++) {
       if (int r = dalloc(L.get(), &L->d_pop[b][k], popb)) return r;
       PS_CUDA(cudaMemsetAsync(L->d_pop[b][k], 0, popb, L->stream));
       if (precision >= 2) {
-        if (int r = dalloc(L.get(), &L->d_rho[b][k], sizeof(float) * nv)) return r;
-        PS_CUDA(cudaMemsetAsync(L->d_rho[b][k], 0, sizeof(float) * nv, L->stream));
+        if (int r = dalloc(L.get(), &L->d_rho[b][k], sizeof(float) * pitch)) return r;
+        PS_CUDA(cudaMemsetAsync(L->d_rho[b][k], 0, sizeof(float) * pitch, L->stream));
       }
     }
   if (int r = dalloc(L.get(), &L->d_Kd, sizeof(LbmConst<double>))) return r;
   PS_CUDA(cudaMemcpyAsync(L->d_Kd, &L->Kd, sizeof(LbmConst<double>), cudaMemcpyHostToDevice, L->stream));
-  L->tx = 128;
-  L->ty = 256;
-  L->zchunk = 0;
+  default_config(L.get());
   PS_CUDA(cudaStreamSynchronize(L->stream));
   *handle = L.release();
   return PS_OK;
@@ -664,15 +738,12 @@ int ps_lbm_fields(void* h, double* rr, double* rb, double* cf)
   LbmLaunchArgs a = L->args(L->cur, L->cur);
   cudaError_t e = PREC_DISPATCH(lbm_fields_launch, L->prec, a, L->d_rr, L->d_rb, L->d_cf, L->d_cc);
   if (e != cudaSuccess) return cuda_fail(e, "fields kernel");
-  std::vector<double> buf((size_t)L->nvox);
   double* outs[3] = {rr, rb, cf};
   double* srcs[3] = {L->d_rr, L->d_rb, L->d_cf};
-  for (int q = 0; q < 3; q++) {
-    if (!outs[q]) continue;
-    PS_CUDA(cudaMemcpyAsync(buf.data(), srcs[q], sizeof(double) * L->nvox, cudaMemcpyDeviceToHost, L->stream));
-    PS_CUDA(cudaStreamSynchronize(L->stream));
-    for (long long i = 0; i < L->nl; i++) outs[q][i] = buf[L->fvox[i]];
-  }
+  for (int q = 0; q < 3; q++)
+    if (outs[q] && L->nl > 0)
+      PS_CUDA(cudaMemcpyAsync(outs[q], srcs[q], sizeof(double) * L->nl, cudaMemcpyDeviceToHost, L->stream));
+  PS_CUDA(cudaStreamSynchronize(L->stream));
   return PS_OK;
 }
 
@@ -689,11 +760,14 @@ int ps_lbm_set_tile(void* h, int32_t tx, int32_t ty, int32_t zchunk)
 {
   if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_tile: null handle");
   Lattice* L = as_lattice(h);
-  if (lbm_step_smem(L->prec, tx, ty) == 0)
-    return fail(PS_ERR_ARG, "ps_lbm_set_tile: blocks %d/%d not compiled for precision %d", tx, ty, L->prec);
-  if (zchunk != 0) return fail(PS_ERR_ARG, "ps_lbm_set_tile: zchunk must be 0 (the step kernels do not march in z)");
+  if (ty < 0 || zchunk < 0) return fail(PS_ERR_ARG, "ps_lbm_set_tile: negative ty or zchunk");
+  const size_t sm = lbm_step_smem(L->prec, tx, ty, L->nx);
+  if (sm == 0) return fail(PS_ERR_ARG, "ps_lbm_set_tile: %d threads per CTA not compiled (128 or 256)", tx);
+  if (sm > kMaxFusedSmem)
+    return fail(PS_ERR_ARG, "ps_lbm_set_tile: %d rows of %d voxels need %zu B of shared memory", ty, L->nx, sm);
   L->tx = tx;
   L->ty = ty;
+  L->zchunk = ty == 0 ? 0 : (zchunk == 0 ? default_zchunk(L, ty) : std::min<int>(zchunk, L->nz));
   return PS_OK;
 }
 
@@ -706,19 +780,29 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   // candidates: every compiled tile x a few z-chunk lengths; the state is
   // advanced an even number of steps per candidate and then restored by
   // re-running from a saved copy of the current buffer
-  const size_t popb = L->elem() * 19 * (size_t)L->nvox;
+  const size_t popb = L->elem() * 19 * (size_t)std::max(64LL, L->pitch);
   void* save[2] = {nullptr, nullptr};
   float* saver[2] = {nullptr, nullptr};
   for (int k = 0; k < 2; k++) {
     PS_CUDA(cudaMalloc(&save[k], popb));
     PS_CUDA(cudaMemcpyAsync(save[k], L->d_pop[L->cur][k], popb, cudaMemcpyDeviceToDevice, L->stream));
     if (L->prec >= 2) {
-      PS_CUDA(cudaMalloc((void**)&saver[k], sizeof(float) * L->nvox));
-      PS_CUDA(cudaMemcpyAsync(saver[k], L->d_rho[L->cur][k], sizeof(float) * L->nvox, cudaMemcpyDeviceToDevice, L->stream));
+      PS_CUDA(cudaMalloc((void**)&saver[k], sizeof(float) * std::max(64LL, L->pitch)));
+      PS_CUDA(cudaMemcpyAsync(saver[k], L->d_rho[L->cur][k], sizeof(float) * std::max(64LL, L->pitch), cudaMemcpyDeviceToDevice, L->stream));
     }
   }
-  TileCfg tiles[16];
-  const int nt = lbm_tiles(L->prec, tiles, 16);
+  struct Cfg {
+    int tx, ty, zc;
+  };
+  std::vector<Cfg> cand;
+  for (int tx : {128, 256}) {
+    cand.push_back({tx, 0, 0});
+    for (int ty : {2, 4, 8, 16}) {
+      if (ty > L->ny || lbm_step_smem(L->prec, tx, ty, L->nx) > 160 * 1024) continue;
+      for (int zc : {4, 8, 16, 32})
+        if (zc <= L->nz) cand.push_back({tx, ty, zc});
+    }
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -726,9 +810,10 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   int btx = L->tx, bty = L->ty, bzc = L->zchunk;
   const int saved_cur = L->cur;
   int rc = PS_OK;
-  for (int i = 0; i < nt && rc == PS_OK; i++) {
-    L->tx = tiles[i].tx;
-    L->ty = tiles[i].ty;
+  for (const Cfg& c : cand) {
+    L->tx = c.tx;
+    L->ty = c.ty;
+    L->zchunk = c.zc;
     rc = launch_steps(L, 2);  // warm-up
     if (rc) break;
     cudaEventRecord(e0, L->stream);
@@ -739,9 +824,9 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
     cudaEventElapsedTime(&ms, e0, e1);
     if (rc == PS_OK && ms < best) {
       best = ms;
-      btx = L->tx;
-      bty = L->ty;
-      bzc = 0;
+      btx = c.tx;
+      bty = c.ty;
+      bzc = c.zc;
     }
   }
   cudaEventDestroy(e0);
@@ -750,7 +835,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   L->cur = saved_cur;
   for (int k = 0; k < 2; k++) {
     cudaMemcpyAsync(L->d_pop[L->cur][k], save[k], popb, cudaMemcpyDeviceToDevice, L->stream);
-    if (saver[k]) cudaMemcpyAsync(L->d_rho[L->cur][k], saver[k], sizeof(float) * L->nvox, cudaMemcpyDeviceToDevice, L->stream);
+    if (saver[k]) cudaMemcpyAsync(L->d_rho[L->cur][k], saver[k], sizeof(float) * std::max(64LL, L->pitch), cudaMemcpyDeviceToDevice, L->stream);
   }
   cudaStreamSynchronize(L->stream);
   for (int k = 0; k < 2; k++) {

@@ -1,29 +1,35 @@
 // lbm_kernels.cuh -- device side of the colour-gradient D3Q19 lattice.
 //
 // Data layout in HBM (one lattice):
-//   * dense box nx*ny*nz, voxel v = x + nx*(y + ny*z);
-//   * populations structure-of-arrays pop[component][direction][v] for the
+//   * fluid nodes only, numbered in ascending voxel order (x fastest, then
+//     y, then z): compact index i.  A warp's 32 consecutive nodes are
+//     consecutive in memory, and the fluid runs of a row stay contiguous, so
+//     nearly every fetched sector is used (a dense box wastes about half of
+//     each sector on the solid voxels between fluid runs);
+//   * populations structure-of-arrays pop[component][direction][i] for the
 //     two components (red, blue), double-buffered (src/dst swap every step);
 //   * the buffers hold POST-COLLISION populations of the previous step, so a
 //     step is a pull: node x reads direction d from x - c_d, or, when that
 //     link is a wall link, its own reflected population opp(d) (half-way
 //     bounce-back).  This is the reference's push streaming (ips) and
 //     bounce-back (ipb2, ipb4) seen from the receiving node;
-//   * mask[v]: bit 31 = fluid node, bit d-1 (d = 1..18) = incoming link d
-//     open (the link from x - c_d is one of the reference's ips entries),
-//     bits 18..23 = node on the low/high x, y, z face of the box (periodic
-//     wrap), so neighbour addresses need no division;
-//   * pvox[i]: the fluid voxels in ascending voxel order -- every thread of
-//     the step kernels owns one fluid node, so no lane idles on solid voxels
-//     and consecutive lanes read consecutive voxels;
-//   * cc[v]: the stencil colour of the current step (wetting colour on
-//     non-fluid voxels, written once at creation);
+//   * coord[i] (x | y<<10 | z<<20) and mask[i]: bit d-1 (d = 1..18) =
+//     incoming link d open (the link from x - c_d is one of the reference's
+//     ips entries), bits 18..23 = node on the low/high x, y, z face of the box;
+//   * row tables: rowstart[row] = compact index of the first fluid voxel of
+//     row (y, z), and per 32-voxel word of the row its fluid bits and the
+//     fluid count before it.  The compact index of fluid voxel (x, y, z) is
+//     rowstart + rank of x in its row -- one L1/L2-resident lookup per
+//     neighbour row, no per-node neighbour table in HBM;
+//   * cc[v]: the stencil colour of the current step on the dense box
+//     (wetting colour on non-fluid voxels, written once at creation), read
+//     27 times per interface node from L1/L2;
 //   * 16-bit storage keeps each population as a deviation from the rest
 //     equilibrium t_d * rho_ref of its own component and node; rho_ref is the
 //     component density of the node at the step that wrote it, stored in
-//     FP32 next to the populations (rho[component][v]).
+//     FP32 next to the populations (rho[component][i]).
 //
-// One step = two launches over the fluid list:
+// One step = two launches over the fluid nodes:
 //   k_lbm_dens  pulls the populations, writes the colour (and for 16-bit
 //               storage the component densities of the new buffer);
 //   k_lbm_coll  pulls again, collides with the 27-point colour stencil and
@@ -69,41 +75,22 @@ __host__ __device__ constexpr int wcls(int d) { return d == 0 ? 0 : (d < 7 ? 1 :
 static_assert(opp(7) == 10 && opp(8) == 9 && opp(11) == 14 && opp(12) == 13, "opposites");
 static_assert(opp(15) == 18 && opp(16) == 17 && opp(1) == 2 && opp(5) == 6, "opposites");
 
-constexpr uint32_t kFluidBit = 1u << 31;
-constexpr int kWrapShift = 18;  // bits 18..23: x==0, x==nx-1, y==0, y==ny-1, z==0, z==nz-1
-
-// voxel-index offsets of the neighbours at -1, 0, +1 along each axis,
-// periodic wrap taken from the mask's face bits
-struct NbOff {
-  int x[3], y[3], z[3];
-};
-__device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int nz)
-{
-  NbOff o;
-  const int ny_nx = nxy;  // nx*ny
-  o.x[0] = (m & (1u << (kWrapShift + 0))) ? nx - 1 : -1;
-  o.x[1] = 0;
-  o.x[2] = (m & (1u << (kWrapShift + 1))) ? 1 - nx : 1;
-  o.y[0] = (m & (1u << (kWrapShift + 2))) ? ny_nx - nx : -nx;
-  o.y[1] = 0;
-  o.y[2] = (m & (1u << (kWrapShift + 3))) ? nx - ny_nx : nx;
-  o.z[0] = (m & (1u << (kWrapShift + 4))) ? (nz - 1) * ny_nx : -ny_nx;
-  o.z[1] = 0;
-  o.z[2] = (m & (1u << (kWrapShift + 5))) ? (1 - nz) * ny_nx : ny_nx;
-  return o;
-}
+constexpr int kWrapShift = 18;  // mask bits 18..23: x==0, x==nx-1, y==0, y==ny-1, z==0, z==nz-1
+constexpr int kCoordBits = 10;  // coord packing: x, y in 10 bits, z in 12
 
 struct GeomDev {
-  int nx, ny, nz;
+  int nx, ny, nz, nwords;  // box; 32-voxel words per row
   long long nvox;
-  const uint32_t* mask;
-  const int32_t* fid;   // voxel -> fluid index (0-based, reference order) or -1
-  const int32_t* fvox;  // fluid index -> voxel (reference order)
-  const int32_t* pvox;  // fluid voxels in ascending voxel order (processing order)
-  long long nl;
+  long long nl;            // fluid nodes
+  long long pitch;         // elements per direction array (>= nl)
+  const uint32_t* coord;   // [nl] packed coordinates
+  const uint32_t* mask;    // [nl] link and face bits
+  const int32_t* ref;      // [nl] reference fluid index (i outer, k inner order)
+  const int32_t* rowstart; // [ny*nz + 1]
+  const uint2* rowbits;    // [ny*nz*nwords] (fluid bits, fluid count before the word)
 };
 
-// one population buffer: pop[k] -> 19*nvox elements, rho[k] -> nvox floats
+// one population buffer: pop[k] -> 19*pitch elements, rho[k] -> pitch floats
 struct BufDev {
   void* pop[2];
   float* rho[2];
@@ -161,95 +148,131 @@ struct Pop {
   using S = Store<PREC>;
   using T = typename S::T;
   using R = typename S::R;
-  // population d of component k stored at voxel v
-  __device__ __forceinline__ static R load(const LbmConst<R>& K, const BufDev& b, int k, int d, long long v,
-                                           long long nvox)
+  // population d of component k stored at compact node i
+  __device__ __forceinline__ static R load(const LbmConst<R>& K, const BufDev& b, int k, int d, int i, long long pitch)
   {
     const T* p = static_cast<const T*>(b.pop[k]);
     if constexpr (S::kDev) {
       const float w = K.t[k][wcls(d)];
-      return w * __ldg(b.rho[k] + v) + to_f(p[(long long)d * nvox + v]) * DevScale<T>::down;
+      return w * __ldg(b.rho[k] + i) + to_f(p[(long long)d * pitch + i]) * DevScale<T>::down;
     } else {
-      return __ldg(p + (long long)d * nvox + v);
+      return __ldg(p + (long long)d * pitch + i);
     }
   }
-  // writes the 19 populations of component k at voxel v; rho = density
-  // the collision used for that component (the deviation reference, which
-  // the density kernel of the same step stored in b.rho[k][v])
-  __device__ __forceinline__ static void store(const LbmConst<R>& K, const BufDev& b, int k, long long v,
-                                               long long nvox, const R* out, R rho)
+  // writes the 19 populations of component k at node i; rho = density the
+  // collision used for that component (the deviation reference, which the
+  // density kernel of the same step stored in b.rho[k][i])
+  __device__ __forceinline__ static void store(const LbmConst<R>& K, const BufDev& b, int k, int i, long long pitch,
+                                               const R* out, R rho)
   {
     T* p = static_cast<T*>(b.pop[k]);
     if constexpr (S::kDev) {
 #pragma unroll
       for (int d = 0; d < 19; d++) {
         const float w = K.t[k][wcls(d)];
-        p[(long long)d * nvox + v] = from_f<T>((out[d] - w * rho) * DevScale<T>::up);
+        p[(long long)d * pitch + i] = from_f<T>((out[d] - w * rho) * DevScale<T>::up);
       }
     } else {
 #pragma unroll
-      for (int d = 0; d < 19; d++) p[(long long)d * nvox + v] = out[d];
+      for (int d = 0; d < 19; d++) p[(long long)d * pitch + i] = out[d];
     }
   }
 };
 
-// wrapped neighbour coordinates: idx 0 = c-1, 1 = c, 2 = c+1
-__device__ __forceinline__ void nb3(int c, int n, int* o)
+// Compact indices of the 18 pull sources x - c_d of node i (src[0] = i).
+// Entries of closed links are unspecified.  Each neighbour row needs one
+// rank lookup that also serves its x-1 and x+1 voxels: the fluid voxel at
+// x-1 has index rank(x) - 1, the one at x+1 has rank(x) + [x fluid].
+struct RowRank {
+  int base;   // rowstart of the row
+  int rank;   // fluid voxels before x in the row
+  int fx;     // 1 when voxel x of the row is fluid
+};
+__device__ __forceinline__ RowRank row_rank(const GeomDev& G, int row, int x)
 {
-  o[0] = c == 0 ? n - 1 : c - 1;
-  o[1] = c;
-  o[2] = c == n - 1 ? 0 : c + 1;
+  const uint2 w = __ldg(G.rowbits + (long long)row * G.nwords + (x >> 5));
+  const int b = x & 31;
+  RowRank r;
+  r.base = __ldg(G.rowstart + row);
+  r.rank = (int)w.y + __popc(w.x & ((1u << b) - 1u));
+  r.fx = (w.x >> b) & 1u;
+  return r;
 }
-
-// Pulls the 19 post-streaming populations of both components at voxel
-// (x,y,z), returns them in f[0..18] (red) and f[19..37] (blue).
-template <int PREC>
-__device__ __forceinline__ void pull_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& src, int x, int y, int z, uint32_t m,
-                                          typename Store<PREC>::R* f)
+__device__ __forceinline__ void pull_sources(const GeomDev& G, int i, uint32_t c, uint32_t m, int* src)
 {
-  int xs[3], ys[3], zs[3];
-  nb3(x, G.nx, xs);
-  nb3(y, G.ny, ys);
-  nb3(z, G.nz, zs);
-  const long long nxl = G.nx, nxy = (long long)G.nx * G.ny;
-  const long long v = x + nxl * y + nxy * z;
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    f[19 * k] = Pop<PREC>::load(K, src, k, 0, v, G.nvox);
-#pragma unroll
-    for (int d = 1; d < 19; d++) {
-      long long vs;
-      int ds;
-      if (m & (1u << (d - 1))) {  // streamed from x - c_d
-        vs = xs[1 - cvx(d)] + nxl * ys[1 - cvy(d)] + nxy * zs[1 - cvz(d)];
-        ds = d;
-      } else {  // reflected at the wall: own population of the opposite direction
-        vs = v;
-        ds = opp(d);
-      }
-      f[19 * k + d] = Pop<PREC>::load(K, src, k, ds, vs, G.nvox);
-    }
+  const int x = c & ((1 << kCoordBits) - 1), y = (c >> kCoordBits) & ((1 << kCoordBits) - 1), z = c >> (2 * kCoordBits);
+  const int ny = G.ny;
+  const int ym = (m & (1u << (kWrapShift + 2))) ? ny - 1 : y - 1;
+  const int yp = (m & (1u << (kWrapShift + 3))) ? 0 : y + 1;
+  const int zm = (m & (1u << (kWrapShift + 4))) ? G.nz - 1 : z - 1;
+  const int zp = (m & (1u << (kWrapShift + 5))) ? 0 : z + 1;
+  const bool x0 = m & (1u << (kWrapShift + 0)), x1 = m & (1u << (kWrapShift + 1));
+  // index of the voxel at x-1 / x / x+1 of a row from its rank at x
+  auto at = [&](const RowRank& r, int row, int dx) -> int {
+    if (dx == 0) return r.base + r.rank;
+    if (dx < 0) return x0 ? __ldg(G.rowstart + row + 1) - 1 : r.base + r.rank - 1;
+    return x1 ? r.base : r.base + r.rank + r.fx;
+  };
+  src[0] = i;
+  {  // own row: x -/+ 1
+    const int row = y + ny * z;
+    src[1] = x0 ? __ldg(G.rowstart + row + 1) - 1 : i - 1;
+    src[2] = x1 ? __ldg(G.rowstart + row) : i + 1;
+  }
+  {  // row (y-1, z): d = 3 (x), 7 (x-1), 8 (x+1)
+    const int row = ym + ny * z;
+    const RowRank r = row_rank(G, row, x);
+    src[3] = at(r, row, 0);
+    src[7] = at(r, row, -1);
+    src[8] = at(r, row, 1);
+  }
+  {  // row (y+1, z): d = 4 (x), 9 (x-1), 10 (x+1)
+    const int row = yp + ny * z;
+    const RowRank r = row_rank(G, row, x);
+    src[4] = at(r, row, 0);
+    src[9] = at(r, row, -1);
+    src[10] = at(r, row, 1);
+  }
+  {  // row (y, z-1): d = 5 (x), 11 (x-1), 12 (x+1)
+    const int row = y + ny * zm;
+    const RowRank r = row_rank(G, row, x);
+    src[5] = at(r, row, 0);
+    src[11] = at(r, row, -1);
+    src[12] = at(r, row, 1);
+  }
+  {  // row (y, z+1): d = 6 (x), 13 (x-1), 14 (x+1)
+    const int row = y + ny * zp;
+    const RowRank r = row_rank(G, row, x);
+    src[6] = at(r, row, 0);
+    src[13] = at(r, row, -1);
+    src[14] = at(r, row, 1);
+  }
+  {  // yz diagonals
+    const RowRank a = row_rank(G, ym + ny * zm, x);
+    src[15] = a.base + a.rank;
+    const RowRank b = row_rank(G, yp + ny * zm, x);
+    src[16] = b.base + b.rank;
+    const RowRank c2 = row_rank(G, ym + ny * zp, x);
+    src[17] = c2.base + c2.rank;
+    const RowRank e = row_rank(G, yp + ny * zp, x);
+    src[18] = e.base + e.rank;
   }
 }
 
-// Pull by voxel index and mask only (32-bit addressing): the step kernels'
-// form of pull_node.
+// Pulls the 19 post-streaming populations of both components of node i:
+// f[0..18] red, f[19..37] blue.
 template <int PREC>
-__device__ __forceinline__ void pull_fast(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& src, int v, uint32_t m, const NbOff& o,
+__device__ __forceinline__ void pull_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, int i, uint32_t m, const int* s,
                                           typename Store<PREC>::R* f)
 {
-  const long long nv = G.nvox;
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    f[19 * k] = Pop<PREC>::load(K, src, k, 0, v, nv);
+    f[19 * k] = Pop<PREC>::load(K, src, k, 0, i, G.pitch);
 #pragma unroll
     for (int d = 1; d < 19; d++) {
       const bool open = m & (1u << (d - 1));
-      const int vs = open ? v + o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : v;
-      const int ds = open ? d : opp(d);
-      f[19 * k + d] = Pop<PREC>::load(K, src, k, ds, vs, nv);
+      f[19 * k + d] = Pop<PREC>::load(K, src, k, open ? d : opp(d), open ? s[d] : i, G.pitch);
     }
   }
 }
@@ -275,6 +298,33 @@ __device__ __forceinline__ R stencil_colour(R rr, R rb, R wet)
   return (cf - wet) + wet;
 }
 
+__device__ __forceinline__ void unpack(uint32_t c, int& x, int& y, int& z)
+{
+  x = c & ((1 << kCoordBits) - 1);
+  y = (c >> kCoordBits) & ((1 << kCoordBits) - 1);
+  z = c >> (2 * kCoordBits);
+}
+
+// dense-box offsets of the -1 / 0 / +1 neighbours along each axis, periodic
+// wrap from the face bits of the mask (for the colour stencil)
+struct NbOff {
+  int x[3], y[3], z[3];
+};
+__device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int nz)
+{
+  NbOff o;
+  o.x[0] = (m & (1u << (kWrapShift + 0))) ? nx - 1 : -1;
+  o.x[1] = 0;
+  o.x[2] = (m & (1u << (kWrapShift + 1))) ? 1 - nx : 1;
+  o.y[0] = (m & (1u << (kWrapShift + 2))) ? nxy - nx : -nx;
+  o.y[1] = 0;
+  o.y[2] = (m & (1u << (kWrapShift + 3))) ? nx - nxy : nx;
+  o.z[0] = (m & (1u << (kWrapShift + 4))) ? (nz - 1) * nxy : -nxy;
+  o.z[1] = 0;
+  o.z[2] = (m & (1u << (kWrapShift + 5))) ? (1 - nz) * nxy : nxy;
+  return o;
+}
+
 // ---- step kernels ---------------------------------------------------------
 // colour (and 16-bit reference densities) of the current step
 template <int PREC, int BLK>
@@ -285,17 +335,19 @@ __global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmCon
   using R = typename Store<PREC>::R;
   const int i = blockIdx.x * BLK + threadIdx.x;
   if (i >= G.nl) return;
-  const int v = __ldg(G.pvox + i);
-  const uint32_t m = __ldg(G.mask + v);
-  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.nz);
+  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+  int s[19];
+  pull_sources(G, i, c, m, s);
   R f[38];
-  pull_fast<PREC>(K, G, src, v, m, o, f);
+  pull_node<PREC>(K, G, src, i, m, s, f);
   R rr, rb;
   densities(f, rr, rb);
-  cc[v] = stencil_colour(rr, rb, K.wet);
+  int x, y, z;
+  unpack(c, x, y, z);
+  cc[x + G.nx * (y + G.ny * z)] = stencil_colour(rr, rb, K.wet);
   if constexpr (Store<PREC>::kDev) {
-    dst.rho[0][v] = rr;
-    dst.rho[1][v] = rb;
+    dst.rho[0][i] = rr;
+    dst.rho[1][i] = rb;
   }
 }
 
@@ -308,46 +360,176 @@ __global__ void __launch_bounds__(BLK) k_lbm_coll(const __grid_constant__ LbmCon
   using R = typename Store<PREC>::R;
   const int i = blockIdx.x * BLK + threadIdx.x;
   if (i >= G.nl) return;
-  const int v = __ldg(G.pvox + i);
-  const uint32_t m = __ldg(G.mask + v);
-  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.nz);
+  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
   R f[38];
-  pull_fast<PREC>(K, G, src, v, m, o, f);
+  {
+    int s[19];
+    pull_sources(G, i, c, m, s);
+    pull_node<PREC>(K, G, src, i, m, s, f);
+  }
   R rr, rb;
   densities(f, rr, rb);
-  auto col = [&](int a, int b, int c) -> R { return cc[v + o.x[a] + o.y[b] + o.z[c]]; };
+  int x, y, z;
+  unpack(c, x, y, z);
+  const int nxy = G.nx * G.ny;
+  const int v = x + G.nx * y + nxy * z;
+  const NbOff o = nb_offsets(m, G.nx, nxy, G.nz);
+  auto col = [&](int a, int b, int e) -> R { return cc[v + o.x[a] + o.y[b] + o.z[e]]; };
   R outr[19], outb[19];
   node_update(K, f, f + 19, rr, rb, col, outr, outb);
-  Pop<PREC>::store(K, dst, 0, v, G.nvox, outr, rr);
-  Pop<PREC>::store(K, dst, 1, v, G.nvox, outb, rb);
+  Pop<PREC>::store(K, dst, 0, i, G.pitch, outr, rr);
+  Pop<PREC>::store(K, dst, 1, i, G.pitch, outb, rb);
+}
+
+// ---- fused step kernel ----------------------------------------------------
+// One launch per step.  A CTA owns TY consecutive full rows (y0..y0+TY-1,
+// all x) and a chunk of z-planes.  For each plane z it first computes the
+// colour of plane z+1 on its rows plus one halo row on each side into a
+// 3-plane ring in shared memory, then collides its nodes of plane z with the
+// 27-point stencil read from the ring.  Each population is read from HBM
+// about once per step (the second pull and the halo rows hit L2), against
+// twice for the two-launch form.  The fluid nodes of a (rows, plane) slab
+// are contiguous compact ranges, so the work is distributed over fluid nodes
+// only.
+template <typename R>
+struct FusedSmem {
+  static size_t bytes(int ty, int nx) { return sizeof(R) * 3 * (size_t)(ty + 2) * nx; }
+};
+
+template <int PREC, int BLK>
+__global__ void __launch_bounds__(BLK) k_lbm_fused(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+                                                   const __grid_constant__ GeomDev G, const BufDev src,
+                                                   const BufDev dst, int ty, int zchunk)
+{
+  using R = typename Store<PREC>::R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* ring = reinterpret_cast<R*>(smem_raw);
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const int y0 = blockIdx.x * ty;
+  const int nrow = min(ty, ny - y0);  // rows owned by this CTA
+  const int z0 = blockIdx.y * zchunk;
+  if (z0 >= nz) return;
+  const int z1 = min(z0 + zchunk, nz);
+  const int slab = (ty + 2) * nx;  // one ring plane: rows y0-1 .. y0+ty
+  const int ylo = y0 == 0 ? ny - 1 : y0 - 1;
+  const int yhi = y0 + nrow == ny ? 0 : y0 + nrow;
+
+  // colour of plane zp into ring plane `slot`: wetting colour everywhere,
+  // then the fluid nodes of the halo row below, the owned rows and the halo
+  // row above.  `own` = also store the 16-bit reference densities.
+  auto colour_plane = [&](int zp, int slot, bool own) {
+    R* pl = ring + slot * slab;
+    for (int j = threadIdx.x; j < slab; j += BLK) pl[j] = K.wet;
+    __syncthreads();
+    const int rlo = ylo + ny * zp, rmid = y0 + ny * zp, rhi = yhi + ny * zp;
+    const int a0 = __ldg(G.rowstart + rlo), n0 = __ldg(G.rowstart + rlo + 1) - a0;
+    const int a1 = __ldg(G.rowstart + rmid), n1 = __ldg(G.rowstart + rmid + nrow) - a1;
+    const int a2 = __ldg(G.rowstart + rhi), n2 = __ldg(G.rowstart + rhi + 1) - a2;
+    const int ntot = n0 + n1 + n2;
+    for (int j = threadIdx.x; j < ntot; j += BLK) {
+      int i, rs;  // node and its ring row
+      if (j < n0) {
+        i = a0 + j;
+        rs = 0;
+      } else if (j < n0 + n1) {
+        i = a1 + (j - n0);
+        rs = -1;  // from the coordinates below
+      } else {
+        i = a2 + (j - n0 - n1);
+        rs = nrow + 1;
+      }
+      const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+      int s[19];
+      pull_sources(G, i, c, m, s);
+      R f[38];
+      pull_node<PREC>(K, G, src, i, m, s, f);
+      R rr, rb;
+      densities(f, rr, rb);
+      int x, y, z;
+      unpack(c, x, y, z);
+      if (rs < 0) rs = y - y0 + 1;
+      pl[rs * nx + x] = stencil_colour(rr, rb, K.wet);
+      if constexpr (Store<PREC>::kDev) {
+        if (own && rs >= 1 && rs <= nrow) {
+          dst.rho[0][i] = rr;
+          dst.rho[1][i] = rb;
+        }
+      }
+    }
+  };
+
+  colour_plane(z0 == 0 ? nz - 1 : z0 - 1, 0, false);
+  __syncthreads();
+  colour_plane(z0, 1, true);
+  int slo = 0, smid = 1, shi = 2;
+  for (int z = z0; z < z1; z++) {
+    const int zn = z + 1 == nz ? 0 : z + 1;
+    __syncthreads();  // the previous collision finished reading ring plane shi
+    colour_plane(zn, shi, zn >= z0 && zn < z1);
+    __syncthreads();
+    // collide the owned nodes of plane z
+    const int a = __ldg(G.rowstart + y0 + ny * z), n = __ldg(G.rowstart + y0 + nrow + ny * z) - a;
+    const R* plo = ring + slo * slab;
+    const R* pmid = ring + smid * slab;
+    const R* phi = ring + shi * slab;
+    for (int j = threadIdx.x; j < n; j += BLK) {
+      const int i = a + j;
+      const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+      R f[38];
+      {
+        int s[19];
+        pull_sources(G, i, c, m, s);
+        pull_node<PREC>(K, G, src, i, m, s, f);
+      }
+      R rr, rb;
+      densities(f, rr, rb);
+      int x, y, zz;
+      unpack(c, x, y, zz);
+      const int r = y - y0 + 1;
+      const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+      auto col = [&](int ax, int by, int cz) -> R {
+        const R* pl = cz == 0 ? plo : (cz == 1 ? pmid : phi);
+        const int xx = ax == 0 ? xm : (ax == 1 ? x : xp);
+        return pl[(r + by - 1) * nx + xx];
+      };
+      R outr[19], outb[19];
+      node_update(K, f, f + 19, rr, rb, col, outr, outb);
+      Pop<PREC>::store(K, dst, 0, i, G.pitch, outr, rr);
+      Pop<PREC>::store(K, dst, 1, i, G.pitch, outb, rb);
+    }
+    const int t = slo;
+    slo = smid;
+    smid = shi;
+    shi = t;
+  }
 }
 
 // ---- colour/density field (observables, fields) ---------------------------
-// rr, rb (FP64) and the stencil colour cc (FP64, wetting colour for
-// non-fluid voxels) of the current state, dense.
+// rr, rb, cf in the reference fluid order and the FP64 stencil colour cc on
+// the dense box (the wetting colour on non-fluid voxels is set by the host)
 template <int PREC>
 __global__ void k_lbm_fields(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                              const __grid_constant__ GeomDev G, const BufDev src, double* rr, double* rb,
                              double* cf, double* cc)
 {
   using R = typename Store<PREC>::R;
-  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (v >= G.nvox) return;
-  const uint32_t m = G.mask[v];
-  if (!(m & kFluidBit)) {
-    cc[v] = (double)K.wet;
-    return;
-  }
-  const int x = (int)(v % G.nx), y = (int)((v / G.nx) % G.ny), z = (int)(v / ((long long)G.nx * G.ny));
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= G.nl) return;
+  const uint32_t c = G.coord[i], m = G.mask[i];
+  int s[19];
+  pull_sources(G, i, c, m, s);
   R f[38];
-  pull_node<PREC>(K, G, src, x, y, z, m, f);
+  pull_node<PREC>(K, G, src, i, m, s, f);
   R a, b;
   densities(f, a, b);
-  rr[v] = (double)a;
-  rb[v] = (double)b;
-  const R c = (a - b) / (a + b);
-  cf[v] = (double)c;
-  cc[v] = (double)((c - K.wet) + K.wet);
+  const int r = G.ref[i];
+  rr[r] = (double)a;
+  rb[r] = (double)b;
+  const R q = (a - b) / (a + b);
+  cf[r] = (double)q;
+  int x, y, z;
+  unpack(c, x, y, z);
+  cc[x + G.nx * (y + G.ny * z)] = (double)((q - K.wet) + K.wet);
 }
 
 // post-streaming populations in the reference layout fr(19,nl), fb(19,nl)
@@ -356,24 +538,27 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
                                 const __grid_constant__ GeomDev G, const BufDev src, double* fr, double* fb)
 {
   using R = typename Store<PREC>::R;
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
-  const long long v = G.fvox[i];
-  const int x = (int)(v % G.nx), y = (int)((v / G.nx) % G.ny), z = (int)(v / ((long long)G.nx * G.ny));
+  const uint32_t m = G.mask[i];
+  int s[19];
+  pull_sources(G, i, G.coord[i], m, s);
   R f[38];
-  pull_node<PREC>(K, G, src, x, y, z, G.mask[v], f);
+  pull_node<PREC>(K, G, src, i, m, s, f);
+  const long long r = G.ref[i];
 #pragma unroll
   for (int d = 0; d < 19; d++) {
-    fr[19 * i + d] = (double)f[d];
-    fb[19 * i + d] = (double)f[19 + d];
+    fr[19 * r + d] = (double)f[d];
+    fb[19 * r + d] = (double)f[19 + d];
   }
 }
 
 // Inverse of the pull: given post-streaming populations fr, fb (reference
-// layout), writes the pre-pull buffer so that pull_node reproduces them.
-// Population d at voxel y goes to the node it streams to (y + c_d), or, if
-// that link is a wall link, it is the reflection of y's own population
-// opp(d).
+// layout), writes the pre-pull buffer so that the pull reproduces them.
+// Population d of node y goes to the node it streams to (y + c_d, the pull
+// source of direction opp(d)); when that link is a wall link it is the
+// reflection of y's own population opp(d).  Links are symmetric: y -> y+c_d
+// streams exactly when y's incoming link opp(d) is open.
 template <int PREC>
 __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                 const __grid_constant__ GeomDev G, const BufDev dst, const double* fr,
@@ -381,39 +566,31 @@ __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<
 {
   using S = Store<PREC>;
   using R = typename S::R;
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
-  const long long v = G.fvox[i];
-  const int x = (int)(v % G.nx), y = (int)((v / G.nx) % G.ny), z = (int)(v / ((long long)G.nx * G.ny));
-  int xs[3], ys[3], zs[3];
-  nb3(x, G.nx, xs);
-  nb3(y, G.ny, ys);
-  nb3(z, G.nz, zs);
-  const long long nxl = G.nx, nxy = (long long)G.nx * G.ny;
+  const uint32_t m = G.mask[i];
+  int s[19];
+  pull_sources(G, i, G.coord[i], m, s);
+  const long long me = G.ref[i];
   const double* fk[2] = {fr, fb};
 #pragma unroll
   for (int k = 0; k < 2; k++) {
     R out[19];
     R rho = R(0);
-    out[0] = (R)fk[k][19 * i];
+    out[0] = (R)fk[k][19 * me];
     for (int d = 1; d < 19; d++) {
-      const long long vt = xs[1 + cvx(d)] + nxl * ys[1 + cvy(d)] + nxy * zs[1 + cvz(d)];
-      const uint32_t mt = G.mask[vt];
-      const bool open = (mt & kFluidBit) && (mt & (1u << (d - 1)));
-      double val;
-      if (open)
-        val = fk[k][19 * (long long)G.fid[vt] + d];
-      else
-        val = fk[k][19 * i + opp(d)];
+      const int od = opp(d);
+      const bool open = m & (1u << (od - 1));
+      const double val = open ? fk[k][19 * (long long)G.ref[s[od]] + d] : fk[k][19 * me + od];
       out[d] = (R)val;
     }
     if constexpr (S::kDev) {
-      double s = fk[k][19 * i];
-      for (int d = 1; d < 19; d++) s += fk[k][19 * i + d];
-      rho = (R)s;
-      dst.rho[k][v] = rho;
+      double sum = fk[k][19 * me];
+      for (int d = 1; d < 19; d++) sum += fk[k][19 * me + d];
+      rho = (R)sum;
+      dst.rho[k][i] = rho;
     }
-    Pop<PREC>::store(K, dst, k, v, G.nvox, out, rho);
+    Pop<PREC>::store(K, dst, k, i, G.pitch, out, rho);
   }
 }
 
@@ -435,10 +612,13 @@ __global__ void __launch_bounds__(256) k_lbm_obs(const __grid_constant__ LbmCons
   const LbmConst<double>& D = *Kd;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.nl;
        i += (long long)gridDim.x * blockDim.x) {
-    const long long v = G.fvox[i];
-    const int x = (int)(v % G.nx), y = (int)((v / G.nx) % G.ny), z = (int)(v / ((long long)G.nx * G.ny));
+    const uint32_t cw = G.coord[i], m = G.mask[i];
+    int s[19];
+    pull_sources(G, (int)i, cw, m, s);
     R fR[38];
-    pull_node<PREC>(K, G, src, x, y, z, G.mask[v], fR);
+    pull_node<PREC>(K, G, src, (int)i, m, s, fR);
+    int x, y, z;
+    unpack(cw, x, y, z);
     double f[38];
 #pragma unroll
     for (int d = 0; d < 38; d++) f[d] = (double)fR[d];
@@ -474,12 +654,10 @@ __global__ void __launch_bounds__(256) k_lbm_obs(const __grid_constant__ LbmCons
       acc[31 + 3 * k] += jy;
       acc[32 + 3 * k] += jz;
     }
-    int xs[3], ys[3], zs[3];
-    nb3(x, G.nx, xs);
-    nb3(y, G.ny, ys);
-    nb3(z, G.nz, zs);
-    const long long nxl = G.nx, nxy = (long long)G.nx * G.ny;
-    auto ccf = [&](int a, int b, int c) -> double { return cc[xs[a] + nxl * ys[b] + nxy * zs[c]]; };
+    const int nxy = G.nx * G.ny;
+    const int v = x + G.nx * y + nxy * z;
+    const NbOff o = nb_offsets(m, G.nx, nxy, G.nz);
+    auto ccf = [&](int a, int b, int c) -> double { return cc[v + o.x[a] + o.y[b] + o.z[c]]; };
     double n[3], Fs[3];
     csf_force(D, ccf, n, Fs);
     double g[19];

@@ -17,23 +17,17 @@ struct LbmLaunchArgs {
   cudaStream_t stream;
 };
 
-// block sizes compiled for the step kernels: tx = collide kernel, ty =
-// density kernel (threads per CTA)
-struct TileCfg {
-  int tx, ty;
-};
-
-// returns cudaErrorInvalidValue when (tx,ty) is not a compiled block pair
+// returns cudaErrorInvalidValue when (tx, ty) is not a compiled configuration
+// (tx threads per CTA; ty rows per CTA of the fused kernel, 0 = two launches)
 cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunchArgs& a);
 cudaError_t lbm_fields_launch(int prec, const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc);
 cudaError_t lbm_get_state_launch(int prec, const LbmLaunchArgs& a, double* fr, double* fb);
 cudaError_t lbm_set_state_launch(int prec, const LbmLaunchArgs& a, const double* fr, const double* fb);
 cudaError_t lbm_obs_launch(int prec, const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,
                            double* out);
-// the compiled tiles of a precision (n returned, at most cap written)
-int lbm_tiles(int prec, TileCfg* out, int cap);
-// smem bytes of the step kernel for a tile (0 if not compiled)
-size_t lbm_step_smem(int prec, int tx, int ty);
+// dynamic shared memory of a step configuration for rows of nx voxels
+// (0 when the configuration is not compiled, 1 for the two-launch form)
+size_t lbm_step_smem(int prec, int tx, int ty, int nx);
 
 // per-precision implementations
 #define PS_DECL_PREC(P)                                                                                     \
@@ -43,8 +37,7 @@ size_t lbm_step_smem(int prec, int tx, int ty);
   cudaError_t lbm_set_state_launch_##P(const LbmLaunchArgs& a, const double* fr, const double* fb);        \
   cudaError_t lbm_obs_launch_##P(const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,   \
                                  double* out);                                                              \
-  int lbm_tiles_##P(TileCfg* out, int cap);                                                                 \
-  size_t lbm_step_smem_##P(int tx, int ty);
+  size_t lbm_step_smem_##P(int tx, int ty, int nx);
 PS_DECL_PREC(0)
 PS_DECL_PREC(1)
 PS_DECL_PREC(2)

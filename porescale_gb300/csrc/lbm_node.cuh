@@ -155,6 +155,54 @@ PS_HD void mrt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r
   for (int i = 1; i < 19; i++) pcf[i] = f[i] - mb[i] + Fp[i];
 }
 
+// The same collision in two-relaxation-time population form, used by the
+// FP32 paths.  With the reference's rates every even non-conserved moment
+// relaxes with S[1] (= s_nu) and every odd one with S[4] (= s_q, the TRT
+// magic 3/16 pair), and the equilibrium conserves density and momentum
+// exactly, so M^-1 S M (f - fe) equals s_nu (f - fe)^+ + s_q (f - fe)^- for
+// each opposite pair: the operator of mrt_collide in ~80 operations
+// instead of ~300, differing only by rounding.
+template <typename R>
+PS_HD void trt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r, const R* bf, const R* Fp,
+                       const R* S)
+{
+  const R dt = K.dt, dti = K.dti, dt2 = K.dt2;
+  const R jx = (f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14]) * dti;
+  const R jy = (f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18]) * dti;
+  const R jz = (f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18]) * dti;
+  const R rinv = R(1) / r;
+  const R ux = (jx + bf[0] * R(0.5) * dt) * rinv;
+  const R uy = (jy + bf[1] * R(0.5) * dt) * rinv;
+  const R uz = (jz + bf[2] * R(0.5) * dt) * rinv;
+  const R uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+  const R usq = (uxx + uyy + uzz) * R(0.5);
+  const R wp = S[1], wm = S[4];
+  // rest
+  pcf[0] = f[0] - wp * (f[0] - r * (t1 - usq * dt2)) + Fp[0];
+  // even part of an opposite pair's equilibrium, odd part
+  const R rq = r * R(0.25) * dt2;
+  const R e1 = (t2 - usq * K.c1d6 * dt2) * r;
+  const R c6 = K.c1d6 * dt, c12 = K.c1d12 * dt;
+  auto pair = [&](int a, int b, R even, R odd) {
+    const R la = f[a] - (even + odd), lb = f[b] - (even - odd);
+    const R p = (la + lb) * R(0.5), m = (la - lb) * R(0.5);
+    pcf[a] = f[a] - wp * p - wm * m + Fp[a];
+    pcf[b] = f[b] - wp * p + wm * m + Fp[b];
+  };
+  pair(1, 2, e1 + rq * uxx, jx * c6);
+  pair(3, 4, e1 + rq * uyy, jy * c6);
+  pair(5, 6, e1 + rq * uzz, jz * c6);
+  const R ro = r * R(0.125) * dt2;
+  const R e2 = (t3 - usq * K.c1d12 * dt2) * r;
+  pair(7, 10, e2 + ro * (ux + uy) * (ux + uy), (jx + jy) * c12);
+  pair(8, 9, e2 + ro * (ux - uy) * (ux - uy), (jy - jx) * c12);
+  pair(11, 14, e2 + ro * (ux + uz) * (ux + uz), (jx + jz) * c12);
+  pair(12, 13, e2 + ro * (ux - uz) * (ux - uz), (jz - jx) * c12);
+  pair(15, 18, e2 + ro * (uy + uz) * (uy + uz), (jy + jz) * c12);
+  pair(16, 17, e2 + ro * (uy - uz) * (uy - uz), (jz - jy) * c12);
+  f[0] = pcf[0];
+}
+
 // CSF surface tension from the colour neighbourhood.  cc(i,j,k), i,j,k in
 // {0,1,2} (offsets -1,0,+1 in x,y,z) returns the stencil colour: the node's
 // colour for fluid voxels, the wetting colour for the others.  The colour
@@ -293,7 +341,10 @@ PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R r
     bf[1] = K.bf[k][1];
     bf[2] = K.bf[k][2];
   }
-  mrt_collide(K, t1, t2, t3, f, pcf, r, bf, Fp, S);
+  if constexpr (kExact)
+    mrt_collide(K, t1, t2, t3, f, pcf, r, bf, Fp, S);
+  else
+    trt_collide(K, t1, t2, t3, f, pcf, r, bf, Fp, S);
   if (iface) {
     // cosine between the colour normal and each direction
     R cs[19];

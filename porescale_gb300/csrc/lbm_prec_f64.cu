@@ -4,5 +4,4 @@
 // CPU restatement bit for bit.
 #include "lbm_prec_impl.cuh"
 
-#define PS_TILES_0(X, P) X(P, 128, 256) X(P, 256, 256)
-PS_DEFINE_PREC(0, PS_TILES_0)
+PS_DEFINE_PREC(0)

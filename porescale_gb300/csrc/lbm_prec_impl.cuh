@@ -19,11 +19,33 @@ cudaError_t step_blk(const LbmLaunchArgs& a)
   return cudaGetLastError();
 }
 
+// fused step: BLK threads, TY rows per CTA, zchunk planes per CTA
+template <int PREC, int BLK>
+cudaError_t step_fused(int ty, int zchunk, const LbmLaunchArgs& a)
+{
+  using R = typename Store<PREC>::R;
+  const GeomDev& G = a.G;
+  if (G.nl == 0) return cudaSuccess;
+  const size_t smem = FusedSmem<R>::bytes(ty, G.nx);
+  static size_t attr = 0;  // per instantiation: largest dynamic smem opted in so far
+  if (smem > 48 * 1024 && smem > attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_lbm_fused<PREC, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = smem;
+  }
+  if (zchunk <= 0) zchunk = G.nz;
+  dim3 grid((G.ny + ty - 1) / ty, (G.nz + zchunk - 1) / zchunk);
+  const LbmConst<R>& C = *static_cast<const LbmConst<R>*>(a.K);
+  k_lbm_fused<PREC, BLK><<<grid, BLK, smem, a.stream>>>(C, G, a.src, a.dst, ty, zchunk);
+  return cudaGetLastError();
+}
+
 template <int PREC>
 cudaError_t fields(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc)
 {
   using R = typename Store<PREC>::R;
-  const long long n = a.G.nvox;
+  const long long n = a.G.nl;
+  if (n == 0) return cudaSuccess;
   k_lbm_fields<PREC><<<(unsigned)((n + 255) / 256), 256, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K), a.G,
                                                                           a.src, rr, rb, cf, cc);
   return cudaGetLastError();
@@ -67,20 +89,21 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
 }  // namespace ps
 
 // Defines the per-precision entry points declared in lbm_launch.h for
-// precision P.  The step kernels are instantiated for the (collide block,
-// density block) sizes listed in the PS_TILES_<P> X-macro of the including
-// file.
-#define PS_STEP_CASE(P, TX, TY) \
-  if (tx == TX && ty == TY) return detail::step_blk<P, TX, TY>(a);
-#define PS_TILE_ITEM(P, TX, TY) {TX, TY},
-#define PS_SMEM_CASE(P, TX, TY) \
-  if (tx == TX && ty == TY) return 1;
-
-#define PS_DEFINE_PREC(P, TILES)                                                                           \
+// precision P.  A step configuration is (tx, ty, zchunk): tx threads per
+// CTA; ty >= 1 rows per CTA for the fused kernel (zchunk planes per CTA), or
+// ty == 0 for the two-launch form (tx threads for the collide kernel, 256
+// for the density kernel).
+#define PS_DEFINE_PREC(P)                                                                                  \
   namespace ps {                                                                                           \
   cudaError_t lbm_step_launch_##P(int tx, int ty, int zchunk, const LbmLaunchArgs& a)                      \
   {                                                                                                        \
-    TILES(PS_STEP_CASE, P)                                                                                 \
+    if (ty == 0) {                                                                                         \
+      if (tx == 128) return detail::step_blk<P, 128, 256>(a);                                              \
+      if (tx == 256) return detail::step_blk<P, 256, 256>(a);                                              \
+      return cudaErrorInvalidValue;                                                                        \
+    }                                                                                                      \
+    if (tx == 128) return detail::step_fused<P, 128>(ty, zchunk, a);                                       \
+    if (tx == 256) return detail::step_fused<P, 256>(ty, zchunk, a);                                       \
     return cudaErrorInvalidValue;                                                                          \
   }                                                                                                        \
   cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc) \
@@ -100,16 +123,10 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
   {                                                                                                        \
     return detail::obs<P>(a, cc, partial, nblocks, out);                                                   \
   }                                                                                                        \
-  int lbm_tiles_##P(TileCfg* out, int cap)                                                                 \
+  size_t lbm_step_smem_##P(int tx, int ty, int nx)                                                         \
   {                                                                                                        \
-    static const TileCfg t[] = {TILES(PS_TILE_ITEM, P)};                                                   \
-    const int n = (int)(sizeof t / sizeof t[0]);                                                           \
-    for (int i = 0; i < n && i < cap; i++) out[i] = t[i];                                                  \
-    return n;                                                                                              \
-  }                                                                                                        \
-  size_t lbm_step_smem_##P(int tx, int ty)                                                                 \
-  {                                                                                                        \
-    TILES(PS_SMEM_CASE, P)                                                                                 \
-    return 0;                                                                                              \
+    if (tx != 128 && tx != 256) return 0;                                                                  \
+    if (ty == 0) return 1;                                                                                 \
+    return FusedSmem<typename Store<P>::R>::bytes(ty, nx);                                                 \
   }                                                                                                        \
   }

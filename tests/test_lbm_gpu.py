@@ -116,16 +116,18 @@ def test_low_precision_close_to_oracle(gpu, oracle_lib, prec, tol):
     assert err <= tol, err
 
 
-def test_block_sizes_agree(gpu):
-    """Every compiled (collide, density) block-size pair gives the same FP64 result."""
-    ind, p = _case(n=(40, 12, 20))
+@pytest.mark.parametrize("prec", [PREC_F64, PREC_F32, PREC_F16])
+def test_step_configurations_agree(gpu, prec):
+    """The fused kernel (any rows per CTA / planes per CTA, including ragged
+    last tiles and chunks) and the two-launch form give identical states."""
+    ind, p = _case(n=(11, 13, 40))
     ref = None
-    for tx, ty in ((128, 256), (256, 256)):
-        with Lattice(p, ind, PREC_F64) as L:
-            L.set_tile(tx, ty, 0)
+    for tx, ty, zc in ((256, 0, 0), (128, 0, 0), (256, 8, 4), (128, 4, 3), (256, 2, 7), (256, 16, 40), (128, 1, 1)):
+        with Lattice(p, ind, prec) as L:
+            L.set_tile(tx, ty, zc)
             L.init_random(0.4)
             L.step(6)
             st = L.get_state()
         if ref is None:
             ref = st
-        assert np.array_equal(st[0], ref[0]) and np.array_equal(st[1], ref[1]), (tx, ty)
+        assert np.array_equal(st[0], ref[0]) and np.array_equal(st[1], ref[1]), (tx, ty, zc)

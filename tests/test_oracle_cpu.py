@@ -151,3 +151,35 @@ def test_lsm_bond_table_counts(oracle_lib):
     # per unique node 9 bonds, plus the in-plane bonds of the duplicate
     # plane (y, z edges and the yz face diagonals: 4 per node)
     assert len(bon) == 9 * n ** 3 + 4 * n * n
+
+
+def _golden():
+    import json
+    import os
+    return json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_tables.json")))
+
+
+def test_angle_table_matches_reference(oracle_lib):
+    """Our derivation of anf (n = c_j x c_k / |.|, f_j = n x c_j / |c_j|^2,
+    f_k = -n x c_k / |c_k|^2) equals the literal table of the reference
+    (S1:264-432) row by row up to the orientation of the plane normal: the
+    reference orients its xz-plane angles against the right-hand rule
+    (normal +y), which negates n, f_j and f_k together and leaves every
+    force and stress unchanged (they are bilinear in the row)."""
+    g = np.array(_golden()["anf"])
+    anf, *_ = oracle_lib.lsm_constant_tables()
+    for i in range(48):
+        assert np.allclose(anf[i], g[i], atol=1e-15) or np.allclose(anf[i], -g[i], atol=1e-15), i + 1
+    flipped = [i + 1 for i in range(48) if not np.allclose(anf[i], g[i], atol=1e-15)]
+    assert flipped == list(range(9, 17))  # exactly the eight xz-plane angles
+
+
+def test_cube_tables_match_reference(oracle_lib):
+    """The 24 cube bonds and 72 cube angles we generate from geometry are the
+    reference's cube_bon / cube_ang sets with the same unit constants."""
+    g = _golden()
+    _, b, sb, a, ab = oracle_lib.lsm_constant_tables()
+    bonds = sorted([int(x[0]), int(x[1]), int(x[2]), float(s)] for x, s in zip(b, sb))
+    angles = sorted([*map(int, x), float(s)] for x, s in zip(a, ab))
+    assert bonds == [list(r) for r in g["cube_bonds"]]
+    assert angles == [list(r) for r in g["cube_angles"]]
