@@ -170,6 +170,22 @@ int ps_lsm_solve(void *handle, double rtol, int32_t maxit, ps_lsm_result *out);
 int ps_lsm_get_disp(void *handle, double *u);
 void *ps_lsm_stream(void *handle);
 
+/* Largest box (voxel cubes) ps_lsm_stress_noalloc accepts: 128^3. */
+#define PS_LSM_NOALLOC_MAX_CUBES (2 * 1024 * 1024)
+/* Allocation-free stress evaluation -- no counterpart in the reference.
+ * For callers that cannot allocate device memory when they need the moduli
+ * (a time loop being captured into a CUDA graph, or a driver confined to a
+ * fixed device memory budget).  d_u is a DEVICE array of the displacements
+ * of the unique nodes of the handle's box, three planes (x, y, z component)
+ * of nx*ny*nz values, node (x,y,z) at x + nx*(y + ny*z), without the jump;
+ * out (host) receives the 9 summed cube stresses (as ps_lsm_result.sigma)
+ * and then the modulus.  Uses a static device scratch array instead of
+ * cudaMalloc; boxes above PS_LSM_NOALLOC_MAX_CUBES are rejected
+ * (PS_ERR_ARG).  Calls that overlap on the GPU share that array and race;
+ * the first call on a device sets it up and should precede any stream
+ * capture. */
+int ps_lsm_stress_noalloc(void *handle, const double *d_u, double *out);
+
 /* Message of the last error on this thread (always NUL-terminated). */
 int ps_last_error(char *buf, int32_t len);
 /* Library build information ("porescale_gb300 <version> sm_103a"). */

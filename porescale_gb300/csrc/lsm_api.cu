@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "lsm_cube.h"
@@ -279,6 +280,44 @@ int compute_stress(Springs* S, ps_lsm_result* out)
   return PS_OK;
 }
 
+// ---- no-allocation stress reduction -------------------------------------
+// Scratch of ps_lsm_stress_noalloc: one 9-component partial sum per CTA of
+// the stress kernel plus the 9 final sums.  It is a file-scope device array,
+// so the entry point never allocates; every GPU that loads the library holds
+// it (about 590 KB) until the process exits.
+constexpr int kNoAllocMaxBlocks = PS_LSM_NOALLOC_MAX_CUBES / kBlk;
+static __device__ __align__(256) double g_stress_scratch[9 * kNoAllocMaxBlocks + 9];
+
+// fixed-order sum of n partials (9 components each) into out[0..8]
+__global__ void k_stress_final(const double* part, int n, double* out)
+{
+  if (threadIdx.x >= 9) return;
+  double s = 0.0;
+  for (int b = 0; b < n; b++) s += part[(long long)b * 9 + threadIdx.x];
+  out[threadIdx.x] = s;
+}
+
+// device address of g_stress_scratch on each device, looked up once per
+// device with that device current (the host-side symbol is only a stand-in)
+std::mutex g_scratch_mu;
+double* g_scratch_ptr[64] = {nullptr};
+
+int noalloc_scratch(double** out)
+{
+  int dev = 0;
+  PS_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(PS_ERR_ARG, "ps_lsm_stress_noalloc: device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    double* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&p, g_stress_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_stress_scratch)");
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return PS_OK;
+}
+
 }  // namespace
 }  // namespace ps
 
@@ -510,5 +549,43 @@ int ps_lsm_get_disp(void* h, double* u)
 }
 
 void* ps_lsm_stream(void* h) { return h ? (void*)static_cast<Springs*>(h)->stream : nullptr; }
+
+// Stress and modulus of a caller-supplied displacement field, computed
+// without any device allocation: the per-CTA partial sums go to the
+// library's static scratch array instead of memory from cudaMalloc.  Meant
+// for callers that may not allocate at that point -- a time loop being
+// captured into a CUDA graph, or a driver running inside a fixed device
+// memory budget that re-evaluates the moduli every few steps.  The handle
+// must already exist (ps_lsm_create allocates; this call does not).
+//
+// The scratch array is shared by every call in the process and keeps the
+// last call's partial sums; each call rewrites the slots it reads before
+// reading them.  Calls that overlap on the GPU (from several host threads or
+// streams) race on it and must be serialised by the caller.  The first call
+// on a device looks up the array's device address with that device current.
+int ps_lsm_stress_noalloc(void* h, const double* d_u, double* out)
+{
+  if (!h || !d_u || !out) return fail(PS_ERR_ARG, "ps_lsm_stress_noalloc: null argument");
+  Springs* S = static_cast<Springs*>(h);
+  if ((long long)S->nvox > PS_LSM_NOALLOC_MAX_CUBES)
+    return fail(PS_ERR_ARG, "ps_lsm_stress_noalloc: %d voxel cubes exceed the no-allocation maximum of %d",
+                S->nvox, PS_LSM_NOALLOC_MAX_CUBES);
+  double* scratch = nullptr;
+  if (int e = noalloc_scratch(&scratch)) return e;
+  const int nb = blocks_for(S->nvox);
+  const double jump = 2.0 * S->p.gstrain;
+  lsm::k_lsm_stress<kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->pa, S->jc, jump, d_u, scratch);
+  PS_CUDA(cudaGetLastError());
+  k_stress_final<<<1, 32, 0, S->stream>>>(scratch, nb, scratch + 9 * kNoAllocMaxBlocks);
+  PS_CUDA(cudaGetLastError());
+  double sig[9];
+  PS_CUDA(cudaMemcpyAsync(sig, scratch + 9 * kNoAllocMaxBlocks, sizeof sig, cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  const double vcell = (double)S->nx * S->ny * S->nz;
+  const double nax = S->pa == 0 ? S->nx : S->ny;
+  for (int i = 0; i < 9; i++) out[i] = sig[i];
+  out[9] = (S->pa == 0 ? sig[0] : sig[5]) / (vcell * jump / nax);
+  return PS_OK;
+}
 
 }  // extern "C"

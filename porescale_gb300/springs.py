@@ -45,6 +45,7 @@ _SIGS = {
     "ps_lsm_solve": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.POINTER(LsmResult)]),
     "ps_lsm_get_disp": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ps_lsm_stream": (C.c_void_p, [C.c_void_p]),
+    "ps_lsm_stress_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
 }
 _lib.SIGNATURES.update(_SIGS)
 

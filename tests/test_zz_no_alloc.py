@@ -1,0 +1,93 @@
+"""The allocation-free stress entry point (ps_lsm_stress_noalloc) against
+ps_lsm_solve's own stress result.
+
+ps_lsm_stress_noalloc serves callers that cannot allocate device memory
+when they need the moduli (a time loop being captured into a CUDA graph, a
+driver confined to a fixed device memory budget); its partial sums live in
+a static device array of the library.  This file runs last (pytest collects
+it after the others) and also passes on its own in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from porescale_gb300 import geometry as geo
+from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, SpringNetwork
+
+pytestmark = pytest.mark.gpu
+
+# the tolerance of the FP64 modulus checks in test_lsm_gpu.py
+RTOL = 1e-9
+
+
+def _reference_nodes(ind, pa):
+    """Coordinates of the reference's solid nodes in its node order: k-j-i
+    over the padded grid, the loaded axis having node planes 0..N (plane N
+    duplicates plane 0); a node exists when one of its cubes is solid, with
+    no cubes beyond the ends of the loaded axis."""
+    nz, ny, nx = ind.shape
+    N = np.array([nx, ny, nz])
+    M = N.copy()
+    M[pa] += 1
+    solid = (ind == 0) | (ind == 3)
+    zz, yy, xx = np.meshgrid(np.arange(M[2]), np.arange(M[1]), np.arange(M[0]), indexing="ij")
+    coords = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1)
+    exists = np.zeros(len(coords), bool)
+    for e in range(8):
+        c = coords - np.array([e & 1, (e >> 1) & 1, (e >> 2) & 1])
+        ok = (c[:, pa] >= 0) & (c[:, pa] < N[pa])
+        for d in range(3):
+            c[:, d] = np.clip(c[:, d], 0, N[d] - 1) if d == pa else c[:, d] % N[d]
+        exists |= ok & solid[c[:, 2], c[:, 1], c[:, 0]]
+    return coords[exists], N
+
+
+def _unique_field(u_ref, nodes, N, pa, jc, g):
+    """Reference-order displacements -> the layout ps_lsm_stress_noalloc
+    reads: 3 planes of nx*ny*nz unique nodes, without the jump."""
+    vals = u_ref.copy()
+    vals[nodes[:, pa] == N[pa], jc] -= 2 * g
+    uniq = nodes % N
+    U = np.zeros((3, N[2], N[1], N[0]))
+    U[:, uniq[:, 2], uniq[:, 1], uniq[:, 0]] = vals.T
+    return np.ascontiguousarray(U)
+
+
+@pytest.mark.parametrize("load", [LOAD_XSTRETCH, LOAD_YZSHEAR])
+def test_stress_noalloc_matches_solve(gpu, load):
+    import torch
+
+    n = 16
+    ind = geo.inclusions(n, 0.25, 3.0, seed=21)
+    g = 1e-3 * n / 2
+    pa, jc = (0, 0) if load == LOAD_XSTRETCH else (1, 2)
+    nodes, N = _reference_nodes(ind, pa)
+    with SpringNetwork(ind, 1.0, 0.4, 0.3, 0.1, g, load, LSM_F64) as S:
+        r = S.solve(1e-11, 100000)
+        u_ref = S.displacements(len(nodes))
+        d_u = torch.from_numpy(_unique_field(u_ref, nodes, N, pa, jc, g)).cuda()
+        torch.cuda.synchronize()
+        sig_ref = np.array(r.sigma[:])
+        for call in range(2):  # two calls in a row on the same static scratch
+            out = (C.c_double * 10)()
+            rc = S._lib.ps_lsm_stress_noalloc(S._h, C.c_void_p(d_u.data_ptr()), out)
+            assert rc == 0, call
+            sig = np.array(out[:9])
+            assert np.allclose(sig, sig_ref, rtol=RTOL, atol=RTOL * np.abs(sig_ref).max()), call
+            assert out[9] == pytest.approx(r.modulus, rel=RTOL), call
+
+
+def test_stress_noalloc_rejects_oversized_box(gpu):
+    """Boxes above PS_LSM_NOALLOC_MAX_CUBES (128^3) are refused with PS_ERR_ARG."""
+    import torch
+
+    from porescale_gb300._lib import last_error
+
+    ind = np.zeros((128, 128, 136), np.int32)  # 2,228,224 cubes
+    with SpringNetwork(ind, 1.0, 0.4, 1.0, 0.4, 0.01, LOAD_XSTRETCH, LSM_F64) as S:
+        d_u = torch.zeros(3 * ind.size, dtype=torch.float64, device="cuda")
+        out = (C.c_double * 10)()
+        rc = S._lib.ps_lsm_stress_noalloc(S._h, C.c_void_p(d_u.data_ptr()), out)
+        assert rc == 1
+        assert "maximum" in last_error()
