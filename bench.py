@@ -173,6 +173,75 @@ def cpu_oracle_mlups(ind, p, fr, fb, threads: int, budget_s: float):
     return nl * n / dt / 1e6, n, dt
 
 
+def lsm_leg(size=64, seed=20240601):
+    """Lattice-spring static solve on the two-solid cube (matrix alpha 1.0,
+    beta 0.4; radius-5 inclusions at volume fraction 0.25, alpha 0.3, beta
+    0.1; strain 1e-3): Cxxxx and Cyzyz by FP64 CG and by FP32 CG in FP64
+    refinement, CG iterations per second and the inner iteration's
+    bandwidth (133 algorithmic bytes per node per FP32 iteration, 265 for
+    FP64)."""
+    from porescale_gb300 import geometry
+    from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, LSM_MIXED, SpringNetwork
+    ind = geometry.inclusions(size, 0.25, 5.0, seed)
+    g = 1e-3 * size / 2
+    out = {"workload": f"two-solid lattice-spring cube {size}^3, radius-5 inclusions (fraction 0.25)",
+           "rtol": 1e-10}
+    peak, _ = load_peaks()
+    for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
+        for prec, pname, bpn in ((LSM_F64, "f64", 265), (LSM_MIXED, "mixed", 133)):
+            with SpringNetwork(ind, 1.0, 0.4, 0.3, 0.1, g, load, prec) as S:
+                S.solve(1e-10, 200000)  # warm-up (kernel loading, caches)
+                t = time.perf_counter()
+                r = S.solve(1e-10, 200000)
+                dt = time.perf_counter() - t
+                its = r.inner_iterations
+                out[f"{name}_{pname}"] = {"modulus": r.modulus, "relres": r.relres, "iterations": its,
+                                          "refinements": r.refinements, "seconds": dt,
+                                          "cg_iters_per_s": its / dt,
+                                          "achieved_gbs": its * r.nnode * bpn / dt / 1e9,
+                                          "frac": its * r.nnode * bpn / dt / 1e9 / peak}
+        out[f"{name}_rel_diff_mixed_vs_f64"] = abs(out[f"{name}_mixed"]["modulus"] - out[f"{name}_f64"]["modulus"]) / \
+            abs(out[f"{name}_f64"]["modulus"])
+    return out
+
+
+def accuracy(args, cfg):
+    """Relative-permeability, saturation and mass errors of the FP32 and
+    16-bit forms against the FP64 lattice (which reproduces the FP64 oracle
+    bit for bit) after the same number of steps on the same workload."""
+    from porescale_gb300.lattice import Lattice
+    ind, p, fr, fb = make_workload(cfg)
+    every = args.accuracy_every or args.accuracy_steps
+    hist = {}
+    t_run = {}
+    for q in ("f64", "f32", "f16", "bf16"):
+        L = Lattice(p, ind, PREC_ID[q])
+        L.set_state(fr, fb)
+        rows = []
+        t0 = time.perf_counter()
+        done = 0
+        while done < args.accuracy_steps:
+            n = min(every, args.accuracy_steps - done)
+            L.step(n)
+            done += n
+            o = L.observables()
+            rows.append({"step": done, "permr": o.permr, "permb": o.permb, "sat_r": o.sat_r, "sat_b": o.sat_b,
+                         "tmr": o.tmr, "tmb": o.tmb})
+        t_run[q] = time.perf_counter() - t0
+        hist[q] = rows
+        L.close()
+    ref = hist["f64"]
+    out = {"mode": "accuracy", "workload": cfg["workload"], "steps": args.accuracy_steps, "fluid_nodes": None,
+           "seconds": t_run, "final": {q: hist[q][-1] for q in hist}, "rel_err_vs_f64": {}}
+    for q in ("f32", "f16", "bf16"):
+        e = {}
+        for k in ("permr", "permb", "sat_r", "sat_b", "tmr", "tmb"):
+            e[k] = max(abs(a[k] - b[k]) / max(abs(b[k]), 1e-300) for a, b in zip(hist[q], ref))
+        out["rel_err_vs_f64"][q] = e
+    out["history"] = hist
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -186,8 +255,12 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the FP64/FP32 comparison legs")
-    ap.add_argument("--accuracy-steps", type=int, default=0)
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="instead of timing: run this many steps in every precision and report the errors of "
+                         "permeabilities, saturation and masses against FP64")
+    ap.add_argument("--accuracy-every", type=int, default=0, help="observable cadence of the accuracy run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default step configuration")
+    ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -228,6 +301,9 @@ def main():
     from porescale_gb300 import _build
     _build.build_all()
     from porescale_gb300.lattice import Lattice
+    if args.accuracy_steps > 0:
+        accuracy(args, cfg)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -264,7 +340,7 @@ def main():
         launch_s = t / steps
         achieved = nl * ALGO_BYTES[q] / launch_s / 1e9
         res[q] = {"mlups": mlups, "ms_per_step": launch_s * 1e3, "steps": steps, "achieved_gbs": achieved,
-                  "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.zchunk]}
+                  "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.occupancy]}
         if q == args.prec:
             # e2e through the C ABI with host buffers (pinned)
             hfr = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
@@ -303,6 +379,9 @@ def main():
         cpu = {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
                "sample": f"{n} full-lattice steps of the {args.size}^3 workload ({dt:.1f} s, FP64 C restatement)"}
 
+    lsm = None
+    if rank == 0 and not args.no_lsm:
+        lsm = lsm_leg()
     h = res[args.prec]
     traffic = load_traffic(args.prec, nl)
     line = {
@@ -319,6 +398,7 @@ def main():
         "gpu_launches": h["steps"],
         "clocks": clocks,
         "legs": {q: res[q] for q in legs},
+        "lsm": lsm,
     }
     if "f64" in res:
         line["mixed_vs_f64"] = h["mlups"] / res["f64"]["mlups"]

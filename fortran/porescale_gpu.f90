@@ -25,7 +25,7 @@ module porescale_gpu
 
   type, bind(c) :: ps_lbm_info
     integer(c_int64_t) :: nl, nps, npb2, npb4, ns, nvox
-    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, zchunk, reserved
+    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, occupancy, reserved
     integer(c_int64_t) :: device_bytes
   end type
 

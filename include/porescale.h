@@ -63,7 +63,7 @@ typedef struct {
   int64_t ns;    /* LSM solid nodes after corner dilation (S1:608) */
   int64_t nvox;  /* nx*ny*nz                                      */
   int32_t nx, ny, nz, precision;
-  int32_t tile_x, tile_y, zchunk, reserved;
+  int32_t tile_x, tile_y, occupancy, reserved;  /* step-kernel configuration */
   int64_t device_bytes; /* device memory held by the handle */
 } ps_lbm_info;
 
@@ -114,12 +114,15 @@ int ps_lbm_fields(void *handle, double *rr, double *rb, double *cf);
 /* Stream handle (cudaStream_t) the lattice launches on, for event timing. */
 void *ps_lbm_stream(void *handle);
 int ps_lbm_sync(void *handle);
-/* Tile of the fused step kernel: tx*ty threads per CTA, zchunk z-planes per
- * CTA (0 = automatic).  Used by the autotuner; values are validated. */
-int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t zchunk);
-/* Times candidate tiles on the current state (restored afterwards) and
- * keeps the fastest; writes the chosen tile to *tx, *ty, *zchunk. */
-int ps_lbm_autotune(void *handle, int32_t steps, int32_t *tx, int32_t *ty, int32_t *zchunk);
+/* Step-kernel configuration: tx threads per CTA of the collide kernel, ty
+ * of the density kernel, occ the minimum resident collide CTAs per SM asked
+ * of the register allocator (0 = its choice).  Compiled: (128,256,0),
+ * (256,256,0), (128,128,0), (256,512,0), (128,256,6), (128,256,8),
+ * (256,256,3).  Used by the autotuner; values are validated. */
+int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
+/* Times the candidate configurations on the current state (restored
+ * afterwards) and keeps the fastest; writes it to *tx, *ty, *occ. */
+int ps_lbm_autotune(void *handle, int32_t steps, int32_t *tx, int32_t *ty, int32_t *occ);
 
 /* ---- lattice-spring static solve (hot path b) ---- */
 #define PS_LOAD_XSTRETCH 0 /* x stretch with tied x faces: Cxxxx (XX_P.f) */

@@ -24,6 +24,8 @@ CSRC = os.path.join(PKG, "csrc")
 ORACLE = os.path.join(ROOT, "oracle")
 BUILD = os.path.join(PKG, "_objs")
 LIB = os.path.join(PKG, "libporescale_gpu.so")
+DRIVER = os.path.join(PKG, "porescale_run")
+DRIVER_SRC = os.path.join(PKG, "driver", "porescale_run.cpp")
 ORACLE_LIB = os.path.join(ORACLE, "libps_oracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -81,6 +83,16 @@ def build_gpu(verbose: bool = False, ptxas_info: bool = False) -> str:
     return LIB
 
 
+def build_driver() -> str:
+    """porescale_run: the reference driver's LBM loop on the C ABI."""
+    lib = build_gpu()
+    if _newer(DRIVER, [DRIVER_SRC, lib, os.path.join(ROOT, "include", "porescale.h")]):
+        cxx = shutil.which("g++") or "c++"
+        _run([cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), DRIVER_SRC, "-o", DRIVER,
+              "-L" + PKG, "-lporescale_gpu", "-Wl,-rpath,$ORIGIN"])
+    return DRIVER
+
+
 def build_oracle() -> str:
     srcs = sorted(glob.glob(os.path.join(ORACLE, "*.c")))
     hdrs = glob.glob(os.path.join(ORACLE, "*.h"))
@@ -97,6 +109,7 @@ def build_all(verbose: bool = False) -> None:
         f2 = ex.submit(build_oracle)
         f1.result()
         f2.result()
+    build_driver()
 
 
 if __name__ == "__main__":

@@ -34,7 +34,7 @@ class LbmParams(C.Structure):
 class LbmInfo(C.Structure):
     _fields_ = [("nl", C.c_int64), ("nps", C.c_int64), ("npb2", C.c_int64), ("npb4", C.c_int64),
                 ("ns", C.c_int64), ("nvox", C.c_int64), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
-                ("precision", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("zchunk", C.c_int32),
+                ("precision", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("occupancy", C.c_int32),
                 ("reserved", C.c_int32), ("device_bytes", C.c_int64)]
 
 

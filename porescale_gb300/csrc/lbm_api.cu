@@ -50,8 +50,8 @@ struct Lattice {
   int32_t* d_rowstart = nullptr;
   uint2* d_rowbits = nullptr;
   void* d_col = nullptr;  // colour field of the step kernels (R per voxel)
-  void* d_pop[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer][component]
-  float* d_rho[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  void* d_pop[2] = {nullptr, nullptr};    // per buffer: 19 x pitch (red, blue) pairs
+  float2* d_rho[2] = {nullptr, nullptr};  // per buffer: (red, blue) reference densities
   LbmConst<double>* d_Kd = nullptr;
   double *d_fr = nullptr, *d_fb = nullptr;                       // state staging (reference layout)
   double *d_rr = nullptr, *d_rb = nullptr, *d_cf = nullptr, *d_cc = nullptr;  // dense fields
@@ -83,10 +83,8 @@ struct Lattice {
   BufDev buf(int b) const
   {
     BufDev r;
-    r.pop[0] = d_pop[b][0];
-    r.pop[1] = d_pop[b][1];
-    r.rho[0] = d_rho[b][0];
-    r.rho[1] = d_rho[b][1];
+    r.pop = d_pop[b];
+    r.rho = d_rho[b];
     return r;
   }
   LbmLaunchArgs args(int src, int dst) const
@@ -122,11 +120,10 @@ void free_lattice(Lattice* L)
   cudaFree(L->d_rowstart);
   cudaFree(L->d_rowbits);
   cudaFree(L->d_col);
-  for (int b = 0; b < 2; b++)
-    for (int k = 0; k < 2; k++) {
-      cudaFree(L->d_pop[b][k]);
-      cudaFree(L->d_rho[b][k]);
-    }
+  for (int b = 0; b < 2; b++) {
+    cudaFree(L->d_pop[b]);
+    cudaFree(L->d_rho[b]);
+  }
   cudaFree(L->d_Kd);
   cudaFree(L->d_fr);
   cudaFree(L->d_fb);
@@ -371,37 +368,12 @@ int launch_steps(Lattice* L, int n)
   return PS_OK;
 }
 
-constexpr size_t kMaxFusedSmem = 227 * 1024;
-
-int sm_count()
-{
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return sms;
-}
-
-// planes per CTA so that the fused grid holds about `waves` CTAs per SM
-int default_zchunk(const Lattice* L, int ty, int waves = 4)
-{
-  const long long tiles = (L->ny + ty - 1) / ty;
-  const long long want = (long long)waves * sm_count();
-  const long long nch = std::max(1LL, (want + tiles - 1) / tiles);
-  return (int)std::max(4LL, std::min<long long>(L->nz, (L->nz + nch - 1) / nch));
-}
-
-// default step configuration: the fused kernel with the largest row count
-// up to 8 whose shared-memory ring stays under 96 KB, else two launches
+// default step configuration: 128-thread collide CTAs, 256-thread density CTAs
 void default_config(Lattice* L)
 {
-  L->tx = 256;
-  L->ty = 0;
-  for (int ty = 8; ty >= 1; ty /= 2)
-    if (lbm_step_smem(L->prec, 256, ty, L->nx) <= 96 * 1024) {
-      L->ty = ty;
-      break;
-    }
-  L->zchunk = L->ty ? default_zchunk(L, L->ty) : 0;
+  L->tx = 128;
+  L->ty = 256;
+  L->zchunk = 0;
 }
 
 }  // namespace
@@ -411,7 +383,7 @@ cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunc
 {
   return PREC_DISPATCH(lbm_step_launch, prec, tx, ty, zchunk, a);
 }
-size_t lbm_step_smem(int prec, int tx, int ty, int nx) { return PREC_DISPATCH(lbm_step_smem, prec, tx, ty, nx); }
+size_t lbm_step_smem(int prec, int tx, int ty, int occ) { return PREC_DISPATCH(lbm_step_smem, prec, tx, ty, occ); }
 
 }  // namespace ps
 
@@ -487,16 +459,15 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
     }
   }
   const size_t pitch = (size_t)std::max(64LL, L->pitch);
-  const size_t popb = L->elem() * 19 * pitch;
-  for (int b = 0; b < 2; b++)
-    for (int k = 0; k < 2; k++) {
-      if (int r = dalloc(L.get(), &L->d_pop[b][k], popb)) return r;
-      PS_CUDA(cudaMemsetAsync(L->d_pop[b][k], 0, popb, L->stream));
-      if (precision >= 2) {
-        if (int r = dalloc(L.get(), &L->d_rho[b][k], sizeof(float) * pitch)) return r;
-        PS_CUDA(cudaMemsetAsync(L->d_rho[b][k], 0, sizeof(float) * pitch, L->stream));
-      }
+  const size_t popb = 2 * L->elem() * 19 * pitch;
+  for (int b = 0; b < 2; b++) {
+    if (int r = dalloc(L.get(), &L->d_pop[b], popb)) return r;
+    PS_CUDA(cudaMemsetAsync(L->d_pop[b], 0, popb, L->stream));
+    if (precision >= 2) {
+      if (int r = dalloc(L.get(), &L->d_rho[b], sizeof(float2) * pitch)) return r;
+      PS_CUDA(cudaMemsetAsync(L->d_rho[b], 0, sizeof(float2) * pitch, L->stream));
     }
+  }
   if (int r = dalloc(L.get(), &L->d_Kd, sizeof(LbmConst<double>))) return r;
   PS_CUDA(cudaMemcpyAsync(L->d_Kd, &L->Kd, sizeof(LbmConst<double>), cudaMemcpyHostToDevice, L->stream));
   default_config(L.get());
@@ -531,7 +502,7 @@ int ps_lbm_get_info(void* h, ps_lbm_info* o)
   o->precision = L->prec;
   o->tile_x = L->tx;
   o->tile_y = L->ty;
-  o->zchunk = L->zchunk;
+  o->occupancy = L->zchunk;
   o->device_bytes = L->dev_bytes;
   return PS_OK;
 }
@@ -760,14 +731,11 @@ int ps_lbm_set_tile(void* h, int32_t tx, int32_t ty, int32_t zchunk)
 {
   if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_tile: null handle");
   Lattice* L = as_lattice(h);
-  if (ty < 0 || zchunk < 0) return fail(PS_ERR_ARG, "ps_lbm_set_tile: negative ty or zchunk");
-  const size_t sm = lbm_step_smem(L->prec, tx, ty, L->nx);
-  if (sm == 0) return fail(PS_ERR_ARG, "ps_lbm_set_tile: %d threads per CTA not compiled (128 or 256)", tx);
-  if (sm > kMaxFusedSmem)
-    return fail(PS_ERR_ARG, "ps_lbm_set_tile: %d rows of %d voxels need %zu B of shared memory", ty, L->nx, sm);
+  if (lbm_step_smem(L->prec, tx, ty, zchunk) == 0)
+    return fail(PS_ERR_ARG, "ps_lbm_set_tile: (%d, %d, %d) is not a compiled step configuration", tx, ty, zchunk);
   L->tx = tx;
   L->ty = ty;
-  L->zchunk = ty == 0 ? 0 : (zchunk == 0 ? default_zchunk(L, ty) : std::min<int>(zchunk, L->nz));
+  L->zchunk = zchunk;
   return PS_OK;
 }
 
@@ -780,29 +748,21 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   // candidates: every compiled tile x a few z-chunk lengths; the state is
   // advanced an even number of steps per candidate and then restored by
   // re-running from a saved copy of the current buffer
-  const size_t popb = L->elem() * 19 * (size_t)std::max(64LL, L->pitch);
-  void* save[2] = {nullptr, nullptr};
-  float* saver[2] = {nullptr, nullptr};
-  for (int k = 0; k < 2; k++) {
-    PS_CUDA(cudaMalloc(&save[k], popb));
-    PS_CUDA(cudaMemcpyAsync(save[k], L->d_pop[L->cur][k], popb, cudaMemcpyDeviceToDevice, L->stream));
-    if (L->prec >= 2) {
-      PS_CUDA(cudaMalloc((void**)&saver[k], sizeof(float) * std::max(64LL, L->pitch)));
-      PS_CUDA(cudaMemcpyAsync(saver[k], L->d_rho[L->cur][k], sizeof(float) * std::max(64LL, L->pitch), cudaMemcpyDeviceToDevice, L->stream));
-    }
+  const size_t popb = 2 * L->elem() * 19 * (size_t)std::max(64LL, L->pitch);
+  const size_t rhob = sizeof(float2) * (size_t)std::max(64LL, L->pitch);
+  void* save = nullptr;
+  float2* saver = nullptr;
+  PS_CUDA(cudaMalloc(&save, popb));
+  PS_CUDA(cudaMemcpyAsync(save, L->d_pop[L->cur], popb, cudaMemcpyDeviceToDevice, L->stream));
+  if (L->prec >= 2) {
+    PS_CUDA(cudaMalloc((void**)&saver, rhob));
+    PS_CUDA(cudaMemcpyAsync(saver, L->d_rho[L->cur], rhob, cudaMemcpyDeviceToDevice, L->stream));
   }
   struct Cfg {
     int tx, ty, zc;
   };
-  std::vector<Cfg> cand;
-  for (int tx : {128, 256}) {
-    cand.push_back({tx, 0, 0});
-    for (int ty : {2, 4, 8, 16}) {
-      if (ty > L->ny || lbm_step_smem(L->prec, tx, ty, L->nx) > 160 * 1024) continue;
-      for (int zc : {4, 8, 16, 32})
-        if (zc <= L->nz) cand.push_back({tx, ty, zc});
-    }
-  }
+  const std::vector<Cfg> cand = {{128, 256, 0}, {256, 256, 0}, {128, 128, 0}, {256, 512, 0},
+                                 {128, 256, 6}, {128, 256, 8}, {256, 256, 3}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -833,15 +793,11 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   cudaEventDestroy(e1);
   // restore the state
   L->cur = saved_cur;
-  for (int k = 0; k < 2; k++) {
-    cudaMemcpyAsync(L->d_pop[L->cur][k], save[k], popb, cudaMemcpyDeviceToDevice, L->stream);
-    if (saver[k]) cudaMemcpyAsync(L->d_rho[L->cur][k], saver[k], sizeof(float) * std::max(64LL, L->pitch), cudaMemcpyDeviceToDevice, L->stream);
-  }
+  cudaMemcpyAsync(L->d_pop[L->cur], save, popb, cudaMemcpyDeviceToDevice, L->stream);
+  if (saver) cudaMemcpyAsync(L->d_rho[L->cur], saver, rhob, cudaMemcpyDeviceToDevice, L->stream);
   cudaStreamSynchronize(L->stream);
-  for (int k = 0; k < 2; k++) {
-    cudaFree(save[k]);
-    cudaFree(saver[k]);
-  }
+  cudaFree(save);
+  cudaFree(saver);
   L->tx = btx;
   L->ty = bty;
   L->zchunk = bzc;

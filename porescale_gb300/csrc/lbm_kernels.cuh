@@ -6,16 +6,20 @@
 //     consecutive in memory, and the fluid runs of a row stay contiguous, so
 //     nearly every fetched sector is used (a dense box wastes about half of
 //     each sector on the solid voxels between fluid runs);
-//   * populations structure-of-arrays pop[component][direction][i] for the
-//     two components (red, blue), double-buffered (src/dst swap every step);
-//   * the buffers hold POST-COLLISION populations of the previous step, so a
-//     step is a pull: node x reads direction d from x - c_d, or, when that
-//     link is a wall link, its own reflected population opp(d) (half-way
-//     bounce-back).  This is the reference's push streaming (ips) and
-//     bounce-back (ipb2, ipb4) seen from the receiving node;
+//   * populations structure-of-arrays over directions, pop[direction][i],
+//     each element the (red, blue) pair of that population (double2,
+//     float2, half2 or bfloat162), double-buffered (src/dst swap every
+//     step): one load or store moves both components;
+//   * push layout: slot (d, i) holds the POST-STREAMING population d of node
+//     i, so a node reads its 19 values from its own slots, contiguously and
+//     with no neighbour lookup.  The collision writes population d of node x
+//     into slot (d, x + c_d) when that link streams (the reference's ips
+//     entries) or, at a wall link, into slot (opp(d), x) (half-way
+//     bounce-back, the reference's ipb2 / ipb4 entries);
 //   * coord[i] (x | y<<10 | z<<20) and mask[i]: bit d-1 (d = 1..18) =
-//     incoming link d open (the link from x - c_d is one of the reference's
-//     ips entries), bits 18..23 = node on the low/high x, y, z face of the box;
+//     incoming link d open (the link from x - c_d streams; by symmetry the
+//     outgoing link opp(d) of x streams), bits 18..23 = node on the low/high
+//     x, y, z face of the box;
 //   * row tables: rowstart[row] = compact index of the first fluid voxel of
 //     row (y, z), and per 32-voxel word of the row its fluid bits and the
 //     fluid count before it.  The compact index of fluid voxel (x, y, z) is
@@ -25,15 +29,18 @@
 //     (wetting colour on non-fluid voxels, written once at creation), read
 //     27 times per interface node from L1/L2;
 //   * 16-bit storage keeps each population as a deviation from the rest
-//     equilibrium t_d * rho_ref of its own component and node; rho_ref is the
-//     component density of the node at the step that wrote it, stored in
-//     FP32 next to the populations (rho[component][i]).
+//     equilibrium t_d * rho_ref of its own component, rho_ref being the
+//     component density of the RECEIVING node at the step that wrote it
+//     (FP32 pair rho[i] next to the populations): a reader needs only its
+//     own two densities.
 //
 // One step = two launches over the fluid nodes:
-//   k_lbm_dens  pulls the populations, writes the colour (and for 16-bit
-//               storage the component densities of the new buffer);
-//   k_lbm_coll  pulls again, collides with the 27-point colour stencil and
-//               writes the post-collision populations.
+//   k_lbm_dens  reads each node's populations, writes the colour (and for
+//               16-bit storage the component densities that become the
+//               deviation reference of the populations written this step);
+//   k_lbm_coll  reads them again, collides with the 27-point colour stencil
+//               and writes the post-collision populations to their
+//               receivers.
 // The colour of all 26 neighbours must be that of the same step, which is
 // what separates the two launches.
 #pragma once
@@ -90,10 +97,11 @@ struct GeomDev {
   const uint2* rowbits;    // [ny*nz*nwords] (fluid bits, fluid count before the word)
 };
 
-// one population buffer: pop[k] -> 19*pitch elements, rho[k] -> pitch floats
+// one population buffer: pop -> 19*pitch (red, blue) pairs, rho -> pitch
+// (red, blue) FP32 reference densities (16-bit storage only)
 struct BufDev {
-  void* pop[2];
-  float* rho[2];
+  void* pop;
+  float2* rho;
 };
 
 // ---- storage policies ----------------------------------------------------
@@ -102,24 +110,28 @@ struct Store;
 template <>
 struct Store<0> {  // FP64
   using T = double;
+  using T2 = double2;
   using R = double;
   static constexpr bool kDev = false;
 };
 template <>
 struct Store<1> {  // FP32
   using T = float;
+  using T2 = float2;
   using R = float;
   static constexpr bool kDev = false;
 };
 template <>
 struct Store<2> {  // FP16 deviation
   using T = __half;
+  using T2 = __half2;
   using R = float;
   static constexpr bool kDev = true;
 };
 template <>
 struct Store<3> {  // BF16 deviation
   using T = __nv_bfloat16;
+  using T2 = __nv_bfloat162;
   using R = float;
   static constexpr bool kDev = true;
 };
@@ -134,47 +146,54 @@ struct DevScale<__half> {
   static constexpr float up = 1024.0f, down = 1.0f / 1024.0f;
 };
 
-__device__ __forceinline__ float to_f(__half h) { return __half2float(h); }
-__device__ __forceinline__ float to_f(__nv_bfloat16 h) { return __bfloat162float(h); }
-template <typename T>
-__device__ __forceinline__ T from_f(float v);
+__device__ __forceinline__ float2 to_f2(__half2 h) { return __half22float2(h); }
+__device__ __forceinline__ float2 to_f2(__nv_bfloat162 h) { return __bfloat1622float2(h); }
+template <typename T2>
+__device__ __forceinline__ T2 from_f2(float a, float b);
 template <>
-__device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
+__device__ __forceinline__ __half2 from_f2<__half2>(float a, float b) { return __floats2half2_rn(a, b); }
 template <>
-__device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+__device__ __forceinline__ __nv_bfloat162 from_f2<__nv_bfloat162>(float a, float b)
+{
+  return __floats2bfloat162_rn(a, b);
+}
 
 template <int PREC>
 struct Pop {
   using S = Store<PREC>;
   using T = typename S::T;
+  using T2 = typename S::T2;
   using R = typename S::R;
-  // population d of component k stored at compact node i
-  __device__ __forceinline__ static R load(const LbmConst<R>& K, const BufDev& b, int k, int d, int i, long long pitch)
+  // (red, blue) population d in slot (d, i); rho = the deviation references
+  // of node i (unused for full-precision storage)
+  __device__ __forceinline__ static void load(const LbmConst<R>& K, const BufDev& b, int d, int i, long long pitch,
+                                              float2 rho, R& vr, R& vb)
   {
-    const T* p = static_cast<const T*>(b.pop[k]);
+    const T2* p = static_cast<const T2*>(b.pop) + (long long)d * pitch + i;
     if constexpr (S::kDev) {
-      const float w = K.t[k][wcls(d)];
-      return w * __ldg(b.rho[k] + i) + to_f(p[(long long)d * pitch + i]) * DevScale<T>::down;
+      const float2 v = to_f2(*p);
+      vr = K.t[0][wcls(d)] * rho.x + v.x * DevScale<T>::down;
+      vb = K.t[1][wcls(d)] * rho.y + v.y * DevScale<T>::down;
     } else {
-      return __ldg(p + (long long)d * pitch + i);
+      const T2 v = __ldg(p);
+      vr = v.x;
+      vb = v.y;
     }
   }
-  // writes the 19 populations of component k at node i; rho = density the
-  // collision used for that component (the deviation reference, which the
-  // density kernel of the same step stored in b.rho[k][i])
-  __device__ __forceinline__ static void store(const LbmConst<R>& K, const BufDev& b, int k, int i, long long pitch,
-                                               const R* out, R rho)
+  // writes the (red, blue) pair (vr, vb) into slot (d, i) whose node has
+  // deviation references rho
+  __device__ __forceinline__ static void put(const LbmConst<R>& K, const BufDev& b, int d, int i, long long pitch,
+                                             R vr, R vb, float2 rho)
   {
-    T* p = static_cast<T*>(b.pop[k]);
+    T2* p = static_cast<T2*>(b.pop) + (long long)d * pitch + i;
     if constexpr (S::kDev) {
-#pragma unroll
-      for (int d = 0; d < 19; d++) {
-        const float w = K.t[k][wcls(d)];
-        p[(long long)d * pitch + i] = from_f<T>((out[d] - w * rho) * DevScale<T>::up);
-      }
+      *p = from_f2<T2>((vr - K.t[0][wcls(d)] * rho.x) * DevScale<T>::up,
+                       (vb - K.t[1][wcls(d)] * rho.y) * DevScale<T>::up);
     } else {
-#pragma unroll
-      for (int d = 0; d < 19; d++) p[(long long)d * pitch + i] = out[d];
+      T2 v;
+      v.x = vr;
+      v.y = vb;
+      *p = v;
     }
   }
 };
@@ -259,21 +278,37 @@ __device__ __forceinline__ void pull_sources(const GeomDev& G, int i, uint32_t c
   }
 }
 
-// Pulls the 19 post-streaming populations of both components of node i:
-// f[0..18] red, f[19..37] blue.
+// The 19 post-streaming populations of both components of node i from its
+// own slots: f[0..18] red, f[19..37] blue.
 template <int PREC>
-__device__ __forceinline__ void pull_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& src, int i, uint32_t m, const int* s,
-                                          typename Store<PREC>::R* f)
+__device__ __forceinline__ void read_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, int i, typename Store<PREC>::R* f)
 {
+  float2 rho = make_float2(0.f, 0.f);
+  if constexpr (Store<PREC>::kDev) rho = __ldg(src.rho + i);
 #pragma unroll
-  for (int k = 0; k < 2; k++) {
-    f[19 * k] = Pop<PREC>::load(K, src, k, 0, i, G.pitch);
+  for (int d = 0; d < 19; d++) Pop<PREC>::load(K, src, d, i, G.pitch, rho, f[d], f[19 + d]);
+}
+
+// Writes the 19 post-collision (red, blue) populations of node i to their
+// receivers (push streaming with half-way bounce-back).  s[] are the pull
+// sources of node i (pull_sources): the receiver of an outgoing population
+// e is the source of the incoming direction opp(e).
+template <int PREC>
+__device__ __forceinline__ void push_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& dst, int i, uint32_t m, const int* s,
+                                          const typename Store<PREC>::R* outr, const typename Store<PREC>::R* outb)
+{
+  constexpr bool kDev = Store<PREC>::kDev;
+  const float2 zero = make_float2(0.f, 0.f);
+  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], kDev ? __ldg(dst.rho + i) : zero);
 #pragma unroll
-    for (int d = 1; d < 19; d++) {
-      const bool open = m & (1u << (d - 1));
-      f[19 * k + d] = Pop<PREC>::load(K, src, k, open ? d : opp(d), open ? s[d] : i, G.pitch);
-    }
+  for (int e = 1; e < 19; e++) {
+    const int oe = opp(e);
+    const bool stream = m & (1u << (oe - 1));
+    const int node = stream ? s[oe] : i;
+    const int slot = stream ? e : oe;
+    Pop<PREC>::put(K, dst, slot, node, G.pitch, outr[e], outb[e], kDev ? __ldg(dst.rho + node) : zero);
   }
 }
 
@@ -335,25 +370,23 @@ __global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmCon
   using R = typename Store<PREC>::R;
   const int i = blockIdx.x * BLK + threadIdx.x;
   if (i >= G.nl) return;
-  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
-  int s[19];
-  pull_sources(G, i, c, m, s);
   R f[38];
-  pull_node<PREC>(K, G, src, i, m, s, f);
+  read_node<PREC>(K, G, src, i, f);
   R rr, rb;
   densities(f, rr, rb);
   int x, y, z;
-  unpack(c, x, y, z);
+  unpack(__ldg(G.coord + i), x, y, z);
   cc[x + G.nx * (y + G.ny * z)] = stencil_colour(rr, rb, K.wet);
-  if constexpr (Store<PREC>::kDev) {
-    dst.rho[0][i] = rr;
-    dst.rho[1][i] = rb;
-  }
+  if constexpr (Store<PREC>::kDev) dst.rho[i] = make_float2(rr, rb);
 }
 
-// collision, CSF force, recolouring; writes the post-collision populations
-template <int PREC, int BLK>
-__global__ void __launch_bounds__(BLK) k_lbm_coll(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+// collision, CSF force, recolouring; pushes the post-collision populations
+// to their receivers
+// MINB > 0 asks the register allocator for MINB resident CTAs per SM;
+// 0 keeps 640 resident threads per SM (the allocator's unconstrained
+// choice for this kernel uses too many registers for that)
+template <int PREC, int BLK, int MINB>
+__global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK) k_lbm_coll(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                   const __grid_constant__ GeomDev G, const BufDev src,
                                                   const BufDev dst, const typename Store<PREC>::R* __restrict__ cc)
 {
@@ -362,11 +395,7 @@ __global__ void __launch_bounds__(BLK) k_lbm_coll(const __grid_constant__ LbmCon
   if (i >= G.nl) return;
   const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
   R f[38];
-  {
-    int s[19];
-    pull_sources(G, i, c, m, s);
-    pull_node<PREC>(K, G, src, i, m, s, f);
-  }
+  read_node<PREC>(K, G, src, i, f);
   R rr, rb;
   densities(f, rr, rb);
   int x, y, z;
@@ -377,131 +406,9 @@ __global__ void __launch_bounds__(BLK) k_lbm_coll(const __grid_constant__ LbmCon
   auto col = [&](int a, int b, int e) -> R { return cc[v + o.x[a] + o.y[b] + o.z[e]]; };
   R outr[19], outb[19];
   node_update(K, f, f + 19, rr, rb, col, outr, outb);
-  Pop<PREC>::store(K, dst, 0, i, G.pitch, outr, rr);
-  Pop<PREC>::store(K, dst, 1, i, G.pitch, outb, rb);
-}
-
-// ---- fused step kernel ----------------------------------------------------
-// One launch per step.  A CTA owns TY consecutive full rows (y0..y0+TY-1,
-// all x) and a chunk of z-planes.  For each plane z it first computes the
-// colour of plane z+1 on its rows plus one halo row on each side into a
-// 3-plane ring in shared memory, then collides its nodes of plane z with the
-// 27-point stencil read from the ring.  Each population is read from HBM
-// about once per step (the second pull and the halo rows hit L2), against
-// twice for the two-launch form.  The fluid nodes of a (rows, plane) slab
-// are contiguous compact ranges, so the work is distributed over fluid nodes
-// only.
-template <typename R>
-struct FusedSmem {
-  static size_t bytes(int ty, int nx) { return sizeof(R) * 3 * (size_t)(ty + 2) * nx; }
-};
-
-template <int PREC, int BLK>
-__global__ void __launch_bounds__(BLK) k_lbm_fused(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
-                                                   const __grid_constant__ GeomDev G, const BufDev src,
-                                                   const BufDev dst, int ty, int zchunk)
-{
-  using R = typename Store<PREC>::R;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  R* ring = reinterpret_cast<R*>(smem_raw);
-  const int nx = G.nx, ny = G.ny, nz = G.nz;
-  const int y0 = blockIdx.x * ty;
-  const int nrow = min(ty, ny - y0);  // rows owned by this CTA
-  const int z0 = blockIdx.y * zchunk;
-  if (z0 >= nz) return;
-  const int z1 = min(z0 + zchunk, nz);
-  const int slab = (ty + 2) * nx;  // one ring plane: rows y0-1 .. y0+ty
-  const int ylo = y0 == 0 ? ny - 1 : y0 - 1;
-  const int yhi = y0 + nrow == ny ? 0 : y0 + nrow;
-
-  // colour of plane zp into ring plane `slot`: wetting colour everywhere,
-  // then the fluid nodes of the halo row below, the owned rows and the halo
-  // row above.  `own` = also store the 16-bit reference densities.
-  auto colour_plane = [&](int zp, int slot, bool own) {
-    R* pl = ring + slot * slab;
-    for (int j = threadIdx.x; j < slab; j += BLK) pl[j] = K.wet;
-    __syncthreads();
-    const int rlo = ylo + ny * zp, rmid = y0 + ny * zp, rhi = yhi + ny * zp;
-    const int a0 = __ldg(G.rowstart + rlo), n0 = __ldg(G.rowstart + rlo + 1) - a0;
-    const int a1 = __ldg(G.rowstart + rmid), n1 = __ldg(G.rowstart + rmid + nrow) - a1;
-    const int a2 = __ldg(G.rowstart + rhi), n2 = __ldg(G.rowstart + rhi + 1) - a2;
-    const int ntot = n0 + n1 + n2;
-    for (int j = threadIdx.x; j < ntot; j += BLK) {
-      int i, rs;  // node and its ring row
-      if (j < n0) {
-        i = a0 + j;
-        rs = 0;
-      } else if (j < n0 + n1) {
-        i = a1 + (j - n0);
-        rs = -1;  // from the coordinates below
-      } else {
-        i = a2 + (j - n0 - n1);
-        rs = nrow + 1;
-      }
-      const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
-      int s[19];
-      pull_sources(G, i, c, m, s);
-      R f[38];
-      pull_node<PREC>(K, G, src, i, m, s, f);
-      R rr, rb;
-      densities(f, rr, rb);
-      int x, y, z;
-      unpack(c, x, y, z);
-      if (rs < 0) rs = y - y0 + 1;
-      pl[rs * nx + x] = stencil_colour(rr, rb, K.wet);
-      if constexpr (Store<PREC>::kDev) {
-        if (own && rs >= 1 && rs <= nrow) {
-          dst.rho[0][i] = rr;
-          dst.rho[1][i] = rb;
-        }
-      }
-    }
-  };
-
-  colour_plane(z0 == 0 ? nz - 1 : z0 - 1, 0, false);
-  __syncthreads();
-  colour_plane(z0, 1, true);
-  int slo = 0, smid = 1, shi = 2;
-  for (int z = z0; z < z1; z++) {
-    const int zn = z + 1 == nz ? 0 : z + 1;
-    __syncthreads();  // the previous collision finished reading ring plane shi
-    colour_plane(zn, shi, zn >= z0 && zn < z1);
-    __syncthreads();
-    // collide the owned nodes of plane z
-    const int a = __ldg(G.rowstart + y0 + ny * z), n = __ldg(G.rowstart + y0 + nrow + ny * z) - a;
-    const R* plo = ring + slo * slab;
-    const R* pmid = ring + smid * slab;
-    const R* phi = ring + shi * slab;
-    for (int j = threadIdx.x; j < n; j += BLK) {
-      const int i = a + j;
-      const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
-      R f[38];
-      {
-        int s[19];
-        pull_sources(G, i, c, m, s);
-        pull_node<PREC>(K, G, src, i, m, s, f);
-      }
-      R rr, rb;
-      densities(f, rr, rb);
-      int x, y, zz;
-      unpack(c, x, y, zz);
-      const int r = y - y0 + 1;
-      const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
-      auto col = [&](int ax, int by, int cz) -> R {
-        const R* pl = cz == 0 ? plo : (cz == 1 ? pmid : phi);
-        const int xx = ax == 0 ? xm : (ax == 1 ? x : xp);
-        return pl[(r + by - 1) * nx + xx];
-      };
-      R outr[19], outb[19];
-      node_update(K, f, f + 19, rr, rb, col, outr, outb);
-      Pop<PREC>::store(K, dst, 0, i, G.pitch, outr, rr);
-      Pop<PREC>::store(K, dst, 1, i, G.pitch, outb, rb);
-    }
-    const int t = slo;
-    slo = smid;
-    smid = shi;
-    shi = t;
-  }
+  int s[19];
+  pull_sources(G, i, c, m, s);
+  push_node<PREC>(K, G, dst, i, m, s, outr, outb);
 }
 
 // ---- colour/density field (observables, fields) ---------------------------
@@ -515,11 +422,8 @@ __global__ void k_lbm_fields(const __grid_constant__ LbmConst<typename Store<PRE
   using R = typename Store<PREC>::R;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
-  const uint32_t c = G.coord[i], m = G.mask[i];
-  int s[19];
-  pull_sources(G, i, c, m, s);
   R f[38];
-  pull_node<PREC>(K, G, src, i, m, s, f);
+  read_node<PREC>(K, G, src, i, f);
   R a, b;
   densities(f, a, b);
   const int r = G.ref[i];
@@ -528,7 +432,7 @@ __global__ void k_lbm_fields(const __grid_constant__ LbmConst<typename Store<PRE
   const R q = (a - b) / (a + b);
   cf[r] = (double)q;
   int x, y, z;
-  unpack(c, x, y, z);
+  unpack(G.coord[i], x, y, z);
   cc[x + G.nx * (y + G.ny * z)] = (double)((q - K.wet) + K.wet);
 }
 
@@ -540,11 +444,8 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
   using R = typename Store<PREC>::R;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
-  const uint32_t m = G.mask[i];
-  int s[19];
-  pull_sources(G, i, G.coord[i], m, s);
   R f[38];
-  pull_node<PREC>(K, G, src, i, m, s, f);
+  read_node<PREC>(K, G, src, i, f);
   const long long r = G.ref[i];
 #pragma unroll
   for (int d = 0; d < 19; d++) {
@@ -553,12 +454,8 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
   }
 }
 
-// Inverse of the pull: given post-streaming populations fr, fb (reference
-// layout), writes the pre-pull buffer so that the pull reproduces them.
-// Population d of node y goes to the node it streams to (y + c_d, the pull
-// source of direction opp(d)); when that link is a wall link it is the
-// reflection of y's own population opp(d).  Links are symmetric: y -> y+c_d
-// streams exactly when y's incoming link opp(d) is open.
+// post-streaming populations fr, fb (reference layout) into the node's own
+// slots; 16-bit storage takes the node's own densities as the reference
 template <int PREC>
 __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                 const __grid_constant__ GeomDev G, const BufDev dst, const double* fr,
@@ -568,30 +465,18 @@ __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<
   using R = typename S::R;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
-  const uint32_t m = G.mask[i];
-  int s[19];
-  pull_sources(G, i, G.coord[i], m, s);
   const long long me = G.ref[i];
-  const double* fk[2] = {fr, fb};
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    R out[19];
-    R rho = R(0);
-    out[0] = (R)fk[k][19 * me];
+  float2 rho = make_float2(0.f, 0.f);
+  if constexpr (S::kDev) {
+    double sr = fr[19 * me], sb = fb[19 * me];
     for (int d = 1; d < 19; d++) {
-      const int od = opp(d);
-      const bool open = m & (1u << (od - 1));
-      const double val = open ? fk[k][19 * (long long)G.ref[s[od]] + d] : fk[k][19 * me + od];
-      out[d] = (R)val;
+      sr += fr[19 * me + d];
+      sb += fb[19 * me + d];
     }
-    if constexpr (S::kDev) {
-      double sum = fk[k][19 * me];
-      for (int d = 1; d < 19; d++) sum += fk[k][19 * me + d];
-      rho = (R)sum;
-      dst.rho[k][i] = rho;
-    }
-    Pop<PREC>::store(K, dst, k, i, G.pitch, out, rho);
+    rho = make_float2((float)sr, (float)sb);
+    dst.rho[i] = rho;
   }
+  for (int d = 0; d < 19; d++) Pop<PREC>::put(K, dst, d, i, G.pitch, (R)fr[19 * me + d], (R)fb[19 * me + d], rho);
 }
 
 // ---- check_state reductions -------------------------------------------------
@@ -613,10 +498,8 @@ __global__ void __launch_bounds__(256) k_lbm_obs(const __grid_constant__ LbmCons
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.nl;
        i += (long long)gridDim.x * blockDim.x) {
     const uint32_t cw = G.coord[i], m = G.mask[i];
-    int s[19];
-    pull_sources(G, (int)i, cw, m, s);
     R fR[38];
-    pull_node<PREC>(K, G, src, (int)i, m, s, fR);
+    read_node<PREC>(K, G, src, (int)i, fR);
     int x, y, z;
     unpack(cw, x, y, z);
     double f[38];

@@ -17,17 +17,17 @@ struct LbmLaunchArgs {
   cudaStream_t stream;
 };
 
-// returns cudaErrorInvalidValue when (tx, ty) is not a compiled configuration
-// (tx threads per CTA; ty rows per CTA of the fused kernel, 0 = two launches)
-cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunchArgs& a);
+// returns cudaErrorInvalidValue when (tx, ty, occ) is not a compiled
+// configuration (tx / ty threads per CTA of the collide / density kernel,
+// occ minimum resident collide CTAs per SM, 0 = compiler's choice)
+cudaError_t lbm_step_launch(int prec, int tx, int ty, int occ, const LbmLaunchArgs& a);
 cudaError_t lbm_fields_launch(int prec, const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc);
 cudaError_t lbm_get_state_launch(int prec, const LbmLaunchArgs& a, double* fr, double* fb);
 cudaError_t lbm_set_state_launch(int prec, const LbmLaunchArgs& a, const double* fr, const double* fb);
 cudaError_t lbm_obs_launch(int prec, const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,
                            double* out);
-// dynamic shared memory of a step configuration for rows of nx voxels
-// (0 when the configuration is not compiled, 1 for the two-launch form)
-size_t lbm_step_smem(int prec, int tx, int ty, int nx);
+// 1 when (tx, ty, occ) is a compiled step configuration, else 0
+size_t lbm_step_smem(int prec, int tx, int ty, int occ);
 
 // per-precision implementations
 #define PS_DECL_PREC(P)                                                                                     \
@@ -37,7 +37,7 @@ size_t lbm_step_smem(int prec, int tx, int ty, int nx);
   cudaError_t lbm_set_state_launch_##P(const LbmLaunchArgs& a, const double* fr, const double* fb);        \
   cudaError_t lbm_obs_launch_##P(const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,   \
                                  double* out);                                                              \
-  size_t lbm_step_smem_##P(int tx, int ty, int nx);
+  size_t lbm_step_smem_##P(int tx, int ty, int occ);
 PS_DECL_PREC(0)
 PS_DECL_PREC(1)
 PS_DECL_PREC(2)

@@ -157,49 +157,50 @@ PS_HD void mrt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r
 
 // The same collision in two-relaxation-time population form, used by the
 // FP32 paths.  With the reference's rates every even non-conserved moment
-// relaxes with S[1] (= s_nu) and every odd one with S[4] (= s_q, the TRT
-// magic 3/16 pair), and the equilibrium conserves density and momentum
-// exactly, so M^-1 S M (f - fe) equals s_nu (f - fe)^+ + s_q (f - fe)^- for
-// each opposite pair: the operator of mrt_collide in ~80 operations
-// instead of ~300, differing only by rounding.
+// relaxes with wp = s_nu and every odd one with wm = s_q (the TRT magic
+// 3/16 pair), and the equilibrium conserves density and momentum exactly,
+// so M^-1 S M (f - fe) equals s_nu (f - fe)^+ + s_q (f - fe)^- for each
+// opposite pair: the operator of mrt_collide in ~80 operations instead of
+// ~300, differing only by rounding.  F is the total body force; its
+// projections are formed per pair instead of being passed in.
 template <typename R>
-PS_HD void trt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r, const R* bf, const R* Fp,
-                       const R* S)
+PS_HD void trt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r, const R* F, R wp, R wm)
 {
   const R dt = K.dt, dti = K.dti, dt2 = K.dt2;
   const R jx = (f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14]) * dti;
   const R jy = (f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18]) * dti;
   const R jz = (f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18]) * dti;
   const R rinv = R(1) / r;
-  const R ux = (jx + bf[0] * R(0.5) * dt) * rinv;
-  const R uy = (jy + bf[1] * R(0.5) * dt) * rinv;
-  const R uz = (jz + bf[2] * R(0.5) * dt) * rinv;
+  const R ux = (jx + F[0] * R(0.5) * dt) * rinv;
+  const R uy = (jy + F[1] * R(0.5) * dt) * rinv;
+  const R uz = (jz + F[2] * R(0.5) * dt) * rinv;
   const R uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
   const R usq = (uxx + uyy + uzz) * R(0.5);
-  const R wp = S[1], wm = S[4];
-  // rest
-  pcf[0] = f[0] - wp * (f[0] - r * (t1 - usq * dt2)) + Fp[0];
-  // even part of an opposite pair's equilibrium, odd part
+  // rest (no force projection on the rest population)
+  pcf[0] = f[0] - wp * (f[0] - r * (t1 - usq * dt2));
+  // each opposite pair (a, b = opp(a)): even and odd equilibrium parts and
+  // the body-force projection rk (c_a . F) dt^2 (S1:3428-3430, 3734-3752)
   const R rq = r * R(0.25) * dt2;
   const R e1 = (t2 - usq * K.c1d6 * dt2) * r;
   const R c6 = K.c1d6 * dt, c12 = K.c1d12 * dt;
-  auto pair = [&](int a, int b, R even, R odd) {
+  const R w6 = K.c1d6 * dt2, w12 = K.c1d12 * dt2;
+  auto pair = [&](int a, int b, R even, R odd, R fa) {
     const R la = f[a] - (even + odd), lb = f[b] - (even - odd);
     const R p = (la + lb) * R(0.5), m = (la - lb) * R(0.5);
-    pcf[a] = f[a] - wp * p - wm * m + Fp[a];
-    pcf[b] = f[b] - wp * p + wm * m + Fp[b];
+    pcf[a] = f[a] - wp * p - wm * m + fa;
+    pcf[b] = f[b] - wp * p + wm * m - fa;
   };
-  pair(1, 2, e1 + rq * uxx, jx * c6);
-  pair(3, 4, e1 + rq * uyy, jy * c6);
-  pair(5, 6, e1 + rq * uzz, jz * c6);
+  pair(1, 2, e1 + rq * uxx, jx * c6, w6 * F[0]);
+  pair(3, 4, e1 + rq * uyy, jy * c6, w6 * F[1]);
+  pair(5, 6, e1 + rq * uzz, jz * c6, w6 * F[2]);
   const R ro = r * R(0.125) * dt2;
   const R e2 = (t3 - usq * K.c1d12 * dt2) * r;
-  pair(7, 10, e2 + ro * (ux + uy) * (ux + uy), (jx + jy) * c12);
-  pair(8, 9, e2 + ro * (ux - uy) * (ux - uy), (jy - jx) * c12);
-  pair(11, 14, e2 + ro * (ux + uz) * (ux + uz), (jx + jz) * c12);
-  pair(12, 13, e2 + ro * (ux - uz) * (ux - uz), (jz - jx) * c12);
-  pair(15, 18, e2 + ro * (uy + uz) * (uy + uz), (jy + jz) * c12);
-  pair(16, 17, e2 + ro * (uy - uz) * (uy - uz), (jz - jy) * c12);
+  pair(7, 10, e2 + ro * (ux + uy) * (ux + uy), (jx + jy) * c12, w12 * (F[0] + F[1]));
+  pair(8, 9, e2 + ro * (ux - uy) * (ux - uy), (jy - jx) * c12, w12 * (F[1] - F[0]));
+  pair(11, 14, e2 + ro * (ux + uz) * (ux + uz), (jx + jz) * c12, w12 * (F[0] + F[2]));
+  pair(12, 13, e2 + ro * (ux - uz) * (ux - uz), (jz - jx) * c12, w12 * (F[2] - F[0]));
+  pair(15, 18, e2 + ro * (uy + uz) * (uy + uz), (jy + jz) * c12, w12 * (F[1] + F[2]));
+  pair(16, 17, e2 + ro * (uy - uz) * (uy - uz), (jz - jy) * c12, w12 * (F[2] - F[1]));
   f[0] = pcf[0];
 }
 
@@ -239,7 +240,8 @@ PS_HD void csf_force(const LbmConst<R>& K, CC cc, R* n, R* Fs)
     ny = ny + g[s][1];
     nz = nz + g[s][2];
   }
-  const R nrm = sqrt(nx * nx + ny * ny + nz * nz);
+  constexpr bool kExact = sizeof(R) == 8;  // FP64: IEEE sqrt and divisions as the reference
+  const R n2 = nx * nx + ny * ny + nz * nz;
   // divergence of the sub-cube gradients (high half minus low half per axis,
   // in the reference's summation order)
   const R k1 = (g[1][0] + g[3][0] + g[5][0] + g[7][0] - g[0][0] - g[2][0] - g[4][0] - g[6][0]) +
@@ -247,16 +249,31 @@ PS_HD void csf_force(const LbmConst<R>& K, CC cc, R* n, R* Fs)
                (g[4][2] + g[5][2] + g[6][2] + g[7][2] - g[0][2] - g[1][2] - g[2][2] - g[3][2]);
   R m[8];
 #pragma unroll
-  for (int s = 0; s < 8; s++) m[s] = sqrt(g[s][0] * g[s][0] + g[s][1] * g[s][1] + g[s][2] * g[s][2]);
+  for (int s = 0; s < 8; s++) {
+    const R q = g[s][0] * g[s][0] + g[s][1] * g[s][1] + g[s][2] * g[s][2];
+    if constexpr (kExact)
+      m[s] = sqrt(q);
+    else
+      m[s] = q > R(0) ? q * rsqrt(q) : R(0);  // FP32 paths: hardware reciprocal square root
+  }
   const R mx = m[1] + m[3] + m[5] + m[7] - m[0] - m[2] - m[4] - m[6];
   const R my = m[3] + m[7] + m[2] + m[6] - m[0] - m[1] - m[4] - m[5];
   const R mz = m[4] + m[5] + m[6] + m[7] - m[0] - m[1] - m[2] - m[3];
   R k2 = nx * mx + ny * my + nz * mz;
-  if (nrm != R(0)) {
-    k2 = k2 / nrm;
-    nx = nx / nrm;
-    ny = ny / nrm;
-    nz = nz / nrm;
+  if constexpr (kExact) {
+    const R nrm = sqrt(n2);
+    if (nrm != R(0)) {
+      k2 = k2 / nrm;
+      nx = nx / nrm;
+      ny = ny / nrm;
+      nz = nz / nrm;
+    }
+  } else if (n2 > R(0)) {
+    const R inv = rsqrt(n2);
+    k2 = k2 * inv;
+    nx = nx * inv;
+    ny = ny * inv;
+    nz = nz * inv;
   }
   const R s = K.sig * (k2 - k1);
   n[0] = nx;
@@ -284,67 +301,99 @@ PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R r
   const bool bulk_b = !bulk_r && rr <= K.ee;
   const bool iface = !bulk_r && !bulk_b;
   // collision inputs
-  R f[19], pcf[19], Fp[19], S[19], bf[3], n[3] = {R(0), R(0), R(0)};
+  R f[19], pcf[19], bf[3], n[3] = {R(0), R(0), R(0)};
   R t1, t2, t3, r, ti2 = R(0), ti3 = R(0);
-  if (iface) {
-    R Fs[3];
-    csf_force(K, cc, n, Fs);
+  if constexpr (kExact) {
+    R Fp[19], S[19];
+    if (iface) {
+      R Fs[3];
+      csf_force(K, cc, n, Fs);
 #pragma unroll
-    for (int i = 0; i < 19; i++) f[i] = fr[i] + fb[i];
-    const R ri = rr + rb;
-    const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / ri;
-    t1 = R(1) - R(2) * ci2 * K.dt2;
-    ti2 = ci2 * K.c1d6 * K.dt2;
-    ti3 = ci2 * K.c1d12 * K.dt2;
-    t2 = ti2;
-    t3 = ti3;
-    r = ri;
-    const int ph = rr >= rb ? 0 : 1;
-    bf[0] = K.bf[ph][0] + Fs[0];
-    bf[1] = K.bf[ph][1] + Fs[1];
-    bf[2] = K.bf[ph][2] + Fs[2];
+      for (int i = 0; i < 19; i++) f[i] = fr[i] + fb[i];
+      const R ri = rr + rb;
+      const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / ri;
+      t1 = R(1) - R(2) * ci2 * K.dt2;
+      ti2 = ci2 * K.c1d6 * K.dt2;
+      ti3 = ci2 * K.c1d12 * K.dt2;
+      t2 = ti2;
+      t3 = ti3;
+      r = ri;
+      const int ph = rr >= rb ? 0 : 1;
+      bf[0] = K.bf[ph][0] + Fs[0];
+      bf[1] = K.bf[ph][1] + Fs[1];
+      bf[2] = K.bf[ph][2] + Fs[2];
 #pragma unroll
-    for (int i = 0; i < 19; i++) S[i] = K.S[ph][i];
-    const R dt2 = K.dt2;
-    Fp[0] = R(0);
-    Fp[1] = K.c1d6 * bf[0] * dt2;
-    Fp[2] = -Fp[1];
-    Fp[3] = K.c1d6 * bf[1] * dt2;
-    Fp[4] = -Fp[3];
-    Fp[5] = K.c1d6 * bf[2] * dt2;
-    Fp[6] = -Fp[5];
-    Fp[7] = K.c1d12 * (bf[0] + bf[1]) * dt2;
-    Fp[8] = K.c1d12 * (-bf[0] + bf[1]) * dt2;
-    Fp[9] = -Fp[8];
-    Fp[10] = -Fp[7];
-    Fp[11] = K.c1d12 * (bf[0] + bf[2]) * dt2;
-    Fp[12] = K.c1d12 * (-bf[0] + bf[2]) * dt2;
-    Fp[13] = -Fp[12];
-    Fp[14] = -Fp[11];
-    Fp[15] = K.c1d12 * (bf[1] + bf[2]) * dt2;
-    Fp[16] = K.c1d12 * (-bf[1] + bf[2]) * dt2;
-    Fp[17] = -Fp[16];
-    Fp[18] = -Fp[15];
-  } else {
-    const int k = bulk_r ? 0 : 1;
+      for (int i = 0; i < 19; i++) S[i] = K.S[ph][i];
+      const R dt2 = K.dt2;
+      Fp[0] = R(0);
+      Fp[1] = K.c1d6 * bf[0] * dt2;
+      Fp[2] = -Fp[1];
+      Fp[3] = K.c1d6 * bf[1] * dt2;
+      Fp[4] = -Fp[3];
+      Fp[5] = K.c1d6 * bf[2] * dt2;
+      Fp[6] = -Fp[5];
+      Fp[7] = K.c1d12 * (bf[0] + bf[1]) * dt2;
+      Fp[8] = K.c1d12 * (-bf[0] + bf[1]) * dt2;
+      Fp[9] = -Fp[8];
+      Fp[10] = -Fp[7];
+      Fp[11] = K.c1d12 * (bf[0] + bf[2]) * dt2;
+      Fp[12] = K.c1d12 * (-bf[0] + bf[2]) * dt2;
+      Fp[13] = -Fp[12];
+      Fp[14] = -Fp[11];
+      Fp[15] = K.c1d12 * (bf[1] + bf[2]) * dt2;
+      Fp[16] = K.c1d12 * (-bf[1] + bf[2]) * dt2;
+      Fp[17] = -Fp[16];
+      Fp[18] = -Fp[15];
+    } else {
+      const int k = bulk_r ? 0 : 1;
 #pragma unroll
-    for (int i = 0; i < 19; i++) {
-      f[i] = bulk_r ? fr[i] : fb[i];
-      Fp[i] = K.Fp[k][i];
-      S[i] = K.S[k][i];
+      for (int i = 0; i < 19; i++) {
+        f[i] = bulk_r ? fr[i] : fb[i];
+        Fp[i] = K.Fp[k][i];
+        S[i] = K.S[k][i];
+      }
+      t1 = K.t[k][0];
+      t2 = K.t[k][1];
+      t3 = K.t[k][2];
+      r = bulk_r ? rr : rb;
+      bf[0] = K.bf[k][0];
+      bf[1] = K.bf[k][1];
+      bf[2] = K.bf[k][2];
     }
-    t1 = K.t[k][0];
-    t2 = K.t[k][1];
-    t3 = K.t[k][2];
-    r = bulk_r ? rr : rb;
-    bf[0] = K.bf[k][0];
-    bf[1] = K.bf[k][1];
-    bf[2] = K.bf[k][2];
-  }
-  if constexpr (kExact)
     mrt_collide(K, t1, t2, t3, f, pcf, r, bf, Fp, S);
-  else
-    trt_collide(K, t1, t2, t3, f, pcf, r, bf, Fp, S);
+  } else {
+    // the same inputs without the per-direction arrays (TRT needs two rates)
+    int ph;
+    if (iface) {
+      R Fs[3];
+      csf_force(K, cc, n, Fs);
+#pragma unroll
+      for (int i = 0; i < 19; i++) f[i] = fr[i] + fb[i];
+      r = rr + rb;
+      const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / r;
+      t1 = R(1) - R(2) * ci2 * K.dt2;
+      ti2 = ci2 * K.c1d6 * K.dt2;
+      ti3 = ci2 * K.c1d12 * K.dt2;
+      t2 = ti2;
+      t3 = ti3;
+      ph = rr >= rb ? 0 : 1;
+      bf[0] = K.bf[ph][0] + Fs[0];
+      bf[1] = K.bf[ph][1] + Fs[1];
+      bf[2] = K.bf[ph][2] + Fs[2];
+    } else {
+      ph = bulk_r ? 0 : 1;
+#pragma unroll
+      for (int i = 0; i < 19; i++) f[i] = bulk_r ? fr[i] : fb[i];
+      t1 = K.t[ph][0];
+      t2 = K.t[ph][1];
+      t3 = K.t[ph][2];
+      r = bulk_r ? rr : rb;
+      bf[0] = K.bf[ph][0];
+      bf[1] = K.bf[ph][1];
+      bf[2] = K.bf[ph][2];
+    }
+    trt_collide(K, t1, t2, t3, f, pcf, r, bf, K.S[ph][1], K.S[ph][4]);
+  }
   if (iface) {
     // cosine between the colour normal and each direction
     R cs[19];

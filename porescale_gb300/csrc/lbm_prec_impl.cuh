@@ -6,7 +6,7 @@
 namespace ps {
 namespace detail {
 
-template <int PREC, int BC, int BD>
+template <int PREC, int BC, int BD, int MINB = 0>
 cudaError_t step_blk(const LbmLaunchArgs& a)
 {
   using R = typename Store<PREC>::R;
@@ -15,28 +15,7 @@ cudaError_t step_blk(const LbmLaunchArgs& a)
   const LbmConst<R>& C = *static_cast<const LbmConst<R>*>(a.K);
   R* cc = static_cast<R*>(a.cc);
   k_lbm_dens<PREC, BD><<<(unsigned)((n + BD - 1) / BD), BD, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
-  k_lbm_coll<PREC, BC><<<(unsigned)((n + BC - 1) / BC), BC, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
-  return cudaGetLastError();
-}
-
-// fused step: BLK threads, TY rows per CTA, zchunk planes per CTA
-template <int PREC, int BLK>
-cudaError_t step_fused(int ty, int zchunk, const LbmLaunchArgs& a)
-{
-  using R = typename Store<PREC>::R;
-  const GeomDev& G = a.G;
-  if (G.nl == 0) return cudaSuccess;
-  const size_t smem = FusedSmem<R>::bytes(ty, G.nx);
-  static size_t attr = 0;  // per instantiation: largest dynamic smem opted in so far
-  if (smem > 48 * 1024 && smem > attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_lbm_fused<PREC, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = smem;
-  }
-  if (zchunk <= 0) zchunk = G.nz;
-  dim3 grid((G.ny + ty - 1) / ty, (G.nz + zchunk - 1) / zchunk);
-  const LbmConst<R>& C = *static_cast<const LbmConst<R>*>(a.K);
-  k_lbm_fused<PREC, BLK><<<grid, BLK, smem, a.stream>>>(C, G, a.src, a.dst, ty, zchunk);
+  k_lbm_coll<PREC, BC, MINB><<<(unsigned)((n + BC - 1) / BC), BC, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
   return cudaGetLastError();
 }
 
@@ -89,21 +68,24 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
 }  // namespace ps
 
 // Defines the per-precision entry points declared in lbm_launch.h for
-// precision P.  A step configuration is (tx, ty, zchunk): tx threads per
-// CTA; ty >= 1 rows per CTA for the fused kernel (zchunk planes per CTA), or
-// ty == 0 for the two-launch form (tx threads for the collide kernel, 256
-// for the density kernel).
+// precision P.  A step configuration is (tx, ty, occ): tx threads per CTA
+// of the collide kernel, ty of the density kernel, occ the minimum resident
+// collide CTAs per SM requested from the register allocator (0 = its own
+// choice).
 #define PS_DEFINE_PREC(P)                                                                                  \
   namespace ps {                                                                                           \
   cudaError_t lbm_step_launch_##P(int tx, int ty, int zchunk, const LbmLaunchArgs& a)                      \
   {                                                                                                        \
-    if (ty == 0) {                                                                                         \
-      if (tx == 128) return detail::step_blk<P, 128, 256>(a);                                              \
-      if (tx == 256) return detail::step_blk<P, 256, 256>(a);                                              \
-      return cudaErrorInvalidValue;                                                                        \
+    const int occ = zchunk;                                                                                \
+    if (occ == 0) {                                                                                        \
+      if (tx == 128 && ty == 256) return detail::step_blk<P, 128, 256>(a);                                 \
+      if (tx == 256 && ty == 256) return detail::step_blk<P, 256, 256>(a);                                 \
+      if (tx == 128 && ty == 128) return detail::step_blk<P, 128, 128>(a);                                 \
+      if (tx == 256 && ty == 512) return detail::step_blk<P, 256, 512>(a);                                 \
     }                                                                                                      \
-    if (tx == 128) return detail::step_fused<P, 128>(ty, zchunk, a);                                       \
-    if (tx == 256) return detail::step_fused<P, 256>(ty, zchunk, a);                                       \
+    if (tx == 128 && ty == 256 && occ == 6) return detail::step_blk<P, 128, 256, 6>(a);                    \
+    if (tx == 128 && ty == 256 && occ == 8) return detail::step_blk<P, 128, 256, 8>(a);                    \
+    if (tx == 256 && ty == 256 && occ == 3) return detail::step_blk<P, 256, 256, 3>(a);                    \
     return cudaErrorInvalidValue;                                                                          \
   }                                                                                                        \
   cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc) \
@@ -123,10 +105,10 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
   {                                                                                                        \
     return detail::obs<P>(a, cc, partial, nblocks, out);                                                   \
   }                                                                                                        \
-  size_t lbm_step_smem_##P(int tx, int ty, int nx)                                                         \
+  size_t lbm_step_smem_##P(int tx, int ty, int occ)                                                        \
   {                                                                                                        \
-    if (tx != 128 && tx != 256) return 0;                                                                  \
-    if (ty == 0) return 1;                                                                                 \
-    return FusedSmem<typename Store<P>::R>::bytes(ty, nx);                                                 \
+    const bool base = (tx == 128 && (ty == 256 || ty == 128)) || (tx == 256 && (ty == 256 || ty == 512)); \
+    const bool hi = (tx == 128 && ty == 256 && (occ == 6 || occ == 8)) || (tx == 256 && ty == 256 && occ == 3); \
+    return (occ == 0 && base) || hi ? 1 : 0;                                                               \
   }                                                                                                        \
   }

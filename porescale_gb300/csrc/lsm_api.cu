@@ -30,8 +30,16 @@ using lsm::LsmGeom;
 
 constexpr int kBlk = 256;
 
+// A captured batch of CG iterations (CUDA graph) for one vector set
+struct CgGraph {
+  cudaGraphExec_t exec = nullptr;
+  const void* x = nullptr;
+  double tol2 = -1.0;
+};
+
 struct Springs {
   ps_lsm_params p{};
+  CgGraph g64, g32;
   int nx = 0, ny = 0, nz = 0, nvox = 0, pa = 0, jc = 0;
   long long nnode = 0, ncube = 0, ns_ref = 0;
   std::vector<uint8_t> mat, node;
@@ -71,6 +79,8 @@ void free_springs(Springs* S)
   cudaFree(S->q32);
   cudaFree(S->part);
   cudaFree(S->scal);
+  if (S->g64.exec) cudaGraphExecDestroy(S->g64.exec);
+  if (S->g32.exec) cudaGraphExecDestroy(S->g32.exec);
   if (S->stream) cudaStreamDestroy(S->stream);
   delete S;
 }
@@ -223,7 +233,15 @@ int cg(Springs* S, T* x, T* r, T* p, T* q, double tol, long long maxit, long lon
   const double tol2 = tol * tol;
   const int batch = 16;
   bool done = rr0 == 0.0;
-  while (!done && it < maxit) {
+  // the iteration needs no host decision (alpha, beta and the stop flag live
+  // on the device), so a batch of iterations is captured once into a CUDA
+  // graph and replayed until the stop flag is set
+  CgGraph& cgg = sizeof(T) == 8 ? S->g64 : S->g32;
+  if (!done && (!cgg.exec || cgg.tol2 != tol2 || cgg.x != (const void*)x)) {
+    if (cgg.exec) cudaGraphExecDestroy(cgg.exec);
+    cgg.exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    PS_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < batch; k++) {
       lsm::k_lsm_matvec<T, kBlk><<<nb, kBlk, 0, S->stream>>>(G, p, q, S->part);
       lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, nb, S->scal + 1);
@@ -233,7 +251,16 @@ int cg(Springs* S, T* x, T* r, T* p, T* q, double tol, long long maxit, long lon
       lsm::k_cg_beta<<<1, 1, 0, S->stream>>>(S->scal);
       lsm::k_cg_p<T><<<nb3, kBlk, 0, S->stream>>>(n3, S->scal, r, p);
     }
-    PS_CUDA(cudaGetLastError());
+    cudaError_t ce = cudaStreamEndCapture(S->stream, &graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "CG batch capture");
+    ce = cudaGraphInstantiate(&cgg.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "CG batch instantiate");
+    cgg.tol2 = tol2;
+    cgg.x = x;
+  }
+  while (!done && it < maxit) {
+    PS_CUDA(cudaGraphLaunch(cgg.exec, S->stream));
     if (int e = read_scal(S, h, 7)) return e;
     done = h[6] > 0.0;
     it += batch;

@@ -119,8 +119,10 @@ class Lattice:
         """cudaStream_t (as an int) that this lattice launches on."""
         return int(self._lib.ps_lbm_stream(self._h) or 0)
 
-    def set_tile(self, tx: int, ty: int, zchunk: int = 0) -> None:
-        check(self._lib.ps_lbm_set_tile(self._h, tx, ty, zchunk))
+    def set_tile(self, tx: int, ty: int, occ: int = 0) -> None:
+        """Step-kernel configuration (collide CTA size, density CTA size,
+        minimum collide CTAs per SM)."""
+        check(self._lib.ps_lbm_set_tile(self._h, tx, ty, occ))
         self.info = self.get_info()
 
     def autotune(self, steps: int = 4):

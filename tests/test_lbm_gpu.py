@@ -118,11 +118,11 @@ def test_low_precision_close_to_oracle(gpu, oracle_lib, prec, tol):
 
 @pytest.mark.parametrize("prec", [PREC_F64, PREC_F32, PREC_F16])
 def test_step_configurations_agree(gpu, prec):
-    """The fused kernel (any rows per CTA / planes per CTA, including ragged
-    last tiles and chunks) and the two-launch form give identical states."""
+    """Every compiled (collide, density) CTA-size pair gives the same state."""
     ind, p = _case(n=(11, 13, 40))
     ref = None
-    for tx, ty, zc in ((256, 0, 0), (128, 0, 0), (256, 8, 4), (128, 4, 3), (256, 2, 7), (256, 16, 40), (128, 1, 1)):
+    for tx, ty, zc in ((128, 256, 0), (256, 256, 0), (128, 128, 0), (256, 512, 0), (128, 256, 6), (128, 256, 8),
+                       (256, 256, 3)):
         with Lattice(p, ind, prec) as L:
             L.set_tile(tx, ty, zc)
             L.init_random(0.4)
@@ -131,3 +131,31 @@ def test_step_configurations_agree(gpu, prec):
         if ref is None:
             ref = st
         assert np.array_equal(st[0], ref[0]) and np.array_equal(st[1], ref[1]), (tx, ty, zc)
+
+
+def test_plain_two_phase_64_workload(gpu, oracle_lib):
+    """The plain FP64 two-phase configuration: 64^3 periodic union of
+    radius-6 spheres down to porosity 0.40, each pore voxel red or blue with
+    p = 0.5 (initdistr), tau = 1 (nu = 1/6), A = 1e-3, beta = 0.7, contact
+    angle 45 degrees (wetting colour cos 45), body force 1e-5 along x.  The
+    GPU FP64 lattice equals the oracle bit for bit after the 2 init steps
+    plus 48 steps, and the check_state observables agree to 1e-11."""
+    import math
+    ind = geo.sphere_pack(64, 0.40, 6, seed=20240530)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=1 / 6, wet=math.cos(math.radians(45.0)), bfr=(1e-5, 0, 0),
+                    bfb=(1e-5, 0, 0))
+    o = oracle_lib.OracleLattice(p, ind)
+    o.init_random(0.5)
+    o.run(50, 8)
+    with Lattice(p, ind, PREC_F64) as L:
+        assert L.nl == o.nl and L.info.nps == o.nps
+        L.init_random(0.5)
+        L.step(50)
+        gr, gb = L.get_state()
+        g = L.observables().as_dict()
+    fr, fb = o.get_state()
+    assert np.array_equal(gr, fr) and np.array_equal(gb, fb)
+    ob = o.observables()
+    for k in ("permr", "permb", "tmr", "tmb"):
+        assert g[k] == pytest.approx(ob[k], rel=1e-11), k
+    assert (g["nr"], g["nb"]) == (ob["nr"], ob["nb"])
