@@ -164,7 +164,7 @@ PS_HD void mrt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r
 // ~300, differing only by rounding.  F is the total body force; its
 // projections are formed per pair instead of being passed in.
 template <typename R>
-PS_HD void trt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r, const R* F, R wp, R wm)
+PS_HD void trt_collide(const LbmConst<R>& K, R t2, R t3, R* f, R* pcf, R r, const R* F, R wp, R wm)
 {
   const R dt = K.dt, dti = K.dti, dt2 = K.dt2;
   const R jx = (f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14]) * dti;
@@ -176,12 +176,29 @@ PS_HD void trt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r
   const R uz = (jz + F[2] * R(0.5) * dt) * rinv;
   const R uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
   const R usq = (uxx + uyy + uzz) * R(0.5);
-  // rest (no force projection on the rest population)
-  pcf[0] = f[0] - wp * (f[0] - r * (t1 - usq * dt2));
-  // each opposite pair (a, b = opp(a)): even and odd equilibrium parts and
-  // the body-force projection rk (c_a . F) dt^2 (S1:3428-3430, 3734-3752)
+  // even equilibrium part of each opposite pair (a, b = opp(a))
   const R rq = r * R(0.25) * dt2;
   const R e1 = (t2 - usq * K.c1d6 * dt2) * r;
+  const R ro = r * R(0.125) * dt2;
+  const R e2 = (t3 - usq * K.c1d12 * dt2) * r;
+  const R ev[9] = {e1 + rq * uxx,
+                   e1 + rq * uyy,
+                   e1 + rq * uzz,
+                   e2 + ro * (ux + uy) * (ux + uy),
+                   e2 + ro * (ux - uy) * (ux - uy),
+                   e2 + ro * (ux + uz) * (ux + uz),
+                   e2 + ro * (ux - uz) * (ux - uz),
+                   e2 + ro * (uy + uz) * (uy + uz),
+                   e2 + ro * (uy - uz) * (uy - uz)};
+  // The rest equilibrium is the complement r - sum of the moving ones
+  // (r (t1 - usq dt2) in exact arithmetic).  In FP32 the rounded weights
+  // t1 + 6 t2 + 12 t3 exceed 1 by ~1.5e-8, which would add wp * 1.5e-8 of
+  // mass per node and step; the complement conserves mass up to unbiased
+  // rounding.
+  const R esum = ((ev[0] + ev[1]) + ev[2]) + (((ev[3] + ev[4]) + (ev[5] + ev[6])) + (ev[7] + ev[8]));
+  pcf[0] = f[0] - wp * (f[0] - (r - R(2) * esum));
+  // each pair: odd equilibrium part and the body-force projection
+  // rk (c_a . F) dt^2 (S1:3428-3430, 3734-3752)
   const R c6 = K.c1d6 * dt, c12 = K.c1d12 * dt;
   const R w6 = K.c1d6 * dt2, w12 = K.c1d12 * dt2;
   auto pair = [&](int a, int b, R even, R odd, R fa) {
@@ -190,17 +207,15 @@ PS_HD void trt_collide(const LbmConst<R>& K, R t1, R t2, R t3, R* f, R* pcf, R r
     pcf[a] = f[a] - wp * p - wm * m + fa;
     pcf[b] = f[b] - wp * p + wm * m - fa;
   };
-  pair(1, 2, e1 + rq * uxx, jx * c6, w6 * F[0]);
-  pair(3, 4, e1 + rq * uyy, jy * c6, w6 * F[1]);
-  pair(5, 6, e1 + rq * uzz, jz * c6, w6 * F[2]);
-  const R ro = r * R(0.125) * dt2;
-  const R e2 = (t3 - usq * K.c1d12 * dt2) * r;
-  pair(7, 10, e2 + ro * (ux + uy) * (ux + uy), (jx + jy) * c12, w12 * (F[0] + F[1]));
-  pair(8, 9, e2 + ro * (ux - uy) * (ux - uy), (jy - jx) * c12, w12 * (F[1] - F[0]));
-  pair(11, 14, e2 + ro * (ux + uz) * (ux + uz), (jx + jz) * c12, w12 * (F[0] + F[2]));
-  pair(12, 13, e2 + ro * (ux - uz) * (ux - uz), (jz - jx) * c12, w12 * (F[2] - F[0]));
-  pair(15, 18, e2 + ro * (uy + uz) * (uy + uz), (jy + jz) * c12, w12 * (F[1] + F[2]));
-  pair(16, 17, e2 + ro * (uy - uz) * (uy - uz), (jz - jy) * c12, w12 * (F[2] - F[1]));
+  pair(1, 2, ev[0], jx * c6, w6 * F[0]);
+  pair(3, 4, ev[1], jy * c6, w6 * F[1]);
+  pair(5, 6, ev[2], jz * c6, w6 * F[2]);
+  pair(7, 10, ev[3], (jx + jy) * c12, w12 * (F[0] + F[1]));
+  pair(8, 9, ev[4], (jy - jx) * c12, w12 * (F[1] - F[0]));
+  pair(11, 14, ev[5], (jx + jz) * c12, w12 * (F[0] + F[2]));
+  pair(12, 13, ev[6], (jz - jx) * c12, w12 * (F[2] - F[0]));
+  pair(15, 18, ev[7], (jy + jz) * c12, w12 * (F[1] + F[2]));
+  pair(16, 17, ev[8], (jz - jy) * c12, w12 * (F[2] - F[1]));
   f[0] = pcf[0];
 }
 
@@ -371,7 +386,6 @@ PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R r
       for (int i = 0; i < 19; i++) f[i] = fr[i] + fb[i];
       r = rr + rb;
       const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / r;
-      t1 = R(1) - R(2) * ci2 * K.dt2;
       ti2 = ci2 * K.c1d6 * K.dt2;
       ti3 = ci2 * K.c1d12 * K.dt2;
       t2 = ti2;
@@ -384,7 +398,6 @@ PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R r
       ph = bulk_r ? 0 : 1;
 #pragma unroll
       for (int i = 0; i < 19; i++) f[i] = bulk_r ? fr[i] : fb[i];
-      t1 = K.t[ph][0];
       t2 = K.t[ph][1];
       t3 = K.t[ph][2];
       r = bulk_r ? rr : rb;
@@ -392,7 +405,7 @@ PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R r
       bf[1] = K.bf[ph][1];
       bf[2] = K.bf[ph][2];
     }
-    trt_collide(K, t1, t2, t3, f, pcf, r, bf, K.S[ph][1], K.S[ph][4]);
+    trt_collide(K, t2, t3, f, pcf, r, bf, K.S[ph][1], K.S[ph][4]);
   }
   if (iface) {
     // cosine between the colour normal and each direction
