@@ -125,15 +125,16 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(prec: str, nl: int):
-    """DRAM bytes per launch of the step kernel from the committed ncu summary
-    (scaled to this workload's fluid-node count), or None."""
+def load_traffic(prec: str, nl: int, fused: bool = False):
+    """DRAM bytes of one step from the committed ncu summary (scaled to this
+    workload's fluid-node count; key "<prec>" for the two-pass step,
+    "<prec>_fused" for the fused one), or None."""
     path = os.path.join(ROOT, "profiles", "lbm_step_dram.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    e = d.get(prec)
+    e = d.get(prec + ("_fused" if fused else ""))
     if not e:
         return None
     return float(e["dram_bytes_per_fluid_node"]) * nl
@@ -208,15 +209,28 @@ def lsm_leg(size=64, seed=20240601):
 def accuracy(args, cfg):
     """Relative-permeability, saturation and mass errors of the FP32 and
     16-bit forms against the FP64 lattice (which reproduces the FP64 oracle
-    bit for bit) after the same number of steps on the same workload."""
+    bit for bit) after the same number of steps on the same workload.
+
+    "f64p" is the FP64 lattice started from the same state with every
+    nonzero population moved by one unit in the last place: its distance from
+    "f64" is the flow's own sensitivity to rounding, the floor that no
+    storage precision can go below.  Errors are reported per sample (max
+    over the run) and for the mean over the second half of the run."""
     from porescale_gb300.lattice import Lattice
     ind, p, fr, fb = make_workload(cfg)
     every = args.accuracy_every or args.accuracy_steps
     hist = {}
     t_run = {}
-    for q in ("f64", "f32", "f16", "bf16"):
-        L = Lattice(p, ind, PREC_ID[q])
-        L.set_state(fr, fb)
+    legs = ("f64", "f64p", "f32", "f16", "bf16") if not args.accuracy_legs else ("f64",) + tuple(
+        args.accuracy_legs.split(","))
+    for q in legs:
+        L = Lattice(p, ind, PREC_ID[q[:3] if q == "f64p" else q])
+        if q == "f64p":
+            # exact zeros (the absent component of bulk nodes) stay zero: a
+            # denormal there would turn every bulk node into an interface node
+            L.set_state(np.where(fr != 0, np.nextafter(fr, np.inf), fr), np.where(fb != 0, np.nextafter(fb, np.inf), fb))
+        else:
+            L.set_state(fr, fb)
         rows = []
         t0 = time.perf_counter()
         done = 0
@@ -233,12 +247,199 @@ def accuracy(args, cfg):
     ref = hist["f64"]
     out = {"mode": "accuracy", "workload": cfg["workload"], "steps": args.accuracy_steps, "fluid_nodes": None,
            "seconds": t_run, "final": {q: hist[q][-1] for q in hist}, "rel_err_vs_f64": {}}
-    for q in ("f32", "f16", "bf16"):
-        e = {}
+    out["rel_err_mean_2nd_half_vs_f64"] = {}
+    h0 = len(ref) // 2
+    for q in legs[1:]:
+        e, m = {}, {}
         for k in ("permr", "permb", "sat_r", "sat_b", "tmr", "tmb"):
             e[k] = max(abs(a[k] - b[k]) / max(abs(b[k]), 1e-300) for a, b in zip(hist[q], ref))
+            ma = sum(a[k] for a in hist[q][h0:]) / len(hist[q][h0:])
+            mb = sum(b[k] for b in ref[h0:]) / len(ref[h0:])
+            m[k] = abs(ma - mb) / max(abs(mb), 1e-300)
         out["rel_err_vs_f64"][q] = e
+        out["rel_err_mean_2nd_half_vs_f64"][q] = m
     out["history"] = hist
+    print(json.dumps(out))
+
+
+def differentiation(args):
+    """The differentiation workloads.  (a) Gray partial-bounce-back TRT on a
+    size^3 box (s: seeded Gaussian noise smoothed with sigma 3, sigmoid of
+    slope 8 at the 0.35 quantile), body force 1e-6 along x, `steps` steps:
+    dk/ds by the checkpointed adjoint (checkpoint every 200 steps) against
+    FP64 central differences (h = 1e-4) at 16 seeded voxels.  (b) Two-solid
+    lattice-spring cube (radius-10 inclusions, fraction 0.25): d modulus /
+    d(alf1, bet1, alf2, bet2) from the spring energies against central
+    differences (h = 1e-4 relative), Cxxxx and Cyzyz."""
+    from porescale_gb300 import geometry
+    from porescale_gb300.gray import GrayLattice, gray_params
+    from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, SpringNetwork
+    n, T = args.adjoint_size, args.adjoint_steps
+    s = geometry.gray_field(n, sigma=3.0, slope=8.0, quantile=0.35, seed=20240604)
+    p = gray_params(tau=1.0, F=(1e-6, 0, 0), idir=1, nsteps=T, segment=200)
+    out = {"mode": "differentiation", "gray": {"size": n, "steps": T, "segment": 200, "h": 1e-4}}
+    with GrayLattice(p, s.shape) as G:
+        G.set_field(s)
+        G.permeability()  # warm-up
+        t0 = time.perf_counter()
+        k = G.permeability()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        k2, grad = G.gradient()
+        t_grad = time.perf_counter() - t0
+        rng = np.random.Generator(np.random.PCG64(20240605))
+        h = 1e-4
+        cand = np.argwhere((s > 4 * h) & (s < 1 - 4 * h))
+        picks = cand[rng.choice(len(cand), 16, replace=False)]
+        errs = []
+
+        def central(v, hh):
+            kk = []
+            for sg in (1, -1):
+                sp = s.copy()
+                sp[v] += sg * hh
+                G.set_field(sp)
+                kk.append(G.permeability())
+            return (kk[0] - kk[1]) / (2 * hh)
+
+        for v in map(tuple, picks):
+            fd, fd2 = central(v, h), central(v, 2 * h)
+            rich = (4 * fd - fd2) / 3  # removes the O(h^2) truncation term
+            errs.append({"voxel": [int(c) for c in v], "s": float(s[v]), "adjoint": float(grad[v]), "fd": fd,
+                         "fd_2h": fd2, "rel_err": abs(grad[v] - fd) / abs(fd),
+                         "rel_err_richardson": abs(grad[v] - rich) / abs(rich)})
+    out["gray"].update({"k": k, "k_gradient_run": k2, "forward_s": t_fwd, "gradient_s": t_grad,
+                        "forward_mlups": s.size * T / t_fwd / 1e6, "gradient_over_forward": t_grad / t_fwd,
+                        "max_rel_err": max(e["rel_err"] for e in errs),
+                        "max_rel_err_richardson": max(e["rel_err_richardson"] for e in errs), "checks": errs})
+    m = args.adjoint_lsm_size
+    ind = geometry.inclusions(m, 0.25, 10.0, 20240606)
+    g = 1e-3 * m / 2
+    k0 = np.array([1.0, 0.4, 0.3, 0.1])
+    lsm = {"size": m, "h_rel": 1e-4}
+    for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
+        t0 = time.perf_counter()
+        with SpringNetwork(ind, *k0, g, load, LSM_F64) as S:
+            r = S.solve(1e-12, 400000)
+            gr = S.gradients()
+        t_solve = time.perf_counter() - t0
+        fds = []
+        for i in range(4):
+            hh = 1e-4 * k0[i]
+            mods = []
+            for sg in (1, -1):
+                kk = k0.copy()
+                kk[i] += sg * hh
+                with SpringNetwork(ind, *kk, g, load, LSM_F64) as S:
+                    mods.append(S.solve(1e-12, 400000).modulus)
+            fds.append((mods[0] - mods[1]) / (2 * hh))
+        lsm[name] = {"modulus": r.modulus, "energy_modulus": gr[4], "gradient": gr[:4].tolist(), "fd": fds,
+                     "max_rel_err": max(abs(a - b) / abs(b) for a, b in zip(gr[:4], fds)), "solve_s": t_solve}
+    out["lsm"] = lsm
+    print(json.dumps(out))
+
+
+def batch_workload(nvol, seed):
+    """Subvolume specs of the batched coupled workload: edge from {48, 64,
+    96, 128}, porosity U[0.2, 0.45], sphere radius U[4, 10], initial red
+    saturation U[0.3, 0.7], all from one seeded generator."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs = []
+    for v in range(nvol):
+        specs.append({"edge": int(rng.choice([48, 64, 96, 128])), "porosity": float(rng.uniform(0.2, 0.45)),
+                      "radius": float(rng.uniform(4.0, 10.0)), "sat": float(rng.uniform(0.3, 0.7)),
+                      "seed": int(seed * 1000 + v)})
+    return specs
+
+
+def batch_mode(args):
+    """The batched coupled workload: nvol subvolumes stepped together (one
+    persistent launch per kernel and step, CUDA-graph replays, autotuned
+    configuration), then per subvolume the fluid wall load applied to a
+    two-solid lattice-spring network of the same voxels (matrix alpha 1.0,
+    beta 0.4; radius-3 inclusions at fraction 0.25 of the solid, alpha 0.3,
+    beta 0.1) solved for Cxxxx and Cyzyz.  A few subvolumes are also run on
+    the plain FP64 path for the speed and error comparison."""
+    import concurrent.futures as cf
+    import torch
+    from porescale_gb300 import geometry
+    from porescale_gb300.lattice import Lattice, LatticeBatch, make_params
+    from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_MIXED, SpringNetwork
+    specs = batch_workload(args.batch_volumes, 20240607)
+    p = make_params(B=0.7, sig=1e-3, vir=(0.8 - 0.5) / 3, vib=(1.5 - 0.5) / 3, wet=np.cos(np.radians(30.0)),
+                    bfr=(1e-6, 0, 0), bfb=(1e-6, 0, 0))
+    prec = PREC_ID[args.prec]
+    inds, lats = [], []
+    for sp in specs:
+        ind = geometry.sphere_pack(sp["edge"], sp["porosity"], sp["radius"], sp["seed"])
+        L = Lattice(p, ind, prec)
+        L.init_random(sp["sat"])
+        inds.append(ind)
+        lats.append(L)
+    nodes = sum(L.nl for L in lats)
+    T = args.batch_steps
+    peak, peak_kind = load_peaks()
+    bpn = {"f64": 640, "f32": 320, "f16": 168, "bf16": 168}[args.prec]
+    with LatticeBatch(lats) as B:
+        tile = B.autotune(4)
+        stream = torch.cuda.ExternalStream(B.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        B.step(T)
+        e1.record(stream)
+        e1.synchronize()
+        t_lbm = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+    mlups = nodes * T / (ms * 1e-3) / 1e6
+
+    def lsm_job(v):
+        ind = inds[v]
+        incl = geometry.inclusions(ind.shape, 0.25, 3.0, specs[v]["seed"] + 7)
+        ind_s = np.where(ind == 0, np.where(incl == 3, 3, 0), 1).astype(np.int32)
+        out = {}
+        for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
+            with SpringNetwork(ind_s, 1.0, 0.4, 0.3, 0.1, 1e-3 * ind.shape[2] / 2, load, LSM_MIXED) as S:
+                S.set_wall_load(lats[v], 1.0)
+                r = S.solve(1e-8, 400000)
+                out[name] = r.modulus
+        return out
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(8) as ex:
+        moduli = list(ex.map(lsm_job, range(len(lats))))
+    t_lsm = time.perf_counter() - t0
+    # plain per-volume FP64 path on the first few subvolumes: time and errors
+    nref = min(args.batch_reference, len(lats))
+    ref = []
+    t_f64 = 0.0
+    for v in range(nref):
+        L64 = Lattice(p, inds[v], PREC_ID["f64"])
+        L64.init_random(specs[v]["sat"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L64.step(T)
+        L64.sync()
+        t_f64 += time.perf_counter() - t0
+        o64, o = L64.observables(), lats[v].observables()
+        ref.append({"edge": specs[v]["edge"], "nodes": L64.nl, "permr_f64": o64.permr, "permr": o.permr,
+                    "rel_err_permr": abs(o.permr - o64.permr) / abs(o64.permr),
+                    "rel_err_permb": abs(o.permb - o64.permb) / abs(o64.permb),
+                    "rel_err_sat_r": abs(o.sat_r - o64.sat_r) / abs(o64.sat_r)})
+        L64.close()
+    ref_nodes = sum(r["nodes"] for r in ref)
+    f64_mlups = ref_nodes * T / t_f64 / 1e6 if t_f64 > 0 else None
+    out = {"mode": "batch", "volumes": len(lats), "steps": T, "precision": args.prec, "fluid_nodes": nodes,
+           "tile": list(tile), "lbm_seconds": ms * 1e-3, "lbm_wall_seconds": t_lbm, "mlups": mlups,
+           "achieved_gbs": mlups * 1e6 * bpn / 1e9, "frac": mlups * 1e6 * bpn / 1e9 / peak, "peak_kind": peak_kind,
+           "lsm_seconds": t_lsm, "subvolumes_per_s": len(lats) / (ms * 1e-3 + t_lsm),
+           "lbm_subvolumes_per_s": len(lats) / (ms * 1e-3),
+           "f64_plain_mlups": f64_mlups,
+           "f64_plain_subvolumes_per_s_estimate": (f64_mlups * 1e6 / (nodes * T / len(lats))) if f64_mlups else None,
+           "reference_volumes": ref, "moduli": moduli[:8], "specs": specs}
+    for L in lats:
+        L.close()
     print(json.dumps(out))
 
 
@@ -259,6 +460,19 @@ def main():
                     help="instead of timing: run this many steps in every precision and report the errors of "
                          "permeabilities, saturation and masses against FP64")
     ap.add_argument("--accuracy-every", type=int, default=0, help="observable cadence of the accuracy run")
+    ap.add_argument("--batch", action="store_true",
+                    help="instead of the 256^3 step: the batched coupled workload (subvolumes in shared persistent "
+                         "launches, then wall-loaded lattice-spring solves)")
+    ap.add_argument("--batch-volumes", type=int, default=48)
+    ap.add_argument("--batch-steps", type=int, default=3000)
+    ap.add_argument("--batch-reference", type=int, default=3, help="subvolumes also run on the plain FP64 path")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="instead of timing the step: the differentiation workloads (gray-lattice adjoint and "
+                         "spring-constant gradients against central differences)")
+    ap.add_argument("--adjoint-size", type=int, default=128)
+    ap.add_argument("--adjoint-steps", type=int, default=4000)
+    ap.add_argument("--adjoint-lsm-size", type=int, default=128)
+    ap.add_argument("--accuracy-legs", default="", help="comma list of legs besides f64 (default f64p,f32,f16,bf16)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default step configuration")
     ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
     args = ap.parse_args()
@@ -304,6 +518,12 @@ def main():
     if args.accuracy_steps > 0:
         accuracy(args, cfg)
         return
+    if args.adjoint:
+        differentiation(args)
+        return
+    if args.batch:
+        batch_mode(args)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -339,8 +559,12 @@ def main():
         mlups = nl * steps / t / 1e6 * world
         launch_s = t / steps
         achieved = nl * ALGO_BYTES[q] / launch_s / 1e9
+        sched = int(L.info.schedule)
         res[q] = {"mlups": mlups, "ms_per_step": launch_s * 1e3, "steps": steps, "achieved_gbs": achieved,
-                  "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.occupancy]}
+                  "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.occupancy],
+                  "schedule": ({"kind": "fused", "slab_planes": sched % 256, "lookahead": sched // 256} if sched
+                               else {"kind": "two-pass"}),
+                  "kernels_per_step": 1 if sched else 2}
         if q == args.prec:
             # e2e through the C ABI with host buffers (pinned)
             hfr = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
@@ -383,19 +607,20 @@ def main():
     if rank == 0 and not args.no_lsm:
         lsm = lsm_leg()
     h = res[args.prec]
-    traffic = load_traffic(args.prec, nl)
+    traffic = load_traffic(args.prec, nl, h["schedule"]["kind"] == "fused")
     line = {
         "metric": metric, "value": h["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": h["steps"],
         "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": args.prec, "data": "synthetic",
         "config": {"workload": cfg["workload"], "precision": args.prec, "fluid_nodes": nl, "size": args.size,
-                   "seed": cfg["seed"], "l2": "state > L2 (no flush needed)", "tile": h["tile"]},
+                   "seed": cfg["seed"], "l2": "state > L2 (no flush needed)", "tile": h["tile"],
+                   "schedule": h["schedule"]},
         "roofline": {"bound": "hbm", "achieved": h["achieved_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": h["frac"], "traffic": traffic, "peak_kind": peak_kind,
                      "algo_bytes_per_node": ALGO_BYTES[args.prec]},
         "e2e": res.get("e2e"),
         "cpu_baseline": cpu,
-        "gpu_launches": h["steps"],
+        "gpu_launches": h["steps"] * h["kernels_per_step"],
         "clocks": clocks,
         "legs": {q: res[q] for q in legs},
         "lsm": lsm,

@@ -25,7 +25,7 @@ module porescale_gpu
 
   type, bind(c) :: ps_lbm_info
     integer(c_int64_t) :: nl, nps, npb2, npb4, ns, nvox
-    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, occupancy, reserved
+    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, occupancy, schedule
     integer(c_int64_t) :: device_bytes
   end type
 
@@ -35,6 +35,13 @@ module porescale_gpu
     real(c_double) :: Qr(3), Qb(3), um(3), umr(3), umb(3), tfr(3), tfb(3), bmt(3), rmt(3)
     real(c_double) :: permr, permb, sat_r, sat_b
     integer(c_int32_t) :: isneg, nneg_rr, nneg_rb, reserved
+  end type
+
+  ! gray partial-bounce-back lattice (extension, no reference counterpart)
+  type, bind(c) :: ps_gray_params
+    real(c_double) :: tau, magic
+    real(c_double) :: F(3)
+    integer(c_int32_t) :: idir, nsteps, segment, reserved
   end type
 
   type, bind(c) :: ps_lsm_params
@@ -95,6 +102,53 @@ module porescale_gpu
       type(c_ptr), value :: handle
       type(ps_lbm_obs), intent(out) :: obs
     end function
+    integer(c_int) function ps_lbm_set_fused(handle, planes, ahead) bind(c, name='ps_lbm_set_fused')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: planes, ahead
+    end function
+    integer(c_int) function ps_lbm_autotune(handle, steps, tx, ty, occ) bind(c, name='ps_lbm_autotune')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: steps
+      integer(c_int32_t), intent(out) :: tx, ty, occ
+    end function
+    ! several subvolumes advanced together (handles(n) from ps_lbm_create)
+    integer(c_int) function ps_batch_create(handles, n, batch) bind(c, name='ps_batch_create')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), intent(in) :: handles(*)
+      integer(c_int32_t), value :: n
+      type(c_ptr), intent(out) :: batch
+    end function
+    integer(c_int) function ps_batch_step(batch, nsteps) bind(c, name='ps_batch_step')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: batch
+      integer(c_int32_t), value :: nsteps
+    end function
+    integer(c_int) function ps_batch_destroy(batch) bind(c, name='ps_batch_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: batch
+    end function
+    integer(c_int) function ps_gray_create(p, nx, ny, nz, handle) bind(c, name='ps_gray_create')
+      import :: c_int, c_int32_t, c_ptr, ps_gray_params
+      type(ps_gray_params), intent(in) :: p
+      integer(c_int32_t), value :: nx, ny, nz
+      type(c_ptr), intent(out) :: handle
+    end function
+    integer(c_int) function ps_gray_set_field(handle, s) bind(c, name='ps_gray_set_field')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(in) :: s(*)
+    end function
+    integer(c_int) function ps_gray_gradient(handle, k, dk_ds) bind(c, name='ps_gray_gradient')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: k, dk_ds(*)
+    end function
+    integer(c_int) function ps_gray_destroy(handle) bind(c, name='ps_gray_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: handle
+    end function
     integer(c_int) function ps_lbm_fields(handle, rr, rb, cf) bind(c, name='ps_lbm_fields')
       import :: c_int, c_double, c_ptr
       type(c_ptr), value :: handle
@@ -118,6 +172,33 @@ module porescale_gpu
       import :: c_int, c_double, c_ptr
       type(c_ptr), value :: handle
       real(c_double), intent(out) :: u(*)
+    end function
+    integer(c_int) function ps_lsm_gradients(handle, grad) bind(c, name='ps_lsm_gradients')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: grad(5)
+    end function
+    ! afdat(3,ns) of the coupled step (S1:3849-3882)
+    integer(c_int) function ps_lbm_wall_load(handle, rsi, afdat) bind(c, name='ps_lbm_wall_load')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), value :: rsi
+      real(c_double), intent(out) :: afdat(*)
+    end function
+    integer(c_int) function ps_lsm_set_wall_load(handle, lattice, rsi) bind(c, name='ps_lsm_set_wall_load')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle, lattice
+      real(c_double), value :: rsi
+    end function
+    ! calc_ab (S1:4008-4468): alphai(3,3) (row = force component), betai(npores)
+    integer(c_int) function ps_lsm_alpha_beta(handle, lab, npores, iipore, pres, alphai, betai) &
+        bind(c, name='ps_lsm_alpha_beta')
+      import :: c_int, c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), intent(in) :: lab(*)
+      integer(c_int32_t), value :: npores, iipore
+      real(c_double), value :: pres
+      real(c_double), intent(out) :: alphai(9), betai(*)
     end function
     integer(c_int) function ps_lsm_destroy(handle) bind(c, name='ps_lsm_destroy')
       import :: c_int, c_ptr

@@ -63,7 +63,8 @@ typedef struct {
   int64_t ns;    /* LSM solid nodes after corner dilation (S1:608) */
   int64_t nvox;  /* nx*ny*nz                                      */
   int32_t nx, ny, nz, precision;
-  int32_t tile_x, tile_y, occupancy, reserved;  /* step-kernel configuration */
+  int32_t tile_x, tile_y, occupancy;  /* step-kernel configuration */
+  int32_t schedule;     /* 0: two-pass step; else fused: slab planes + 256 x look-ahead */
   int64_t device_bytes; /* device memory held by the handle */
 } ps_lbm_info;
 
@@ -120,9 +121,42 @@ int ps_lbm_sync(void *handle);
  * (256,256,0), (128,128,0), (256,512,0), (128,256,6), (128,256,8),
  * (256,256,3).  Used by the autotuner; values are validated. */
 int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
-/* Times the candidate configurations on the current state (restored
- * afterwards) and keeps the fastest; writes it to *tx, *ty, *occ. */
+/* Fused step schedule: planes > 0 runs each step as ONE persistent launch
+ * in which CTAs take density tiles and collide tiles of z-slabs of
+ * `planes` planes from a work list (collide tiles of slab k after the
+ * density tiles of slabs k-1..k+1, `ahead` slabs of look-ahead); the
+ * collide tiles re-read their populations from L2 and density (memory) and
+ * collide (compute) work overlap.  Results are identical to the two-pass
+ * step.  Needs a configuration with tx 128 or 256 and occ 0, or tx 128
+ * and occ 6 / 8.  planes = 0 restores the two-pass step.  A collide tile
+ * whose wait gives up (bounded) makes the next synchronising call return
+ * PS_ERR_TIMEOUT. */
+int ps_lbm_set_fused(void *handle, int32_t planes, int32_t ahead);
+/* Times the candidate configurations (two-pass and fused) on the current
+ * state (restored afterwards) and keeps the fastest; writes its tile to
+ * *tx, *ty, *occ (the schedule is in ps_lbm_info.schedule). */
 int ps_lbm_autotune(void *handle, int32_t steps, int32_t *tx, int32_t *ty, int32_t *occ);
+
+/* ---- batches of lattices (extension; no counterpart in the reference) ----
+ * Many subvolumes advanced together: each step is one persistent launch of
+ * the density kernel and one of the collide kernel over a tile list that
+ * covers every lattice of the batch (uneven sizes welcome), and chunks of
+ * 20 steps are replayed from a captured CUDA graph.  The lattices stay
+ * ordinary handles (state, observables, wall load work on each); they must
+ * share the storage precision and the parameters, be distinct, and outlive
+ * the batch.  At most PS_BATCH_MAX_VOLUMES per batch. */
+#define PS_BATCH_MAX_VOLUMES 64
+int ps_batch_create(void *const *lattices, int32_t n, void **handle);
+int ps_batch_destroy(void *handle);
+/* nsteps steps of every lattice (each must have a state); results are
+ * identical to stepping each lattice on its own with the same
+ * configuration */
+int ps_batch_step(void *handle, int32_t nsteps);
+int ps_batch_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
+/* times the compiled configurations on the batch (states restored) and
+ * keeps the fastest */
+int ps_batch_autotune(void *handle, int32_t steps, int32_t *tx, int32_t *ty, int32_t *occ);
+void *ps_batch_stream(void *handle);
 
 /* ---- lattice-spring static solve (hot path b) ---- */
 #define PS_LOAD_XSTRETCH 0 /* x stretch with tied x faces: Cxxxx (XX_P.f) */
@@ -172,6 +206,40 @@ int ps_lsm_solve(void *handle, double rtol, int32_t maxit, ps_lsm_result *out);
  * grid, duplicate plane included, as LSM_displ_field) after a solve. */
 int ps_lsm_get_disp(void *handle, double *u);
 void *ps_lsm_stream(void *handle);
+/* Modulus gradients (extension; no counterpart in the reference).  After
+ * a converged ps_lsm_solve, grad[0..3] = d modulus / d(alf1, bet1, alf2,
+ * bet2) from the spring energies at the converged displacement (the
+ * stiffness is linear in each constant, so dW/dk = u^T (dK/dk) u / 2 at
+ * fixed u, and modulus = 2 W / (V strain^2)); grad[4] = 2 W / (V
+ * strain^2), the energy form of the modulus, equal to ps_lsm_result.modulus
+ * at equilibrium. */
+int ps_lsm_gradients(void *handle, double *grad);
+
+/* ---- fluid -> solid coupling (S1:3849-3882 and calc_ab S1:4008-4468) ---- */
+/* Wall load of the lattice's current state: afdat(3, ns) in the reference's
+ * LSM node order (ps_lbm_info.ns nodes, numbered as mijks by corner
+ * dilation of the solid voxels, S1:541-602).  Every wall link (the ipb2 /
+ * ipb4 entries) contributes floc = -2 (f_r + f_b - 0.99 fq) c rsi / dt^2
+ * from its bounced post-collision populations, split over the 2 nodes of
+ * the wall edge or the 4 of the wall face; FP64 sums in the reference's
+ * order.  Needs a box of at least 2 voxels per axis and a state. */
+int ps_lbm_wall_load(void *handle, double rsi, double *afdat);
+/* Makes the wall load of `lattice` (same box, same GPU) an external nodal
+ * load of the spring network for the following ps_lsm_solve calls: the
+ * solve then balances the imposed strain (gstrain, may be 0) plus this load,
+ * its net force removed (the periodic network carries no net force).
+ * Fails with PS_ERR_ARG when a loaded corner is not a node of the network.
+ * lattice == NULL removes the load.  (Static counterpart of the coupled
+ * dynamic step S1:3849-3886: the reference feeds afdat to lsm_step.) */
+int ps_lsm_set_wall_load(void *handle, void *lattice, double rsi);
+/* calc_ab (S1:4008-4468) on the last solution: alpha(3,3) = -epsi I +
+ * sigma / (V pres), epsi = fraction of voxels labelled iipore, sigma =
+ * ps_lsm_result.sigma (same layout); beta(npores) = -(sum over the faces
+ * between a pore p voxel and a solid voxel (label 0) of the mean face
+ * displacement . c) / (V pres).  lab(nx,ny,nz) = pore labels 1..npores, 0
+ * solid.  The reference evaluates them with pres = 0.01 rr0 cr2 (S1:3987). */
+int ps_lsm_alpha_beta(void *handle, const int32_t *lab, int32_t npores, int32_t iipore, double pres, double *alpha,
+                      double *beta);
 
 /* Largest box (voxel cubes) ps_lsm_stress_noalloc accepts: 128^3. */
 #define PS_LSM_NOALLOC_MAX_CUBES (2 * 1024 * 1024)
@@ -188,6 +256,36 @@ void *ps_lsm_stream(void *handle);
  * the first call on a device sets it up and should precede any stream
  * capture. */
 int ps_lsm_stress_noalloc(void *handle, const double *d_u, double *out);
+
+/* ---- gray partial-bounce-back lattice and its adjoint (extension) ---- */
+/* Single-phase D3Q19 TRT (the reference's single-phase branch, S1:3701-3710)
+ * on a dense periodic box where every voxel carries a solid fraction s in
+ * [0, 1] applied by partial bounce-back (Walsh, Burwinkle & Saar 2009):
+ * out_i = (1 - s) f*_i + s f_opp(i).  No counterpart in the reference.
+ * tau: relaxation time of the even moments; magic: TRT product (3/16);
+ * F: body force; idir (1..3): the permeability direction; nsteps from the
+ * rest state; segment: checkpoint interval of the adjoint. */
+typedef struct {
+  double tau, magic;
+  double F[3];
+  int32_t idir, nsteps, segment, reserved;
+} ps_gray_params;
+
+int ps_gray_create(const ps_gray_params *p, int32_t nx, int32_t ny, int32_t nz, void **handle);
+int ps_gray_destroy(void *handle);
+/* s(nx,ny,nz) in [0, 1] (default 0 everywhere) */
+int ps_gray_set_field(void *handle, const double *s);
+/* nsteps from rest, then k = nu (<j_idir> + F/2) / F_idir over all voxels
+ * (lattice units, FP64) */
+int ps_gray_permeability(void *handle, double *k);
+/* k and dk/ds(nx,ny,nz) by the discrete adjoint: reverse-time adjoint
+ * lattice with a population checkpoint every `segment` steps and the
+ * segment's states recomputed in between (device memory: (nsteps/segment +
+ * segment + 2) x 152 bytes per voxel).  PS_ERR_NOMEM when that does not
+ * fit. */
+int ps_gray_gradient(void *handle, double *k, double *dk_ds);
+/* populations f(19, nx*ny*nz) of the last forward run */
+int ps_gray_get_state(void *handle, double *f);
 
 /* Message of the last error on this thread (always NUL-terminated). */
 int ps_last_error(char *buf, int32_t len);

@@ -45,6 +45,7 @@ def lib():
             "or_lbm_fields": (None, [C.c_void_p, _DP, _DP, _DP]),
             "or_lbm_run": (None, [C.c_void_p, C.c_int, C.c_int]),
             "or_lbm_observables": (None, [C.c_void_p, _DP]),
+            "or_lbm_wall_load": (None, [C.c_void_p, C.c_double, _DP]),
             "or_collision": (None, [C.c_double, C.c_double, C.c_double, _DP, _DP, C.c_double, _DP, _DP, _DP,
                                     C.c_double, C.c_double, C.c_double]),
             "or_collmatr_trt": (None, [C.c_double, _DP]),
@@ -134,10 +135,54 @@ class OracleLattice:
     def run(self, nsteps, nthreads=1):
         lib().or_lbm_run(self._h, int(nsteps), int(nthreads))
 
+    def wall_load(self, rsi):
+        """afdat as (ns, 3) after at least one step (S1:3849-3882)."""
+        out = np.zeros((self.ns, 3))
+        lib().or_lbm_wall_load(self._h, float(rsi), _d(out))
+        return out
+
     def observables(self) -> dict:
         out = np.zeros(41)
         lib().or_lbm_observables(self._h, _d(out))
         return dict(zip(OBS_NAMES, out.tolist()))
+
+
+class OrGrayParams(C.Structure):
+    _fields_ = [("tau", C.c_double), ("magic", C.c_double), ("F", C.c_double * 3), ("idir", C.c_int32),
+                ("nsteps", C.c_int32), ("segment", C.c_int32), ("reserved", C.c_int32)]
+
+
+def _gray_sigs(L):
+    L.or_gray_forward.restype = C.c_double
+    L.or_gray_forward.argtypes = [C.POINTER(OrGrayParams), C.c_int, C.c_int, C.c_int, _DP, _DP]
+    L.or_gray_gradient.restype = C.c_double
+    L.or_gray_gradient.argtypes = [C.POINTER(OrGrayParams), C.c_int, C.c_int, C.c_int, _DP, _DP]
+
+
+def gray_params(tau, magic, F, idir, nsteps, segment=1):
+    return OrGrayParams(tau, magic, (C.c_double * 3)(*F), idir, nsteps, segment, 0)
+
+
+def gray_forward(p, s: np.ndarray, want_state=False):
+    """(k, f(n, 19) or None) of the gray lattice, s shaped (nz, ny, nx)."""
+    L = lib()
+    _gray_sigs(L)
+    s = np.ascontiguousarray(s, np.float64)
+    nz, ny, nx = s.shape
+    f = np.zeros((s.size, 19)) if want_state else None
+    k = L.or_gray_forward(C.byref(p), nx, ny, nz, _d(s), _d(f) if f is not None else None)
+    return k, f
+
+
+def gray_gradient(p, s: np.ndarray):
+    """(k, dk/ds shaped like s) by the oracle's adjoint."""
+    L = lib()
+    _gray_sigs(L)
+    s = np.ascontiguousarray(s, np.float64)
+    nz, ny, nx = s.shape
+    dk = np.zeros_like(s)
+    k = L.or_gray_gradient(C.byref(p), nx, ny, nz, _d(s), _d(dk))
+    return k, dk
 
 
 def _lsm_sigs(L):
@@ -150,6 +195,7 @@ def _lsm_sigs(L):
         "or_lsm_forces": (None, [C.c_void_p, _DP, _DP]),
         "or_lsm_relax": (C.c_int64, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double]),
         "or_lsm_cg": (C.c_int64, [C.c_void_p, C.c_double, C.c_int64, _DP]),
+        "or_lsm_set_load": (None, [C.c_void_p, _DP]),
         "or_lsm_get_disp": (None, [C.c_void_p, _DP]),
         "or_lsm_set_disp": (None, [C.c_void_p, _DP]),
         "or_lsm_stress": (None, [C.c_void_p, _DP]),
@@ -212,6 +258,14 @@ class OracleSprings:
         rel = C.c_double()
         it = int(lib().or_lsm_cg(self._h, rtol, int(maxit), C.byref(rel)))
         return it, rel.value
+
+    def set_load(self, f):
+        """external nodal load (ns, 3) in node order for the next cg(); None removes it"""
+        if f is None:
+            lib().or_lsm_set_load(self._h, None)
+        else:
+            f = np.ascontiguousarray(f, np.float64)
+            lib().or_lsm_set_load(self._h, _d(f))
 
     def disp(self):
         u = np.zeros((self.ns, 3))

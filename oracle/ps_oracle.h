@@ -57,11 +57,28 @@ void or_lbm_fields(const or_lbm *o, double *rr, double *rb, double *cf);
 void or_lbm_run(or_lbm *o, int nsteps, int nthreads);
 /* check_state reductions S1:2988-3202; out layout documented in the .c */
 void or_lbm_observables(const or_lbm *o, double *out);
+/* wall load afdat(3, ns) of the last step (S1:3849-3882) from the
+ * post-collision populations pcfr/pcfb, loops and sums in the reference's
+ * order; needs at least one step run */
+void or_lbm_wall_load(const or_lbm *o, double rsi, double *afdat);
 /* single-node kernels exposed for unit tests */
 void or_collision(double t1, double t2, double t3, double *f, double *pcf, double r,
                   const double bf[3], const double Fp[19], const double S[19],
                   double dt, double dti, double dt2);
 void or_collmatr_trt(double sv, double S[19]);
+
+/* ---------------- gray partial-bounce-back lattice (extension) ----------
+ * single-phase TRT on a dense periodic box, partial bounce-back by the
+ * solid fraction s(nx,ny,nz); no reference counterpart (ps_oracle_gray.c) */
+typedef struct {
+  double tau, magic;
+  double F[3];
+  int32_t idir, nsteps, segment, reserved;
+} or_gray_params;
+/* nsteps from rest; returns k = nu (<j_idir> + F/2) / F; f_out (19, n) or NULL */
+double or_gray_forward(const or_gray_params *p, int nx, int ny, int nz, const double *s, double *f_out);
+/* k and dk/ds by the discrete adjoint (all states kept: small boxes only) */
+double or_gray_gradient(const or_gray_params *p, int nx, int ny, int nz, const double *s, double *dk);
 
 /* ---------------- lattice-spring model ---------------- */
 typedef struct or_lsm or_lsm;
@@ -80,6 +97,8 @@ void or_lsm_forces(const or_lsm *o, const double *u, double *a);
 int64_t or_lsm_relax(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol);
 /* FP64 CG on the same operator over unique nodes; returns iterations */
 int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres);
+/* external nodal load (3, ns) added to the CG right-hand side; NULL = none */
+void or_lsm_set_load(or_lsm *o, const double *f);
 void or_lsm_get_disp(const or_lsm *o, double *u);
 void or_lsm_set_disp(or_lsm *o, const double *u);
 /* calc_stress XX:1628-1997: out[0..8] = <sigma> (3x3, row major),

@@ -722,3 +722,40 @@ void or_lbm_observables(const or_lbm *o, double *out)
   v[34] = isneg; v[35] = nnr; v[36] = nnb; v[37] = permr; v[38] = permb; v[39] = nr_cf; v[40] = nb_cf;
   memcpy(out, v, sizeof v);
 }
+
+/* S1:3849-3882: afdat = 0, then for every ipb2 entry (node n, incoming
+ * direction d, LSM nodes n3 n4) floc = -2((pcfr + pcfb)(niv(d), n) - ppp
+ * fq(d)) vv(:, d) rsdti2 is added with weight 0.5 to both nodes, then for
+ * every ipb4 entry with weight 0.25 to its four nodes.  fq (S1:3417) and
+ * rsdti2 = rsi dti dti (S1:3413), ppp = 0.99 (S1:3406). */
+void or_lbm_wall_load(const or_lbm *o, double rsi, double *afdat)
+{
+  const double dt2 = o->dt2, dti = o->dti;
+  const double c1d6 = 1.0 / 6.0, c1d12 = 1.0 / 12.0, ppp = 0.99;
+  double fq[19];
+  fq[0] = o->p.rr0 * 0.0;
+  for (int d = 1; d < 19; d++) fq[d] = o->p.rr0 * (o->p.cr2 * (d < 7 ? c1d6 : c1d12) * dt2);
+  const double rsdti2 = rsi * dti * dti;
+  for (int64_t i = 0; i < 3 * o->ns; i++) afdat[i] = 0.0;
+  for (int64_t e = 0; e < o->npb2; e++) {
+    const int32_t *r = o->ipb2 + 4 * e;
+    const int64_t n = r[0] - 1;
+    const int d = r[1] - 1, db = o->niv[d] - 1;
+    const double q = (o->pcfr[19 * n + db] + o->pcfb[19 * n + db]) - ppp * fq[d];
+    for (int c = 0; c < 3; c++) {
+      const double floc = -2.0 * q * (double)CV[d][c] * rsdti2;
+      afdat[3 * (int64_t)(r[2] - 1) + c] = afdat[3 * (int64_t)(r[2] - 1) + c] + floc * 0.5;
+      afdat[3 * (int64_t)(r[3] - 1) + c] = afdat[3 * (int64_t)(r[3] - 1) + c] + floc * 0.5;
+    }
+  }
+  for (int64_t e = 0; e < o->npb4; e++) {
+    const int32_t *r = o->ipb4 + 6 * e;
+    const int64_t n = r[0] - 1;
+    const int d = r[1] - 1, db = o->niv[d] - 1;
+    const double q = (o->pcfr[19 * n + db] + o->pcfb[19 * n + db]) - ppp * fq[d];
+    for (int c = 0; c < 3; c++) {
+      const double floc = -2.0 * q * (double)CV[d][c] * rsdti2;
+      for (int k = 2; k < 6; k++) afdat[3 * (int64_t)(r[k] - 1) + c] = afdat[3 * (int64_t)(r[k] - 1) + c] + floc * 0.25;
+    }
+  }
+}

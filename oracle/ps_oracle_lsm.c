@@ -47,6 +47,7 @@ struct or_lsm {
   int32_t *icors, *bon, *ang, *tie;
   double *sbond, *abond;
   double *r, *v, *a; /* displacement, velocity, acceleration (3*ns) */
+  double *load;       /* external nodal load (3*ns) or NULL */
   double anf[48][9], bn[9][3], vb[9][3], vn[19][3], vx[19][3];
 };
 
@@ -310,6 +311,7 @@ void or_lsm_destroy(or_lsm *o)
   if (!o) return;
   free(o->ind); free(o->num); free(o->icors); free(o->bon); free(o->sbond);
   free(o->ang); free(o->abond); free(o->tie); free(o->r); free(o->v); free(o->a);
+  free(o->load);
   free(o);
 }
 
@@ -431,6 +433,11 @@ int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres)
   forces(o, full, f, 1);
   for (int64_t i = 0; i < ns; i++)
     for (int d = 0; d < 3; d++) r[3 * i + d] = dup[i] ? 0.0 : f[3 * i + d];
+  /* external load: equilibrium f(u) + load = 0; a duplicate node's load
+   * acts on its tied partner */
+  if (o->load)
+    for (int64_t i = 0; i < ns; i++)
+      for (int d = 0; d < 3; d++) r[3 * (dup[i] ? partner[i] : i) + d] += o->load[3 * i + d];
   int64_t nu = ns - o->ntie;
   /* remove the rigid-translation component */
   for (int d = 0; d < 3; d++) {
@@ -646,4 +653,16 @@ void or_lsm_stress(const or_lsm *o, double *out)
   out[9] = s / (vcell * strain / nax);
   out[10] = strain / nax;
   out[11] = (double)ncub;
+}
+
+/* external nodal load (3, ns) in node order for the following or_lsm_cg
+ * (the static counterpart of the coupled step's afdat, S1:3849-3886);
+ * NULL removes it */
+void or_lsm_set_load(or_lsm *o, const double *f)
+{
+  free(o->load);
+  o->load = NULL;
+  if (!f) return;
+  o->load = (double *)malloc(sizeof(double) * 3 * (o->ns + 1));
+  memcpy(o->load, f, sizeof(double) * 3 * o->ns);
 }

@@ -31,9 +31,11 @@ ORACLE_LIB = os.path.join(ORACLE, "libps_oracle.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                       "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-# per-TU extra flags: the FP64 LBM kernels must not contract a*b+c into FMA
+# per-TU extra flags: the FP64 LBM and gray-lattice kernels must not contract
+# a*b+c into FMA (bit-exact against the FP64 oracle)
 TU_FLAGS = {
     "lbm_prec_f64.cu": ["--fmad=false"],
+    "gray_api.cu": ["--fmad=false"],
 }
 
 

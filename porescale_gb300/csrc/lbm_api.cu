@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "lbm_launch.h"
+#include "ps_coupling.h"
 #include "ps_common.h"
 
 namespace ps {
@@ -57,6 +58,15 @@ struct Lattice {
   double *d_rr = nullptr, *d_rb = nullptr, *d_cf = nullptr, *d_cc = nullptr;  // dense fields
   double* d_partial = nullptr;
   double* d_obs = nullptr;
+  double* d_wall = nullptr;  // wall load on the corner box [3][nvox]
+  // fused step schedule (0 planes: the two-pass step)
+  int fused_planes = 0, fused_ahead = 1;
+  std::vector<int32_t> rowstart_h;  // host copy of the row starts
+  int4* d_items = nullptr;
+  int* d_ntd = nullptr;
+  unsigned* d_ctr = nullptr;
+  int* d_err = nullptr;
+  int nitems = 0, nslab = 0, sched_tx = 0, sched_planes = 0, sched_ahead = 0;
   int obs_blocks = 0;
   int cur = 0;           // buffer holding the current state
   bool have_state = false;
@@ -115,6 +125,11 @@ void free_lattice(Lattice* L)
 {
   if (!L) return;
   cudaFree(L->d_coord);
+  cudaFree(L->d_wall);
+  cudaFree(L->d_items);
+  cudaFree(L->d_ntd);
+  cudaFree(L->d_ctr);
+  cudaFree(L->d_err);
   cudaFree(L->d_mask);
   cudaFree(L->d_ref);
   cudaFree(L->d_rowstart);
@@ -357,16 +372,98 @@ int ensure_fields(Lattice* L)
 
 Lattice* as_lattice(void* h) { return static_cast<Lattice*>(h); }
 
+// the work list of the fused step for the current (tx, planes, ahead):
+// z-slabs of `planes` planes; density tiles of the slabs in the order
+// S-1, 0, 1, ..., S-2 and the collide tiles of slab k after the density
+// tiles of the `ahead`-th slab past the last one it needs (k-1, k, k+1)
+int ensure_schedule(Lattice* L)
+{
+  const int tx = L->tx, P = L->fused_planes, A = L->fused_ahead;
+  if (L->d_items && L->sched_tx == tx && L->sched_planes == P && L->sched_ahead == A) return PS_OK;
+  const int S = (L->nz + P - 1) / P;
+  std::vector<int> first(S + 1);
+  for (int k = 0; k <= S; k++) first[k] = L->rowstart_h[(size_t)std::min(L->nz, k * P) * L->ny];
+  std::vector<int> ntd(S);
+  auto pos = [&](int sl) { return sl == S - 1 ? 0 : sl + 1; };
+  std::vector<std::vector<int>> after(S);  // collide slabs emitted after dens position p
+  for (int k = 0; k < S; k++) {
+    const int q = std::max(pos((k + S - 1) % S), std::max(pos(k), pos((k + 1) % S)));
+    after[std::min(S - 1, q + A - 1)].push_back(k);
+  }
+  std::vector<int4> items;
+  auto tiles = [&](int kind, int sl) {
+    int n = 0;
+    for (int b = first[sl]; b < first[sl + 1]; b += tx, n++)
+      items.push_back(make_int4(kind | (sl << 1), b, std::min(b + tx, first[sl + 1]), 0));
+    return n;
+  };
+  for (int p = 0; p < S; p++) {
+    const int sl = p == 0 ? S - 1 : p - 1;
+    ntd[sl] = tiles(0, sl);
+    for (int k : after[p]) tiles(1, k);
+  }
+  cudaFree(L->d_items);
+  cudaFree(L->d_ntd);
+  cudaFree(L->d_ctr);
+  L->d_items = nullptr;
+  L->d_ntd = nullptr;
+  L->d_ctr = nullptr;
+  PS_CUDA(cudaMalloc((void**)&L->d_items, sizeof(int4) * std::max<size_t>(1, items.size())));
+  PS_CUDA(cudaMalloc((void**)&L->d_ntd, sizeof(int) * S));
+  PS_CUDA(cudaMalloc((void**)&L->d_ctr, sizeof(unsigned) * (S + 1)));
+  if (!L->d_err) {
+    PS_CUDA(cudaMalloc((void**)&L->d_err, sizeof(int)));
+    PS_CUDA(cudaMemsetAsync(L->d_err, 0, sizeof(int), L->stream));
+  }
+  if (!items.empty())
+    PS_CUDA(cudaMemcpyAsync(L->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, L->stream));
+  PS_CUDA(cudaMemcpyAsync(L->d_ntd, ntd.data(), sizeof(int) * S, cudaMemcpyHostToDevice, L->stream));
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  L->nitems = (int)items.size();
+  L->nslab = S;
+  L->sched_tx = tx;
+  L->sched_planes = P;
+  L->sched_ahead = A;
+  return PS_OK;
+}
+
 int launch_steps(Lattice* L, int n)
 {
+  if (L->fused_planes > 0)
+    if (int r = ensure_schedule(L)) return r;
   for (int s = 0; s < n; s++) {
     LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
-    cudaError_t e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, L->zchunk, a);
+    cudaError_t e;
+    if (L->fused_planes > 0) {
+      FusedArgs f;
+      f.items = L->d_items;
+      f.nitems = L->nitems;
+      f.nslab = L->nslab;
+      f.ntd = L->d_ntd;
+      f.ctr = L->d_ctr;
+      f.err = L->d_err;
+      e = PREC_DISPATCH(lbm_fused_launch, L->prec, L->tx, L->zchunk, a, f);
+    } else {
+      e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, L->zchunk, a);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
     L->cur = 1 - L->cur;
   }
   return PS_OK;
 }
+
+// after a synchronisation: PS_ERR_TIMEOUT when a fused step gave up waiting
+int check_fused(Lattice* L)
+{
+  if (!L->d_err) return PS_OK;
+  int err = 0;
+  PS_CUDA(cudaMemcpy(&err, L->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!err) return PS_OK;
+  PS_CUDA(cudaMemset(L->d_err, 0, sizeof(int)));
+  return fail(PS_ERR_TIMEOUT, "fused step: a collide tile gave up waiting for its density tiles; the state is invalid");
+}
+
+bool fused_config(int tx, int occ) { return (occ == 0 && (tx == 128 || tx == 256)) || (tx == 128 && (occ == 6 || occ == 8)); }
 
 // default step configuration: 128-thread collide CTAs, 256-thread density CTAs
 void default_config(Lattice* L)
@@ -374,6 +471,148 @@ void default_config(Lattice* L)
   L->tx = 128;
   L->ty = 256;
   L->zchunk = 0;
+}
+
+int wall_load_box(Lattice* L, double rsi)
+{
+  if (!L->have_state) return fail(PS_ERR_STATE, "wall load: no state set");
+  if (L->nx < 2 || L->ny < 2 || L->nz < 2) return fail(PS_ERR_ARG, "wall load: needs a box of at least 2 voxels per axis");
+  if (!L->d_wall)
+    if (int r = dalloc(L, &L->d_wall, sizeof(double) * 3 * (size_t)L->nvox)) return r;
+  // fq (S1:3417), rsdti2 = rsi dti^2 (S1:3413), ppp = 0.99 (S1:3406)
+  const double dt2 = L->p.dt * L->p.dt, dti = 1.0 / L->p.dt;
+  const double fq1 = L->p.rr0 * (L->p.cr2 * (1.0 / 6.0) * dt2), fq2 = L->p.rr0 * (L->p.cr2 * (1.0 / 12.0) * dt2);
+  const double rsdti2 = rsi * dti * dti;
+  LbmLaunchArgs a = L->args(L->cur, L->cur);
+  cudaError_t e = PREC_DISPATCH(lbm_wall_load_launch, L->prec, a, fq1, fq2, 0.99, rsdti2, L->d_wall);
+  if (e != cudaSuccess) return cuda_fail(e, "wall load kernel");
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  return PS_OK;
+}
+
+// ---- batches: many lattices advanced by the same launches ---------------
+struct Batch {
+  std::vector<Lattice*> L;
+  int prec = 0;
+  cudaStream_t stream = nullptr;
+  int tx = 128, ty = 256, occ = 0;
+  int2 *d_tc = nullptr, *d_td = nullptr;
+  int ntc = 0, ntd = 0, tiles_tx = 0, tiles_ty = 0;
+  cudaGraphExec_t exec = nullptr;  // kGraphSteps steps from the parity pattern graph_cur
+  std::vector<int> graph_cur;
+  int g_tx = 0, g_ty = 0, g_occ = -1;
+  long long nodes = 0;
+};
+constexpr int kGraphSteps = 20;  // even: a replay returns every lattice to its buffer parity
+
+void free_batch(Batch* B)
+{
+  if (!B) return;
+  cudaFree(B->d_tc);
+  cudaFree(B->d_td);
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+}
+
+int batch_tiles(Batch* B)
+{
+  if (B->tiles_tx == B->tx && B->tiles_ty == B->ty && B->d_tc) return PS_OK;
+  auto build = [&](int blk, int2** d, int* n) -> int {
+    std::vector<int2> t;
+    for (size_t v = 0; v < B->L.size(); v++)
+      for (long long b = 0; b < B->L[v]->nl; b += blk) t.push_back(make_int2((int)v, (int)b));
+    cudaFree(*d);
+    *d = nullptr;
+    PS_CUDA(cudaMalloc((void**)d, sizeof(int2) * std::max<size_t>(1, t.size())));
+    if (!t.empty()) PS_CUDA(cudaMemcpyAsync(*d, t.data(), sizeof(int2) * t.size(), cudaMemcpyHostToDevice, B->stream));
+    PS_CUDA(cudaStreamSynchronize(B->stream));
+    *n = (int)t.size();
+    return PS_OK;
+  };
+  if (int r = build(B->tx, &B->d_tc, &B->ntc)) return r;
+  if (int r = build(B->ty, &B->d_td, &B->ntd)) return r;
+  B->tiles_tx = B->tx;
+  B->tiles_ty = B->ty;
+  return PS_OK;
+}
+
+// descriptor table of one step in which lattice v reads buffer cur_v ^ flip
+VolTable batch_table(const Batch* B, int flip)
+{
+  VolTable T;
+  memset(&T, 0, sizeof T);
+  for (size_t v = 0; v < B->L.size(); v++) {
+    const Lattice* L = B->L[v];
+    const int c = L->cur ^ flip;
+    T.v[v].G = L->geom();
+    T.v[v].src = L->buf(c);
+    T.v[v].dst = L->buf(c ^ 1);
+    T.v[v].cc = L->d_col;
+  }
+  return T;
+}
+
+cudaError_t batch_launch(Batch* B, const VolTable& T)
+{
+  BatchLaunchArgs a;
+  a.K = B->prec == 0 ? (const void*)&B->L[0]->Kd : (const void*)&B->L[0]->Kf;
+  a.T = &T;
+  a.tiles_c = B->d_tc;
+  a.ntc = B->ntc;
+  a.tiles_d = B->d_td;
+  a.ntd = B->ntd;
+  a.stream = B->stream;
+  return PREC_DISPATCH(lbm_batch_step_launch, B->prec, B->tx, B->ty, B->occ, a);
+}
+
+// n steps of every lattice of the batch (graph replays of kGraphSteps, the
+// rest launched directly); the caller has synchronised the lattices
+int batch_steps(Batch* B, int n)
+{
+  if (int r = batch_tiles(B)) return r;
+  std::vector<int> cur;
+  for (Lattice* L : B->L) cur.push_back(L->cur);
+  const bool valid = B->exec && B->g_tx == B->tx && B->g_ty == B->ty && B->g_occ == B->occ && B->graph_cur == cur;
+  if (n >= kGraphSteps && !valid) {
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    B->exec = nullptr;
+    // first-call set-up of the launchers happens outside the capture
+    {
+      BatchLaunchArgs a{};
+      a.K = B->prec == 0 ? (const void*)&B->L[0]->Kd : (const void*)&B->L[0]->Kf;
+      VolTable T = batch_table(B, 0);
+      a.T = &T;
+      a.stream = B->stream;
+      cudaError_t e = PREC_DISPATCH(lbm_batch_step_launch, B->prec, B->tx, B->ty, B->occ, a);
+      if (e != cudaSuccess) return cuda_fail(e, "batch step set-up");
+    }
+    PS_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < kGraphSteps && e == cudaSuccess; k++) e = batch_launch(B, batch_table(B, k & 1));
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(B->stream, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return cuda_fail(e, "batch step capture");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "batch step capture");
+    e = cudaGraphInstantiate(&B->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "batch graph instantiate");
+    B->g_tx = B->tx;
+    B->g_ty = B->ty;
+    B->g_occ = B->occ;
+    B->graph_cur = cur;
+  }
+  int done = 0;
+  for (; B->exec && n - done >= kGraphSteps; done += kGraphSteps) PS_CUDA(cudaGraphLaunch(B->exec, B->stream));
+  for (; done < n; done++) {
+    cudaError_t e = batch_launch(B, batch_table(B, done & 1));
+    if (e != cudaSuccess) return cuda_fail(e, "batch step");
+  }
+  for (Lattice* L : B->L) L->cur ^= (n & 1);
+  return PS_OK;
 }
 
 }  // namespace
@@ -384,6 +623,17 @@ cudaError_t lbm_step_launch(int prec, int tx, int ty, int zchunk, const LbmLaunc
   return PREC_DISPATCH(lbm_step_launch, prec, tx, ty, zchunk, a);
 }
 size_t lbm_step_smem(int prec, int tx, int ty, int occ) { return PREC_DISPATCH(lbm_step_smem, prec, tx, ty, occ); }
+
+int lbm_wall_load_box(void* h, double rsi, const double** d_box, int dims[3])
+{
+  Lattice* L = as_lattice(h);
+  if (int r = wall_load_box(L, rsi)) return r;
+  *d_box = L->d_wall;
+  dims[0] = L->nx;
+  dims[1] = L->ny;
+  dims[2] = L->nz;
+  return PS_OK;
+}
 
 }  // namespace ps
 
@@ -442,6 +692,7 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
     PS_CUDA(cudaMemcpyAsync(L->d_ref, H.ref.data(), sizeof(int32_t) * L->nl, cudaMemcpyHostToDevice, L->stream));
   }
   PS_CUDA(cudaMemcpyAsync(L->d_rowstart, H.rowstart.data(), sizeof(int32_t) * H.rowstart.size(), cudaMemcpyHostToDevice, L->stream));
+  L->rowstart_h = H.rowstart;
   PS_CUDA(cudaMemcpyAsync(L->d_rowbits, H.rowbits.data(), sizeof(uint2) * H.rowbits.size(), cudaMemcpyHostToDevice, L->stream));
   // colour field: the wetting colour everywhere; fluid voxels are rewritten
   // by every step before they are read
@@ -463,7 +714,7 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   for (int b = 0; b < 2; b++) {
     if (int r = dalloc(L.get(), &L->d_pop[b], popb)) return r;
     PS_CUDA(cudaMemsetAsync(L->d_pop[b], 0, popb, L->stream));
-    if (precision >= 2) {
+    if (precision >= 1) {  // deviation storage: the reference densities
       if (int r = dalloc(L.get(), &L->d_rho[b], sizeof(float2) * pitch)) return r;
       PS_CUDA(cudaMemsetAsync(L->d_rho[b], 0, sizeof(float2) * pitch, L->stream));
     }
@@ -503,6 +754,7 @@ int ps_lbm_get_info(void* h, ps_lbm_info* o)
   o->tile_x = L->tx;
   o->tile_y = L->ty;
   o->occupancy = L->zchunk;
+  o->schedule = L->fused_planes > 0 ? L->fused_planes + 256 * L->fused_ahead : 0;
   o->device_bytes = L->dev_bytes;
   return PS_OK;
 }
@@ -619,7 +871,7 @@ int ps_lbm_get_state(void* h, double* fr, double* fb)
     PS_CUDA(cudaMemcpyAsync(fb, L->d_fb, b, cudaMemcpyDeviceToHost, L->stream));
   }
   PS_CUDA(cudaStreamSynchronize(L->stream));
-  return PS_OK;
+  return check_fused(L);
 }
 
 int ps_lbm_init_random(void* h, double sat)
@@ -664,6 +916,7 @@ int ps_lbm_observables(void* h, ps_lbm_obs* out)
   double s[kObsN];
   PS_CUDA(cudaMemcpyAsync(s, L->d_obs, sizeof s, cudaMemcpyDeviceToHost, L->stream));
   PS_CUDA(cudaStreamSynchronize(L->stream));
+  if (int r = check_fused(L)) return r;
   memset(out, 0, sizeof *out);
   const LbmConst<double>& K = L->Kd;
   out->tmr = s[0];
@@ -718,12 +971,180 @@ int ps_lbm_fields(void* h, double* rr, double* rb, double* cf)
   return PS_OK;
 }
 
+int ps_lbm_wall_load(void* h, double rsi, double* afdat)
+{
+  if (!h || !afdat) return fail(PS_ERR_ARG, "ps_lbm_wall_load: null argument");
+  Lattice* L = as_lattice(h);
+  if (int r = wall_load_box(L, rsi)) return r;
+  std::vector<double> box((size_t)3 * L->nvox);
+  PS_CUDA(cudaMemcpyAsync(box.data(), L->d_wall, sizeof(double) * box.size(), cudaMemcpyDeviceToHost, L->stream));
+  PS_CUDA(cudaStreamSynchronize(L->stream));
+  long long ns = 0;
+  const std::vector<int32_t> num = lsm_node_numbers(L, &ns);
+  for (long long v = 0; v < L->nvox; v++)
+    if (num[v] > 0)
+      for (int c = 0; c < 3; c++) afdat[3 * (long long)(num[v] - 1) + c] = box[(size_t)c * L->nvox + v];
+  return PS_OK;
+}
+
+int ps_batch_create(void* const* lattices, int32_t n, void** handle)
+{
+  if (!lattices || !handle) return fail(PS_ERR_ARG, "ps_batch_create: null argument");
+  *handle = nullptr;
+  if (n < 1 || n > kBatchMaxVolumes) return fail(PS_ERR_ARG, "ps_batch_create: %d lattices (1..%d)", n, kBatchMaxVolumes);
+  std::unique_ptr<Batch, void (*)(Batch*)> B(new Batch, free_batch);
+  for (int v = 0; v < n; v++) {
+    if (!lattices[v]) return fail(PS_ERR_ARG, "ps_batch_create: lattice %d is null", v);
+    Lattice* L = as_lattice(lattices[v]);
+    if (v > 0) {
+      const Lattice* L0 = B->L[0];
+      const bool same = L->prec == L0->prec && (L->prec == 0 ? memcmp(&L->Kd, &L0->Kd, sizeof L->Kd) == 0
+                                                             : memcmp(&L->Kf, &L0->Kf, sizeof L->Kf) == 0);
+      if (!same) return fail(PS_ERR_ARG, "ps_batch_create: lattice %d differs in precision or parameters from lattice 0", v);
+      for (int u = 0; u < v; u++)
+        if (B->L[u] == L) return fail(PS_ERR_ARG, "ps_batch_create: lattice %d appears twice", v);
+    }
+    if (L->nl >= (1LL << 31)) return fail(PS_ERR_ARG, "ps_batch_create: lattice %d too large", v);
+    B->L.push_back(L);
+    B->nodes += L->nl;
+  }
+  B->prec = B->L[0]->prec;
+  B->tx = B->L[0]->tx;
+  B->ty = B->L[0]->ty;
+  B->occ = B->L[0]->zchunk;
+  PS_CUDA(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  *handle = B.release();
+  return PS_OK;
+}
+
+int ps_batch_destroy(void* h)
+{
+  free_batch(static_cast<Batch*>(h));
+  return PS_OK;
+}
+
+int ps_batch_step(void* h, int32_t nsteps)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_batch_step: null handle");
+  if (nsteps < 0) return fail(PS_ERR_ARG, "ps_batch_step: nsteps < 0");
+  Batch* B = static_cast<Batch*>(h);
+  for (size_t v = 0; v < B->L.size(); v++) {
+    if (!B->L[v]->have_state) return fail(PS_ERR_STATE, "ps_batch_step: lattice %d has no state", (int)v);
+    PS_CUDA(cudaStreamSynchronize(B->L[v]->stream));
+  }
+  if (int r = batch_steps(B, nsteps)) return r;
+  PS_CUDA(cudaStreamSynchronize(B->stream));
+  return PS_OK;
+}
+
+int ps_batch_set_tile(void* h, int32_t tx, int32_t ty, int32_t occ)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_batch_set_tile: null handle");
+  Batch* B = static_cast<Batch*>(h);
+  if (!lbm_step_smem(B->prec, tx, ty, occ)) return fail(PS_ERR_ARG, "ps_batch_set_tile: (%d, %d, %d) is not a compiled configuration", tx, ty, occ);
+  B->tx = tx;
+  B->ty = ty;
+  B->occ = occ;
+  return PS_OK;
+}
+
+int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, int32_t* occ_out)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_batch_autotune: null handle");
+  Batch* B = static_cast<Batch*>(h);
+  if (steps < 1) steps = 4;
+  const size_t nv = B->L.size();
+  for (size_t v = 0; v < nv; v++) {
+    if (!B->L[v]->have_state) return fail(PS_ERR_STATE, "ps_batch_autotune: lattice %d has no state", (int)v);
+    PS_CUDA(cudaStreamSynchronize(B->L[v]->stream));
+  }
+  // save every lattice's current buffer (populations and reference densities)
+  std::vector<void*> sp(nv, nullptr);
+  std::vector<float2*> sr(nv, nullptr);
+  std::vector<int> cur(nv);
+  auto popb = [&](const Lattice* L) { return 2 * L->elem() * 19 * (size_t)std::max(64LL, L->pitch); };
+  auto rhob = [&](const Lattice* L) { return sizeof(float2) * (size_t)std::max(64LL, L->pitch); };
+  int rc = PS_OK;
+  for (size_t v = 0; v < nv && rc == PS_OK; v++) {
+    Lattice* L = B->L[v];
+    cur[v] = L->cur;
+    cudaError_t e = cudaMalloc(&sp[v], popb(L));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sp[v], L->d_pop[L->cur], popb(L), cudaMemcpyDeviceToDevice, B->stream);
+    if (e == cudaSuccess && L->prec >= 1) e = cudaMalloc((void**)&sr[v], rhob(L));
+    if (e == cudaSuccess && L->prec >= 1)
+      e = cudaMemcpyAsync(sr[v], L->d_rho[L->cur], rhob(L), cudaMemcpyDeviceToDevice, B->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "ps_batch_autotune: saving the states");
+  }
+  struct Cfg {
+    int tx, ty, occ;
+  };
+  const std::vector<Cfg> cand = {{128, 256, 0}, {256, 256, 0}, {128, 128, 0}, {256, 512, 0},
+                                 {128, 256, 6}, {128, 256, 8}, {256, 256, 3}};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  Cfg bc{B->tx, B->ty, B->occ};
+  for (const Cfg& c : cand) {
+    if (rc != PS_OK) break;
+    B->tx = c.tx;
+    B->ty = c.ty;
+    B->occ = c.occ;
+    rc = batch_steps(B, 2);  // warm-up
+    if (rc) break;
+    cudaEventRecord(e0, B->stream);
+    rc = batch_steps(B, steps);
+    cudaEventRecord(e1, B->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rc == PS_OK && ms < best) {
+      best = ms;
+      bc = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (size_t v = 0; v < nv; v++) {  // restore
+    Lattice* L = B->L[v];
+    L->cur = cur[v];
+    if (sp[v]) cudaMemcpyAsync(L->d_pop[L->cur], sp[v], popb(L), cudaMemcpyDeviceToDevice, B->stream);
+    if (sr[v]) cudaMemcpyAsync(L->d_rho[L->cur], sr[v], rhob(L), cudaMemcpyDeviceToDevice, B->stream);
+  }
+  cudaStreamSynchronize(B->stream);
+  for (size_t v = 0; v < nv; v++) {
+    cudaFree(sp[v]);
+    cudaFree(sr[v]);
+  }
+  B->tx = bc.tx;
+  B->ty = bc.ty;
+  B->occ = bc.occ;
+  if (tx_out) *tx_out = bc.tx;
+  if (ty_out) *ty_out = bc.ty;
+  if (occ_out) *occ_out = bc.occ;
+  return rc;
+}
+
+void* ps_batch_stream(void* h) { return h ? (void*)static_cast<Batch*>(h)->stream : nullptr; }
+
 void* ps_lbm_stream(void* h) { return h ? (void*)as_lattice(h)->stream : nullptr; }
 
 int ps_lbm_sync(void* h)
 {
   if (!h) return fail(PS_ERR_ARG, "ps_lbm_sync: null handle");
   PS_CUDA(cudaStreamSynchronize(as_lattice(h)->stream));
+  return check_fused(as_lattice(h));
+}
+
+int ps_lbm_set_fused(void* h, int32_t planes, int32_t ahead)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_fused: null handle");
+  Lattice* L = as_lattice(h);
+  if (planes < 0 || ahead < 1 || ahead > 64) return fail(PS_ERR_ARG, "ps_lbm_set_fused: need planes >= 0 and 1 <= ahead <= 64");
+  if (planes > 0 && !fused_config(L->tx, L->zchunk))
+    return fail(PS_ERR_ARG, "ps_lbm_set_fused: the step configuration (%d, %d, %d) has no fused form", L->tx, L->ty, L->zchunk);
+  L->fused_planes = planes;
+  L->fused_ahead = ahead;
   return PS_OK;
 }
 
@@ -733,6 +1154,8 @@ int ps_lbm_set_tile(void* h, int32_t tx, int32_t ty, int32_t zchunk)
   Lattice* L = as_lattice(h);
   if (lbm_step_smem(L->prec, tx, ty, zchunk) == 0)
     return fail(PS_ERR_ARG, "ps_lbm_set_tile: (%d, %d, %d) is not a compiled step configuration", tx, ty, zchunk);
+  if (L->fused_planes > 0 && !fused_config(tx, zchunk))
+    return fail(PS_ERR_ARG, "ps_lbm_set_tile: (%d, %d, %d) has no fused form (ps_lbm_set_fused(h, 0, 1) first)", tx, ty, zchunk);
   L->tx = tx;
   L->ty = ty;
   L->zchunk = zchunk;
@@ -745,48 +1168,53 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   Lattice* L = as_lattice(h);
   if (!L->have_state) return fail(PS_ERR_STATE, "ps_lbm_autotune: no state set");
   if (steps < 1) steps = 4;
-  // candidates: every compiled tile x a few z-chunk lengths; the state is
-  // advanced an even number of steps per candidate and then restored by
-  // re-running from a saved copy of the current buffer
+  // candidates: the compiled (collide CTA, density CTA, occupancy)
+  // configurations; the state is restored afterwards from a saved copy of
+  // the current buffer
   const size_t popb = 2 * L->elem() * 19 * (size_t)std::max(64LL, L->pitch);
   const size_t rhob = sizeof(float2) * (size_t)std::max(64LL, L->pitch);
   void* save = nullptr;
   float2* saver = nullptr;
   PS_CUDA(cudaMalloc(&save, popb));
   PS_CUDA(cudaMemcpyAsync(save, L->d_pop[L->cur], popb, cudaMemcpyDeviceToDevice, L->stream));
-  if (L->prec >= 2) {
+  if (L->prec >= 1) {
     PS_CUDA(cudaMalloc((void**)&saver, rhob));
     PS_CUDA(cudaMemcpyAsync(saver, L->d_rho[L->cur], rhob, cudaMemcpyDeviceToDevice, L->stream));
   }
   struct Cfg {
-    int tx, ty, zc;
+    int tx, ty, zc, planes, ahead;
   };
-  const std::vector<Cfg> cand = {{128, 256, 0}, {256, 256, 0}, {128, 128, 0}, {256, 512, 0},
-                                 {128, 256, 6}, {128, 256, 8}, {256, 256, 3}};
+  // two-pass configurations, then fused ones (slab planes, look-ahead)
+  const std::vector<Cfg> cand = {{128, 256, 0, 0, 1}, {256, 256, 0, 0, 1}, {128, 128, 0, 0, 1}, {256, 512, 0, 0, 1},
+                                 {128, 256, 6, 0, 1}, {128, 256, 8, 0, 1}, {256, 256, 3, 0, 1}, {128, 256, 0, 2, 1},
+                                 {128, 256, 0, 4, 1}, {128, 256, 0, 8, 1}, {128, 256, 0, 4, 2}, {256, 256, 0, 4, 1},
+                                 {128, 256, 6, 4, 1}, {128, 256, 8, 4, 1}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int btx = L->tx, bty = L->ty, bzc = L->zchunk;
+  Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead};
   const int saved_cur = L->cur;
   int rc = PS_OK;
   for (const Cfg& c : cand) {
     L->tx = c.tx;
     L->ty = c.ty;
     L->zchunk = c.zc;
+    L->fused_planes = c.planes;
+    L->fused_ahead = c.ahead;
     rc = launch_steps(L, 2);  // warm-up
     if (rc) break;
     cudaEventRecord(e0, L->stream);
     rc = launch_steps(L, steps);
     cudaEventRecord(e1, L->stream);
     cudaEventSynchronize(e1);
+    if (rc == PS_OK) rc = check_fused(L);
+    if (rc) break;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    if (rc == PS_OK && ms < best) {
+    if (ms < best) {
       best = ms;
-      btx = c.tx;
-      bty = c.ty;
-      bzc = c.zc;
+      bc = c;
     }
   }
   cudaEventDestroy(e0);
@@ -798,12 +1226,14 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   cudaStreamSynchronize(L->stream);
   cudaFree(save);
   cudaFree(saver);
-  L->tx = btx;
-  L->ty = bty;
-  L->zchunk = bzc;
-  if (tx_out) *tx_out = btx;
-  if (ty_out) *ty_out = bty;
-  if (zc_out) *zc_out = bzc;
+  L->tx = bc.tx;
+  L->ty = bc.ty;
+  L->zchunk = bc.zc;
+  L->fused_planes = bc.planes;
+  L->fused_ahead = bc.ahead;
+  if (tx_out) *tx_out = bc.tx;
+  if (ty_out) *ty_out = bc.ty;
+  if (zc_out) *zc_out = bc.zc;
   return rc;
 }
 

@@ -115,11 +115,11 @@ struct Store<0> {  // FP64
   static constexpr bool kDev = false;
 };
 template <>
-struct Store<1> {  // FP32
+struct Store<1> {  // FP32 deviation
   using T = float;
   using T2 = float2;
   using R = float;
-  static constexpr bool kDev = false;
+  static constexpr bool kDev = true;
 };
 template <>
 struct Store<2> {  // FP16 deviation
@@ -146,10 +146,13 @@ struct DevScale<__half> {
   static constexpr float up = 1024.0f, down = 1.0f / 1024.0f;
 };
 
+__device__ __forceinline__ float2 to_f2(float2 h) { return h; }
 __device__ __forceinline__ float2 to_f2(__half2 h) { return __half22float2(h); }
 __device__ __forceinline__ float2 to_f2(__nv_bfloat162 h) { return __bfloat1622float2(h); }
 template <typename T2>
 __device__ __forceinline__ T2 from_f2(float a, float b);
+template <>
+__device__ __forceinline__ float2 from_f2<float2>(float a, float b) { return make_float2(a, b); }
 template <>
 __device__ __forceinline__ __half2 from_f2<__half2>(float a, float b) { return __floats2half2_rn(a, b); }
 template <>
@@ -179,6 +182,17 @@ struct Pop {
       vr = v.x;
       vb = v.y;
     }
+  }
+  // the stored (red, blue) deviations of slot (d, i) (deviation storage)
+  __device__ __forceinline__ static void load_dev(const BufDev& b, int d, int i, long long pitch, R& gr, R& gb)
+  {
+    const float2 v = to_f2(*(static_cast<const T2*>(b.pop) + (long long)d * pitch + i));
+    gr = v.x * DevScale<T>::down;
+    gb = v.y * DevScale<T>::down;
+  }
+  __device__ __forceinline__ static void put_dev(const BufDev& b, int d, int i, long long pitch, R gr, R gb)
+  {
+    *(static_cast<T2*>(b.pop) + (long long)d * pitch + i) = from_f2<T2>(gr * DevScale<T>::up, gb * DevScale<T>::up);
   }
   // writes the (red, blue) pair (vr, vb) into slot (d, i) whose node has
   // deviation references rho
@@ -293,22 +307,60 @@ __device__ __forceinline__ void read_node(const LbmConst<typename Store<PREC>::R
 // Writes the 19 post-collision (red, blue) populations of node i to their
 // receivers (push streaming with half-way bounce-back).  s[] are the pull
 // sources of node i (pull_sources): the receiver of an outgoing population
-// e is the source of the incoming direction opp(e).
-template <int PREC>
+// e is the source of the incoming direction opp(e).  kCoh: the receivers'
+// reference densities were written by other CTAs of the same launch, so
+// they are read through L2 only (no non-coherent or L1 path).
+template <typename T>
+__device__ __forceinline__ T ld_step(const T* p, bool coherent)
+{
+  return coherent ? __ldcg(p) : __ldg(p);
+}
+
+template <int PREC, bool kCoh = false>
 __device__ __forceinline__ void push_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
                                           const BufDev& dst, int i, uint32_t m, const int* s,
                                           const typename Store<PREC>::R* outr, const typename Store<PREC>::R* outb)
 {
   constexpr bool kDev = Store<PREC>::kDev;
   const float2 zero = make_float2(0.f, 0.f);
-  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], kDev ? __ldg(dst.rho + i) : zero);
+  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], kDev ? ld_step(dst.rho + i, kCoh) : zero);
 #pragma unroll
   for (int e = 1; e < 19; e++) {
     const int oe = opp(e);
     const bool stream = m & (1u << (oe - 1));
     const int node = stream ? s[oe] : i;
     const int slot = stream ? e : oe;
-    Pop<PREC>::put(K, dst, slot, node, G.pitch, outr[e], outb[e], kDev ? __ldg(dst.rho + node) : zero);
+    Pop<PREC>::put(K, dst, slot, node, G.pitch, outr[e], outb[e], kDev ? ld_step(dst.rho + node, kCoh) : zero);
+  }
+}
+
+// deviation storage: node i's stored deviations and their references
+template <int PREC>
+__device__ __forceinline__ float2 read_node_dev(const GeomDev& G, const BufDev& src, int i, float* gr, float* gb)
+{
+#pragma unroll
+  for (int d = 0; d < 19; d++) Pop<PREC>::load_dev(src, d, i, G.pitch, gr[d], gb[d]);
+  return __ldg(src.rho + i);
+}
+
+// deviation storage: pushes out_c[d] = t^c_d S_c + Z_c[d] (node_update_dev)
+// to the receivers, each as t^c_d (S_c - rho'_c) + Z_c[d] against the
+// receiver's current densities rho' (rn for node i itself)
+template <int PREC, bool kCoh = false>
+__device__ __forceinline__ void push_node_dev(const LbmConst<float>& K, const GeomDev& G, const BufDev& dst, int i,
+                                              uint32_t m, const int* s, float Sr, float Sb, const float* Zr,
+                                              const float* Zb, float2 rn)
+{
+  Pop<PREC>::put_dev(dst, 0, i, G.pitch, K.t[0][0] * (Sr - rn.x) + Zr[0], K.t[1][0] * (Sb - rn.y) + Zb[0]);
+#pragma unroll
+  for (int e = 1; e < 19; e++) {
+    const int oe = opp(e);
+    const bool stream = m & (1u << (oe - 1));
+    const int node = stream ? s[oe] : i;
+    const int slot = stream ? e : oe;
+    const float2 rho = stream ? ld_step(dst.rho + node, kCoh) : rn;
+    const int w = wcls(e);
+    Pop<PREC>::put_dev(dst, slot, node, G.pitch, K.t[0][w] * (Sr - rho.x) + Zr[e], K.t[1][w] * (Sb - rho.y) + Zb[e]);
   }
 }
 
@@ -361,27 +413,91 @@ __device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int nz)
 }
 
 // ---- step kernels ---------------------------------------------------------
-// colour (and 16-bit reference densities) of the current step
+// per-node bodies, shared by the single-lattice and the batched kernels
+
+// colour (and, for deviation storage, the current densities that the
+// collide step encodes against) of fluid node i for this step
+template <int PREC>
+__device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, const BufDev& dst, typename Store<PREC>::R* cc, int i)
+{
+  using R = typename Store<PREC>::R;
+  R rr, rb;
+  if constexpr (Store<PREC>::kDev) {
+    float gr[19], gb[19];
+    const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
+    R sr = gr[0], sb = gb[0];
+#pragma unroll
+    for (int d = 1; d < 19; d++) {
+      sr = sr + gr[d];
+      sb = sb + gb[d];
+    }
+    rr = ro.x + sr;
+    rb = ro.y + sb;
+    dst.rho[i] = make_float2(rr, rb);
+  } else {
+    R f[38];
+    read_node<PREC>(K, G, src, i, f);
+    densities(f, rr, rb);
+  }
+  int x, y, z;
+  unpack(__ldg(G.coord + i), x, y, z);
+  cc[x + G.nx * (y + G.ny * z)] = stencil_colour(rr, rb, K.wet);
+}
+
+// collision, CSF force, recolouring of fluid node i; pushes the
+// post-collision populations to their receivers.  kCoh: the colour field
+// and reference densities of this step come from other CTAs of the same
+// launch (the fused schedule) and are read through L2 only.
+template <int PREC, bool kCoh = false>
+__device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, const BufDev& dst,
+                                          const typename Store<PREC>::R* __restrict__ cc, int i)
+{
+  using R = typename Store<PREC>::R;
+  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+  int x, y, z;
+  unpack(c, x, y, z);
+  const int nxy = G.nx * G.ny;
+  const int v = x + G.nx * y + nxy * z;
+  const NbOff o = nb_offsets(m, G.nx, nxy, G.nz);
+  auto col = [&](int a, int b, int e) -> R {
+    const R* p = cc + (v + o.x[a] + o.y[b] + o.z[e]);
+    if constexpr (kCoh)
+      return __ldcg(p);
+    else
+      return *p;
+  };
+  if constexpr (Store<PREC>::kDev) {
+    float gr[19], gb[19], Zr[19], Zb[19], Sr, Sb;
+    const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
+    const float2 rn = ld_step(dst.rho + i, kCoh);  // this step's densities (density pass)
+    node_update_dev(K, gr, gb, ro.x, ro.y, rn.x, rn.y, col, Sr, Sb, Zr, Zb);
+    int s[19];
+    pull_sources(G, i, c, m, s);
+    push_node_dev<PREC, kCoh>(K, G, dst, i, m, s, Sr, Sb, Zr, Zb, rn);
+  } else {
+    R f[38];
+    read_node<PREC>(K, G, src, i, f);
+    R rr, rb;
+    densities(f, rr, rb);
+    R outr[19], outb[19];
+    node_update(K, f, f + 19, rr, rb, col, outr, outb);
+    int s[19];
+    pull_sources(G, i, c, m, s);
+    push_node<PREC, kCoh>(K, G, dst, i, m, s, outr, outb);
+  }
+}
+
 template <int PREC, int BLK>
 __global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                   const __grid_constant__ GeomDev G, const BufDev src,
                                                   const BufDev dst, typename Store<PREC>::R* __restrict__ cc)
 {
-  using R = typename Store<PREC>::R;
   const int i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= G.nl) return;
-  R f[38];
-  read_node<PREC>(K, G, src, i, f);
-  R rr, rb;
-  densities(f, rr, rb);
-  int x, y, z;
-  unpack(__ldg(G.coord + i), x, y, z);
-  cc[x + G.nx * (y + G.ny * z)] = stencil_colour(rr, rb, K.wet);
-  if constexpr (Store<PREC>::kDev) dst.rho[i] = make_float2(rr, rb);
+  if (i < G.nl) dens_node<PREC>(K, G, src, dst, cc, i);
 }
 
-// collision, CSF force, recolouring; pushes the post-collision populations
-// to their receivers
 // MINB > 0 asks the register allocator for MINB resident CTAs per SM;
 // 0 keeps 640 resident threads per SM (the allocator's unconstrained
 // choice for this kernel uses too many registers for that)
@@ -390,25 +506,124 @@ __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK) k_lbm_coll(c
                                                   const __grid_constant__ GeomDev G, const BufDev src,
                                                   const BufDev dst, const typename Store<PREC>::R* __restrict__ cc)
 {
-  using R = typename Store<PREC>::R;
   const int i = blockIdx.x * BLK + threadIdx.x;
-  if (i >= G.nl) return;
-  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
-  R f[38];
-  read_node<PREC>(K, G, src, i, f);
-  R rr, rb;
-  densities(f, rr, rb);
-  int x, y, z;
-  unpack(c, x, y, z);
-  const int nxy = G.nx * G.ny;
-  const int v = x + G.nx * y + nxy * z;
-  const NbOff o = nb_offsets(m, G.nx, nxy, G.nz);
-  auto col = [&](int a, int b, int e) -> R { return cc[v + o.x[a] + o.y[b] + o.z[e]]; };
-  R outr[19], outb[19];
-  node_update(K, f, f + 19, rr, rb, col, outr, outb);
-  int s[19];
-  pull_sources(G, i, c, m, s);
-  push_node<PREC>(K, G, dst, i, m, s, outr, outb);
+  if (i < G.nl) coll_node<PREC>(K, G, src, dst, cc, i);
+}
+
+// ---- batched step kernels: many lattices (subvolumes) per launch ----------
+// Every lattice of a batch shares the constants K; its geometry, buffers
+// and colour field come from the descriptor table passed by value (kernel
+// parameter space, read through the constant cache with a CTA-uniform
+// index).  The work is a list of tiles (lattice, first node) of BLK nodes;
+// a persistent grid (resident CTAs x SMs) strides over it.
+constexpr int kBatchMaxVolumes = 64;
+struct VolDesc {
+  GeomDev G;
+  BufDev src, dst;
+  void* cc;
+};
+struct VolTable {
+  VolDesc v[kBatchMaxVolumes];
+};
+
+template <int PREC, int BLK>
+__global__ void __launch_bounds__(BLK) k_lbm_dens_batch(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+                                                        const __grid_constant__ VolTable T,
+                                                        const int2* __restrict__ tiles, int ntiles)
+{
+  using R = typename Store<PREC>::R;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int2 tl = __ldg(tiles + t);
+    const VolDesc& D = T.v[tl.x];
+    const int i = tl.y + threadIdx.x;
+    if (i < D.G.nl) dens_node<PREC>(K, D.G, D.src, D.dst, static_cast<R*>(D.cc), i);
+  }
+}
+
+template <int PREC, int BLK, int MINB>
+__global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
+    k_lbm_coll_batch(const __grid_constant__ LbmConst<typename Store<PREC>::R> K, const __grid_constant__ VolTable T,
+                     const int2* __restrict__ tiles, int ntiles)
+{
+  using R = typename Store<PREC>::R;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int2 tl = __ldg(tiles + t);
+    const VolDesc& D = T.v[tl.x];
+    const int i = tl.y + threadIdx.x;
+    if (i < D.G.nl) coll_node<PREC>(K, D.G, D.src, D.dst, static_cast<const R*>(D.cc), i);
+  }
+}
+
+// ---- fused step: density and collide tiles in one persistent launch -----
+// The fluid nodes are cut into z-slabs; a work list holds the density tiles
+// of every slab and the collide tiles of every slab, ordered so that the
+// collide tiles of slab k follow the density tiles of slabs k-1, k, k+1
+// (periodic).  CTAs take items in list order from a ticket counter; a
+// density tile publishes its completion on its slab's counter, and a
+// collide tile first waits (bounded) for the three counters it needs.  A
+// CTA only waits for items handed out before its own, to CTAs already
+// running, so the waits end.  The collide tiles re-read populations that
+// the density tiles of the same slab read shortly before (L2 hits), and
+// memory-bound density work overlaps compute-bound collide work.
+struct FusedArgs {
+  const int4* items;     // x = kind (0 density, 1 collide) | slab << 1, y = first node, z = end node
+  int nitems;
+  int nslab;
+  const int* ntd;        // density tiles per slab
+  unsigned int* ctr;     // [0] ticket, [1 + s] completed density tiles of slab s (zeroed before the launch)
+  int* err;              // set to 1 when a wait gave up
+};
+constexpr unsigned kFusedSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
+{
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <int PREC, int BLK, int MINB>
+__global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
+    k_lbm_fused(const __grid_constant__ LbmConst<typename Store<PREC>::R> K, const __grid_constant__ GeomDev G,
+                const BufDev src, const BufDev dst, typename Store<PREC>::R* __restrict__ cc, const FusedArgs F)
+{
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(F.ctr, 1u);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= F.nitems) break;
+    const int4 w = __ldg(F.items + it);
+    const int slab = w.x >> 1;
+    const int i = w.y + threadIdx.x;
+    if ((w.x & 1) == 0) {
+      if (i < w.z) dens_node<PREC>(K, G, src, dst, cc, i);
+      __threadfence();  // this tile's colours and densities before its completion count
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(F.ctr + 1 + slab, 1u);
+    } else {
+      if (threadIdx.x == 0) {
+        bool ok = true;
+        for (int d = -1; d <= 1 && ok; d++) {
+          const int sl = (slab + d + F.nslab) % F.nslab;
+          const unsigned target = (unsigned)__ldg(F.ntd + sl);
+          unsigned n = 0;
+          while (ld_acquire_u32(F.ctr + 1 + sl) < target) {
+            if (++n > kFusedSpinLimit) {
+              atomicExch(F.err, 1);
+              ok = false;
+              break;
+            }
+            __nanosleep(64);
+          }
+        }
+        __threadfence();
+      }
+      __syncthreads();
+      if (i < w.z) coll_node<PREC, true>(K, G, src, dst, cc, i);
+    }
+  }
 }
 
 // ---- colour/density field (observables, fields) ---------------------------
@@ -444,13 +659,23 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
   using R = typename Store<PREC>::R;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
-  R f[38];
-  read_node<PREC>(K, G, src, i, f);
   const long long r = G.ref[i];
+  if constexpr (Store<PREC>::kDev) {  // decode t_d rho + g in FP64
+    float gr[19], gb[19];
+    const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
 #pragma unroll
-  for (int d = 0; d < 19; d++) {
-    fr[19 * r + d] = (double)f[d];
-    fb[19 * r + d] = (double)f[19 + d];
+    for (int d = 0; d < 19; d++) {
+      fr[19 * r + d] = (double)K.t[0][wcls(d)] * (double)ro.x + (double)gr[d];
+      fb[19 * r + d] = (double)K.t[1][wcls(d)] * (double)ro.y + (double)gb[d];
+    }
+  } else {
+    R f[38];
+    read_node<PREC>(K, G, src, i, f);
+#pragma unroll
+    for (int d = 0; d < 19; d++) {
+      fr[19 * r + d] = (double)f[d];
+      fb[19 * r + d] = (double)f[19 + d];
+    }
   }
 }
 
@@ -466,17 +691,22 @@ __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
   const long long me = G.ref[i];
-  float2 rho = make_float2(0.f, 0.f);
   if constexpr (S::kDev) {
+    // the node's own densities are the reference; deviations formed in FP64
     double sr = fr[19 * me], sb = fb[19 * me];
     for (int d = 1; d < 19; d++) {
       sr += fr[19 * me + d];
       sb += fb[19 * me + d];
     }
-    rho = make_float2((float)sr, (float)sb);
+    const float2 rho = make_float2((float)sr, (float)sb);
     dst.rho[i] = rho;
+    for (int d = 0; d < 19; d++)
+      Pop<PREC>::put_dev(dst, d, i, G.pitch, (R)(fr[19 * me + d] - (double)K.t[0][wcls(d)] * (double)rho.x),
+                         (R)(fb[19 * me + d] - (double)K.t[1][wcls(d)] * (double)rho.y));
+  } else {
+    for (int d = 0; d < 19; d++)
+      Pop<PREC>::put(K, dst, d, i, G.pitch, (R)fr[19 * me + d], (R)fb[19 * me + d], make_float2(0.f, 0.f));
   }
-  for (int d = 0; d < 19; d++) Pop<PREC>::put(K, dst, d, i, G.pitch, (R)fr[19 * me + d], (R)fb[19 * me + d], rho);
 }
 
 // ---- check_state reductions -------------------------------------------------
@@ -584,6 +814,100 @@ __global__ void __launch_bounds__(256) k_lbm_obs(const __grid_constant__ LbmCons
 }
 
 // fixed-order sum of the per-block partials (deterministic)
+// index of the moving direction with velocity (cx, cy, cz)
+__device__ __forceinline__ int dir_of(int cx, int cy, int cz)
+{
+  int r = 0;
+#pragma unroll
+  for (int d = 1; d < 19; d++)
+    if (cvx(d) == cx && cvy(d) == cy && cvz(d) == cz) r = d;
+  return r;
+}
+
+// Wall load of the fluid on the LSM corner nodes (S1:3849-3882).  Every wall
+// link of a fluid node n -- outgoing direction e into the wall, so that the
+// incoming link d = opp(e) is closed and slot (d, n) holds the bounced
+// post-collision population e -- carries
+//   floc = -2 ((f_r + f_b)(e) - ppp fq(d)) c_d rsdti2,
+// split equally over the 2 LSM nodes at the ends of the wall edge (diagonal
+// e, the reference's ipb2 entries) or the 4 at the corners of the wall face
+// (axis e, ipb4).  Corner node v = (X, Y, Z) is the low corner of voxel v.
+// Each corner gathers its contributions from the (at most 8) fluid voxels
+// that share it, in the reference's accumulation order: all ipb2 entries,
+// then all ipb4 entries, each by reference fluid index and then direction,
+// so the FP64 sums are those of the reference.  out: [3][nvox].
+template <int PREC>
+__global__ void __launch_bounds__(128) k_lbm_wall_load(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+                                                       const __grid_constant__ GeomDev G, const BufDev src,
+                                                       double fq1, double fq2, double ppp, double rsdti2,
+                                                       double* __restrict__ out)
+{
+  using R = typename Store<PREC>::R;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= G.nvox) return;
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const int X = (int)(v % nx), Y = (int)((v / nx) % ny), Z = (int)(v / ((long long)nx * ny));
+  int idx[8], rf[8], eo[8], n = 0;
+#pragma unroll
+  for (int e = 0; e < 8; e++) {  // voxel v - e has this corner at its offset e
+    const int vx = (e & 1) ? (X == 0 ? nx - 1 : X - 1) : X;
+    const int vy = (e & 2) ? (Y == 0 ? ny - 1 : Y - 1) : Y;
+    const int vz = (e & 4) ? (Z == 0 ? nz - 1 : Z - 1) : Z;
+    const RowRank r = row_rank(G, vy + ny * vz, vx);
+    if (r.fx) {
+      idx[n] = r.base + r.rank;
+      rf[n] = __ldg(G.ref + idx[n]);
+      eo[n] = e;
+      n++;
+    }
+  }
+  for (int a = 1; a < n; a++)  // by reference fluid index
+    for (int b = a; b > 0 && rf[b - 1] > rf[b]; b--) {
+      int t = rf[b]; rf[b] = rf[b - 1]; rf[b - 1] = t;
+      t = idx[b]; idx[b] = idx[b - 1]; idx[b - 1] = t;
+      t = eo[b]; eo[b] = eo[b - 1]; eo[b - 1] = t;
+    }
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int pass = 0; pass < 2; pass++) {  // 0: edges (ipb2), 1: faces (ipb4)
+    const double w = pass == 0 ? 0.5 : 0.25, fq = pass == 0 ? fq2 : fq1;
+    for (int k = 0; k < n; k++) {
+      const int i = idx[k];
+      const uint32_t m = __ldg(G.mask + i);
+      // the corner lies on the voxel's high (+1) or low (-1) side per axis
+      const int sx = (eo[k] & 1) ? 1 : -1, sy = (eo[k] & 2) ? 1 : -1, sz = (eo[k] & 4) ? 1 : -1;
+      int ds[3];
+      if (pass == 0) {
+        ds[0] = dir_of(sx, sy, 0);
+        ds[1] = dir_of(sx, 0, sz);
+        ds[2] = dir_of(0, sy, sz);
+      } else {
+        ds[0] = dir_of(sx, 0, 0);
+        ds[1] = dir_of(0, sy, 0);
+        ds[2] = dir_of(0, 0, sz);
+      }
+      for (int a = 1; a < 3; a++)
+        for (int b = a; b > 0 && ds[b - 1] > ds[b]; b--) {
+          const int t = ds[b]; ds[b] = ds[b - 1]; ds[b - 1] = t;
+        }
+      float2 rho = make_float2(0.f, 0.f);
+      if constexpr (Store<PREC>::kDev) rho = __ldg(src.rho + i);
+      for (int j = 0; j < 3; j++) {
+        const int d = opp(ds[j]);  // incoming link of the bounced population
+        if (m & (1u << (d - 1))) continue;
+        R vr, vb;
+        Pop<PREC>::load(K, src, d, i, G.pitch, rho, vr, vb);
+        const double q = ((double)vr + (double)vb) - ppp * fq;
+        const double c[3] = {(double)cvx(d), (double)cvy(d), (double)cvz(d)};
+#pragma unroll
+        for (int t = 0; t < 3; t++) acc[t] = acc[t] + ((-2.0 * q) * c[t]) * rsdti2 * w;
+      }
+    }
+  }
+  out[v] = acc[0];
+  out[G.nvox + v] = acc[1];
+  out[2 * G.nvox + v] = acc[2];
+}
+
 static __global__ void k_obs_final(const double* partial, int nblocks, double* out)
 {
   const int i = threadIdx.x;

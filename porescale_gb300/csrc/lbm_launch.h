@@ -17,6 +17,18 @@ struct LbmLaunchArgs {
   cudaStream_t stream;
 };
 
+// one batched step over many lattices sharing the constants K: tiles_c /
+// tiles_d list (lattice, first node) per collide / density CTA
+struct BatchLaunchArgs {
+  const void* K;
+  const VolTable* T;
+  const int2* tiles_c;
+  int ntc;
+  const int2* tiles_d;
+  int ntd;
+  cudaStream_t stream;
+};
+
 // returns cudaErrorInvalidValue when (tx, ty, occ) is not a compiled
 // configuration (tx / ty threads per CTA of the collide / density kernel,
 // occ minimum resident collide CTAs per SM, 0 = compiler's choice)
@@ -32,11 +44,15 @@ size_t lbm_step_smem(int prec, int tx, int ty, int occ);
 // per-precision implementations
 #define PS_DECL_PREC(P)                                                                                     \
   cudaError_t lbm_step_launch_##P(int tx, int ty, int zchunk, const LbmLaunchArgs& a);                     \
+  cudaError_t lbm_fused_launch_##P(int tx, int occ, const LbmLaunchArgs& a, const FusedArgs& f);           \
+  cudaError_t lbm_batch_step_launch_##P(int tx, int ty, int occ, const BatchLaunchArgs& b);                \
   cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc); \
   cudaError_t lbm_get_state_launch_##P(const LbmLaunchArgs& a, double* fr, double* fb);                    \
   cudaError_t lbm_set_state_launch_##P(const LbmLaunchArgs& a, const double* fr, const double* fb);        \
   cudaError_t lbm_obs_launch_##P(const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks,   \
                                  double* out);                                                              \
+  cudaError_t lbm_wall_load_launch_##P(const LbmLaunchArgs& a, double fq1, double fq2, double ppp, double rsdti2, \
+                                      double* out);                                                         \
   size_t lbm_step_smem_##P(int tx, int ty, int occ);
 PS_DECL_PREC(0)
 PS_DECL_PREC(1)

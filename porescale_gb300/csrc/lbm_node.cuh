@@ -219,6 +219,63 @@ PS_HD void trt_collide(const LbmConst<R>& K, R t2, R t3, R* f, R* pcf, R r, cons
   f[0] = pcf[0];
 }
 
+// trt_collide on shifted populations g = f - T (T_d the storage reference
+// t^r_d rho^r_old + t^b_d rho^b_old of the node's populations).  dr1 / dr2
+// are t_w r - T_w for the axis / diagonal weight classes (each a small
+// difference computed from densities), dsum = sum_d g_d = sum_d (f_d - T_d);
+// r is the current density.  gs receives g* = f* - T.  Every intermediate
+// is a deviation (~1e-4 in bulk fluid), so FP32 rounding acts on the flow
+// itself, not on the O(t_d) rest populations it rides on.
+template <typename R>
+PS_HD void trt_collide_dev(const LbmConst<R>& K, R dr1, R dr2, R dsum, const R* g, R* gs, R r, const R* F, R wp,
+                           R wm)
+{
+  const R dt = K.dt, dti = K.dti, dt2 = K.dt2;
+  const R jx = (g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14]) * dti;
+  const R jy = (g[3] - g[4] + g[7] + g[8] - g[9] - g[10] + g[15] - g[16] + g[17] - g[18]) * dti;
+  const R jz = (g[5] - g[6] + g[11] + g[12] - g[13] - g[14] + g[15] + g[16] - g[17] - g[18]) * dti;
+  const R rinv = R(1) / r;
+  const R ux = (jx + F[0] * R(0.5) * dt) * rinv;
+  const R uy = (jy + F[1] * R(0.5) * dt) * rinv;
+  const R uz = (jz + F[2] * R(0.5) * dt) * rinv;
+  const R uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+  const R usq = (uxx + uyy + uzz) * R(0.5);
+  // shifted even equilibrium parts e_pair - T_pair
+  const R rq = r * R(0.25) * dt2, ro = r * R(0.125) * dt2;
+  const R e1 = dr1 - usq * K.c1d6 * dt2 * r;
+  const R e2 = dr2 - usq * K.c1d12 * dt2 * r;
+  const R ev[9] = {e1 + rq * uxx,
+                   e1 + rq * uyy,
+                   e1 + rq * uzz,
+                   e2 + ro * (ux + uy) * (ux + uy),
+                   e2 + ro * (ux - uy) * (ux - uy),
+                   e2 + ro * (ux + uz) * (ux + uz),
+                   e2 + ro * (ux - uz) * (ux - uz),
+                   e2 + ro * (uy + uz) * (uy + uz),
+                   e2 + ro * (uy - uz) * (uy - uz)};
+  // rest part: the complement, so that the collision conserves sum g exactly
+  // up to unbiased rounding
+  const R esum = ((ev[0] + ev[1]) + ev[2]) + (((ev[3] + ev[4]) + (ev[5] + ev[6])) + (ev[7] + ev[8]));
+  gs[0] = g[0] - wp * (g[0] - (dsum - R(2) * esum));
+  const R c6 = K.c1d6 * dt, c12 = K.c1d12 * dt;
+  const R w6 = K.c1d6 * dt2, w12 = K.c1d12 * dt2;
+  auto pair = [&](int a, int b, R even, R odd, R fa) {
+    const R la = g[a] - (even + odd), lb = g[b] - (even - odd);
+    const R p = (la + lb) * R(0.5), m = (la - lb) * R(0.5);
+    gs[a] = g[a] - wp * p - wm * m + fa;
+    gs[b] = g[b] - wp * p + wm * m - fa;
+  };
+  pair(1, 2, ev[0], jx * c6, w6 * F[0]);
+  pair(3, 4, ev[1], jy * c6, w6 * F[1]);
+  pair(5, 6, ev[2], jz * c6, w6 * F[2]);
+  pair(7, 10, ev[3], (jx + jy) * c12, w12 * (F[0] + F[1]));
+  pair(8, 9, ev[4], (jy - jx) * c12, w12 * (F[1] - F[0]));
+  pair(11, 14, ev[5], (jx + jz) * c12, w12 * (F[0] + F[2]));
+  pair(12, 13, ev[6], (jz - jx) * c12, w12 * (F[2] - F[0]));
+  pair(15, 18, ev[7], (jy + jz) * c12, w12 * (F[1] + F[2]));
+  pair(16, 17, ev[8], (jz - jy) * c12, w12 * (F[2] - F[1]));
+}
+
 // CSF surface tension from the colour neighbourhood.  cc(i,j,k), i,j,k in
 // {0,1,2} (offsets -1,0,+1 in x,y,z) returns the stencil colour: the node's
 // colour for fluid voxels, the wetting colour for the others.  The colour
@@ -232,21 +289,72 @@ PS_HD void csf_force(const LbmConst<R>& K, CC cc, R* n, R* Fs)
   // gradient components are differences of the two 2x2 faces normal to each
   // axis; every face sum is (edge + edge) with edges summed low index first.
   R g[8][3];
+  if constexpr (sizeof(R) == 8) {
 #pragma unroll
-  for (int s = 0; s < 8; s++) {
-    const int a = s & 1, b = (s >> 1) & 1, c = s >> 2;
-    // x: faces at x=a+1 and x=a, edges along y, summed over z
-    const R xh = (cc(a + 1, b, c) + cc(a + 1, b + 1, c)) + (cc(a + 1, b, c + 1) + cc(a + 1, b + 1, c + 1));
-    const R xl = (cc(a, b, c) + cc(a, b + 1, c)) + (cc(a, b, c + 1) + cc(a, b + 1, c + 1));
-    // y: faces at y=b+1 and y=b, edges along x, summed over z
-    const R yh = (cc(a, b + 1, c) + cc(a + 1, b + 1, c)) + (cc(a, b + 1, c + 1) + cc(a + 1, b + 1, c + 1));
-    const R yl = (cc(a, b, c) + cc(a + 1, b, c)) + (cc(a, b, c + 1) + cc(a + 1, b, c + 1));
-    // z: faces at z=c+1 and z=c, edges along x, summed over y
-    const R zh = (cc(a, b, c + 1) + cc(a + 1, b, c + 1)) + (cc(a, b + 1, c + 1) + cc(a + 1, b + 1, c + 1));
-    const R zl = (cc(a, b, c) + cc(a + 1, b, c)) + (cc(a, b + 1, c) + cc(a + 1, b + 1, c));
-    g[s][0] = xh - xl;
-    g[s][1] = yh - yl;
-    g[s][2] = zh - zl;
+    for (int s = 0; s < 8; s++) {
+      const int a = s & 1, b = (s >> 1) & 1, c = s >> 2;
+      // x: faces at x=a+1 and x=a, edges along y, summed over z
+      const R xh = (cc(a + 1, b, c) + cc(a + 1, b + 1, c)) + (cc(a + 1, b, c + 1) + cc(a + 1, b + 1, c + 1));
+      const R xl = (cc(a, b, c) + cc(a, b + 1, c)) + (cc(a, b, c + 1) + cc(a, b + 1, c + 1));
+      // y: faces at y=b+1 and y=b, edges along x, summed over z
+      const R yh = (cc(a, b + 1, c) + cc(a + 1, b + 1, c)) + (cc(a, b + 1, c + 1) + cc(a + 1, b + 1, c + 1));
+      const R yl = (cc(a, b, c) + cc(a + 1, b, c)) + (cc(a, b, c + 1) + cc(a + 1, b, c + 1));
+      // z: faces at z=c+1 and z=c, edges along x, summed over y
+      const R zh = (cc(a, b, c + 1) + cc(a + 1, b, c + 1)) + (cc(a, b + 1, c + 1) + cc(a + 1, b + 1, c + 1));
+      const R zl = (cc(a, b, c) + cc(a + 1, b, c)) + (cc(a, b + 1, c) + cc(a + 1, b + 1, c));
+      g[s][0] = xh - xl;
+      g[s][1] = yh - yl;
+      g[s][2] = zh - zl;
+    }
+  } else {
+    // FP32 paths: the same 2x2 face sums built from shared pair sums (96
+    // additions instead of 168); only the rounding order differs
+    R v[3][3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) v[i][j][k] = cc(i, j, k);
+    R pz[3][3][2], py[3][2][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int c = 0; c < 2; c++) pz[i][j][c] = v[i][j][c] + v[i][j][c + 1];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int b = 0; b < 2; b++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) py[i][b][k] = v[i][b][k] + v[i][b + 1][k];
+    R syz[3][2][2], sxz[2][3][2], sxy[2][2][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int b = 0; b < 2; b++)
+#pragma unroll
+        for (int c = 0; c < 2; c++) syz[i][b][c] = pz[i][b][c] + pz[i][b + 1][c];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int c = 0; c < 2; c++) sxz[a][j][c] = pz[a][j][c] + pz[a + 1][j][c];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int b = 0; b < 2; b++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) sxy[a][b][k] = py[a][b][k] + py[a + 1][b][k];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+      const int a = s & 1, b = (s >> 1) & 1, c = s >> 2;
+      g[s][0] = syz[a + 1][b][c] - syz[a][b][c];
+      g[s][1] = sxz[a][b + 1][c] - sxz[a][b][c];
+      g[s][2] = sxy[a][b][c + 1] - sxy[a][b][c];
+    }
   }
   R nx = g[0][0], ny = g[0][1], nz = g[0][2];
 #pragma unroll
@@ -459,6 +567,101 @@ PS_HD void node_update(const LbmConst<R>& K, const R* fr, const R* fb, R rr, R r
       out_r[i] = bulk_r ? c : K.t[0][w] * rr;
       out_b[i] = bulk_r ? K.t[1][w] * rb : c;
     }
+  }
+}
+
+// node_update for the FP32 paths in shifted form.  gr / gb are the node's
+// populations as deviations g_c[d] = f_c[d] - t^c_d rho^c_old from the
+// reference densities (ror, rob) they were stored against; rr = ror + sum
+// g_r and rb = rob + sum g_b are the current densities.  The post-collision
+// recoloured populations come out as out_c[d] = t^c_d S_c + Z_c[d]: a
+// receiver whose reference density is rho' stores t^c_d (S_c - rho') +
+// Z_c[d], again a small number.  Same branches, collision and recolouring
+// as node_update; only the representation differs.
+template <typename CC>
+PS_HD void node_update_dev(const LbmConst<float>& K, const float* gr, const float* gb, float ror, float rob,
+                           float rr, float rb, CC cc, float& Sr, float& Sb, float* Zr, float* Zb)
+{
+  using R = float;
+  const bool bulk_r = rb <= K.ee;
+  const bool bulk_b = !bulk_r && rr <= K.ee;
+  R gs[19];
+  if (!bulk_r && !bulk_b) {
+    R g[19], n[3], Fs[3], F[3];
+    csf_force(K, cc, n, Fs);
+    R dsum = R(0);
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      g[i] = gr[i] + gb[i];
+      dsum = dsum + g[i];
+    }
+    const R r = rr + rb, dr = rr - ror, db = rb - rob;
+    const R ci2 = (K.cs2[0] * rr + K.cs2[1] * rb) / r;
+    const R ti2 = ci2 * K.c1d6 * K.dt2, ti3 = ci2 * K.c1d12 * K.dt2;
+    // t_w r - T_w = t^r_w (rr - ror) + t^b_w (rb - rob) (the weights are linear in cs^2)
+    const R dr1 = K.t[0][1] * dr + K.t[1][1] * db, dr2 = K.t[0][2] * dr + K.t[1][2] * db;
+    const int ph = rr >= rb ? 0 : 1;
+    F[0] = K.bf[ph][0] + Fs[0];
+    F[1] = K.bf[ph][1] + Fs[1];
+    F[2] = K.bf[ph][2] + Fs[2];
+    trt_collide_dev(K, dr1, dr2, dsum, g, gs, r, F, K.S[ph][1], K.S[ph][4]);
+    // recolouring (S1:3797-3817): out_r = (f* + B w cos rb) rr / r with f* =
+    // T + g*; T_d = t^r_d (ror + rob) + (t^b_d - t^r_d) rob
+    const R inv = R(1) / r, qr = rr * inv, qb = rb * inv, ro = ror + rob;
+    Sr = qr * ro;
+    Sb = qb * ro;
+    R cs[19];
+    cs[0] = R(0);
+    cs[1] = n[0];
+    cs[2] = -cs[1];
+    cs[3] = n[1];
+    cs[4] = -cs[3];
+    cs[5] = n[2];
+    cs[6] = -cs[5];
+    cs[7] = (n[0] + n[1]) * K.cn;
+    cs[8] = (-n[0] + n[1]) * K.cn;
+    cs[9] = -cs[8];
+    cs[10] = -cs[7];
+    cs[11] = (n[0] + n[2]) * K.cn;
+    cs[12] = (-n[0] + n[2]) * K.cn;
+    cs[13] = -cs[12];
+    cs[14] = -cs[11];
+    cs[15] = (n[1] + n[2]) * K.cn;
+    cs[16] = (-n[1] + n[2]) * K.cn;
+    cs[17] = -cs[16];
+    cs[18] = -cs[15];
+    const bool same_w = K.t[0][1] == K.t[1][1];
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      const int wc = i == 0 ? 0 : (i < 7 ? 1 : 2);
+      const R w = i == 0 ? R(0) : K.B * (i < 7 ? ti2 : ti3) * cs[i];
+      Zr[i] = (gs[i] + w * rb) * qr;
+      Zb[i] = (gs[i] - w * rr) * qb;
+      if (!same_w) {
+        const R dtw = K.t[1][wc] - K.t[0][wc];
+        Zr[i] = Zr[i] + qr * dtw * rob;
+        Zb[i] = Zb[i] - qb * dtw * ror;
+      }
+    }
+  } else {
+    // one component collides against its own reference; the other stays at
+    // its rest equilibrium t_d rho (S = its density, no deviation)
+    const int c = bulk_r ? 0 : 1;
+    const float* g = bulk_r ? gr : gb;
+    const R ro = bulk_r ? ror : rob, rc = bulk_r ? rr : rb, d = rc - ro;
+    R dsum = R(0);
+#pragma unroll
+    for (int i = 0; i < 19; i++) dsum = dsum + g[i];
+    trt_collide_dev(K, K.t[c][1] * d, K.t[c][2] * d, dsum, g, gs, rc, K.bf[c], K.S[c][1], K.S[c][4]);
+    float* Zc = bulk_r ? Zr : Zb;
+    float* Zo = bulk_r ? Zb : Zr;
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+      Zc[i] = gs[i];
+      Zo[i] = R(0);
+    }
+    Sr = bulk_r ? ror : rr;
+    Sb = bulk_r ? rb : rob;
   }
 }
 

@@ -1,6 +1,8 @@
 // lbm_prec_impl.cuh -- launcher bodies for one storage precision PREC.
 // Included by lbm_prec_f64.cu (PREC 0) and lbm_prec_lp.cu (PREC 1..3).
 #pragma once
+#include <algorithm>
+
 #include "lbm_launch.h"
 
 namespace ps {
@@ -16,6 +18,44 @@ cudaError_t step_blk(const LbmLaunchArgs& a)
   R* cc = static_cast<R*>(a.cc);
   k_lbm_dens<PREC, BD><<<(unsigned)((n + BD - 1) / BD), BD, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
   k_lbm_coll<PREC, BC, MINB><<<(unsigned)((n + BC - 1) / BC), BC, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
+  return cudaGetLastError();
+}
+
+// resident CTAs per SM x SMs: the persistent grid of a batched kernel
+template <typename Kern>
+int persistent_grid(Kern kern, int blk)
+{
+  int dev = 0, sms = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, blk, 0);
+  return std::max(1, sms * std::max(1, occ));
+}
+
+template <int PREC, int BC, int BD, int MINB = 0>
+cudaError_t step_batch_blk(const BatchLaunchArgs& b)
+{
+  using R = typename Store<PREC>::R;
+  const LbmConst<R>& C = *static_cast<const LbmConst<R>*>(b.K);
+  static const int gd = persistent_grid(k_lbm_dens_batch<PREC, BD>, BD);
+  static const int gc = persistent_grid(k_lbm_coll_batch<PREC, BC, MINB>, BC);
+  if (b.ntd > 0)
+    k_lbm_dens_batch<PREC, BD><<<std::min(gd, b.ntd), BD, 0, b.stream>>>(C, *b.T, b.tiles_d, b.ntd);
+  if (b.ntc > 0)
+    k_lbm_coll_batch<PREC, BC, MINB><<<std::min(gc, b.ntc), BC, 0, b.stream>>>(C, *b.T, b.tiles_c, b.ntc);
+  return cudaGetLastError();
+}
+
+template <int PREC, int BLK, int MINB = 0>
+cudaError_t step_fused_blk(const LbmLaunchArgs& a, const FusedArgs& f)
+{
+  using R = typename Store<PREC>::R;
+  if (f.nitems == 0) return cudaSuccess;
+  static const int gmax = persistent_grid(k_lbm_fused<PREC, BLK, MINB>, BLK);
+  cudaError_t e = cudaMemsetAsync(f.ctr, 0, sizeof(unsigned) * (size_t)(1 + f.nslab), a.stream);
+  if (e != cudaSuccess) return e;
+  k_lbm_fused<PREC, BLK, MINB><<<std::min(gmax, f.nitems), BLK, 0, a.stream>>>(
+      *static_cast<const LbmConst<R>*>(a.K), a.G, a.src, a.dst, static_cast<R*>(a.cc), f);
   return cudaGetLastError();
 }
 
@@ -64,6 +104,16 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
   return cudaGetLastError();
 }
 
+template <int PREC>
+cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp, double rsdti2, double* out)
+{
+  using R = typename Store<PREC>::R;
+  const long long n = a.G.nvox;
+  k_lbm_wall_load<PREC><<<(unsigned)((n + 127) / 128), 128, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K),
+                                                                           a.G, a.src, fq1, fq2, ppp, rsdti2, out);
+  return cudaGetLastError();
+}
+
 }  // namespace detail
 }  // namespace ps
 
@@ -88,6 +138,27 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
     if (tx == 256 && ty == 256 && occ == 3) return detail::step_blk<P, 256, 256, 3>(a);                    \
     return cudaErrorInvalidValue;                                                                          \
   }                                                                                                        \
+  cudaError_t lbm_fused_launch_##P(int tx, int occ, const LbmLaunchArgs& a, const FusedArgs& f)           \
+  {                                                                                                        \
+    if (tx == 128 && occ == 0) return detail::step_fused_blk<P, 128>(a, f);                                \
+    if (tx == 256 && occ == 0) return detail::step_fused_blk<P, 256>(a, f);                                \
+    if (tx == 128 && occ == 6) return detail::step_fused_blk<P, 128, 6>(a, f);                             \
+    if (tx == 128 && occ == 8) return detail::step_fused_blk<P, 128, 8>(a, f);                             \
+    return cudaErrorInvalidValue;                                                                          \
+  }                                                                                                        \
+  cudaError_t lbm_batch_step_launch_##P(int tx, int ty, int occ, const BatchLaunchArgs& b)                \
+  {                                                                                                        \
+    if (occ == 0) {                                                                                        \
+      if (tx == 128 && ty == 256) return detail::step_batch_blk<P, 128, 256>(b);                           \
+      if (tx == 256 && ty == 256) return detail::step_batch_blk<P, 256, 256>(b);                           \
+      if (tx == 128 && ty == 128) return detail::step_batch_blk<P, 128, 128>(b);                           \
+      if (tx == 256 && ty == 512) return detail::step_batch_blk<P, 256, 512>(b);                           \
+    }                                                                                                      \
+    if (tx == 128 && ty == 256 && occ == 6) return detail::step_batch_blk<P, 128, 256, 6>(b);              \
+    if (tx == 128 && ty == 256 && occ == 8) return detail::step_batch_blk<P, 128, 256, 8>(b);              \
+    if (tx == 256 && ty == 256 && occ == 3) return detail::step_batch_blk<P, 256, 256, 3>(b);              \
+    return cudaErrorInvalidValue;                                                                          \
+  }                                                                                                        \
   cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc) \
   {                                                                                                        \
     return detail::fields<P>(a, rr, rb, cf, cc);                                                           \
@@ -104,6 +175,11 @@ cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int n
                                  double* out)                                                              \
   {                                                                                                        \
     return detail::obs<P>(a, cc, partial, nblocks, out);                                                   \
+  }                                                                                                        \
+  cudaError_t lbm_wall_load_launch_##P(const LbmLaunchArgs& a, double fq1, double fq2, double ppp, double rsdti2, \
+                                      double* out)                                                          \
+  {                                                                                                        \
+    return detail::wall_load<P>(a, fq1, fq2, ppp, rsdti2, out);                                            \
   }                                                                                                        \
   size_t lbm_step_smem_##P(int tx, int ty, int occ)                                                        \
   {                                                                                                        \

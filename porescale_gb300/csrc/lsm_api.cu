@@ -22,6 +22,7 @@
 #include "lsm_cube.h"
 #include "lsm_kernels.cuh"
 #include "ps_common.h"
+#include "ps_coupling.h"
 
 namespace ps {
 namespace {
@@ -46,6 +47,9 @@ struct Springs {
   cudaStream_t stream = nullptr;
   uint8_t *d_mat = nullptr, *d_node = nullptr;
   double *d_K64 = nullptr, *d_S64 = nullptr;  // per-material cube matrices of this handle
+  double* d_Kab = nullptr;                      // material-independent Ka, Kb (modulus gradients)
+  double* fext = nullptr;                       // external nodal load [3][nvox] (fluid wall load)
+  bool has_load = false;
   float* d_K32 = nullptr;
   // FP64 vectors (3*nvox each)
   double *b = nullptr, *x = nullptr, *r = nullptr, *p64 = nullptr, *q64 = nullptr;
@@ -68,6 +72,8 @@ void free_springs(Springs* S)
   cudaFree(S->d_K64);
   cudaFree(S->d_K32);
   cudaFree(S->d_S64);
+  cudaFree(S->d_Kab);
+  cudaFree(S->fext);
   cudaFree(S->b);
   cudaFree(S->x);
   cudaFree(S->r);
@@ -303,7 +309,7 @@ int compute_stress(Springs* S, ps_lsm_result* out)
   const double nax = S->pa == 0 ? S->nx : S->ny;
   const double s = S->pa == 0 ? sig[0] : sig[5];  // asigmap(1,1) or asigmap(2,3)
   out->strain = jump / nax;
-  out->modulus = s / (vcell * jump / nax);
+  out->modulus = jump != 0.0 ? s / (vcell * jump / nax) : 0.0;
   return PS_OK;
 }
 
@@ -343,6 +349,80 @@ int noalloc_scratch(double** out)
   }
   *out = g_scratch_ptr[dev];
   return PS_OK;
+}
+
+// fext = the load on existing nodes; counts loaded corners that are not
+// nodes of this network
+__global__ void k_take_load(int nv, const uint8_t* node, const double* box, double* fext, unsigned long long* lost)
+{
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const bool ok = node[v] != 0;
+  bool loaded = false;
+  for (int c = 0; c < 3; c++) {
+    const double f = box[(size_t)c * nv + v];
+    loaded |= f != 0.0;
+    fext[(size_t)c * nv + v] = ok ? f : 0.0;
+  }
+  if (loaded && !ok) atomicAdd(lost, 1ull);
+}
+
+__global__ void k_add(int n, const double* a, double* b)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] += a[i];
+}
+
+// Surface term of calc_ab's beta (S1:4262-4437) for pore labels
+// [p0, p0 + 32): a pore voxel of label p with a solid (label 0) axis
+// neighbour d contributes -u_face . c_d, u_face the mean displacement of the
+// 4 corner nodes of the shared face.  Per-block FP64 partial sums
+// part[32 b + (p - p0)].
+__global__ void __launch_bounds__(256) k_beta_surface(const LsmGeom G, const int32_t* __restrict__ lab, int p0,
+                                                      const double* __restrict__ u, double* __restrict__ part)
+{
+  const int v = blockIdx.x * 256 + threadIdx.x;
+  int p = -1;
+  double val = 0.0;
+  if (v < G.nvox) {
+    const int l = lab[v];
+    if (l >= p0 && l < p0 + 32 && l > 0) {
+      p = l - p0;
+      const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
+      const int c3[3] = {v % nx, (v / nx) % ny, v / (nx * ny)};
+      const int n3[3] = {nx, ny, nz};
+      for (int d = 0; d < 6; d++) {  // +x, -x, +y, -y, +z, -z (reference l = 2..7)
+        const int ax = d >> 1, sg = (d & 1) ? -1 : 1;
+        int w[3] = {c3[0], c3[1], c3[2]};
+        w[ax] = lsm::wrap_add(c3[ax], sg, n3[ax]);
+        if (lab[w[0] + nx * (w[1] + ny * w[2])] != 0) continue;
+        // face corners: offset (sg + 1) / 2 along ax, 0/1 along the others
+        const int a1 = (ax + 1) % 3, a2 = (ax + 2) % 3;
+        double up[3] = {0.0, 0.0, 0.0};
+        for (int q = 0; q < 4; q++) {
+          int cn[3];
+          cn[ax] = lsm::wrap_add(c3[ax], (sg + 1) / 2, n3[ax]);
+          cn[a1] = lsm::wrap_add(c3[a1], q & 1, n3[a1]);
+          cn[a2] = lsm::wrap_add(c3[a2], q >> 1, n3[a2]);
+          const int nb = cn[0] + nx * (cn[1] + ny * cn[2]);
+          for (int c = 0; c < 3; c++) up[c] += u[(size_t)c * nv + nb];
+        }
+        val -= 0.25 * up[ax] * (double)sg;
+      }
+    }
+  }
+  __shared__ double red[32][8];
+  for (int q = 0; q < 32; q++) {
+    double t = (p == q) ? val : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int w = 0; w < 8; w++) t += red[threadIdx.x][w];
+    part[(long long)blockIdx.x * 32 + threadIdx.x] = t;
+  }
 }
 
 }  // namespace
@@ -398,8 +478,13 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
     lsm::build_cube_matrices(M);
     built = true;
   }
-  std::vector<double> K64(2 * 24 * 24), S64(2 * 9 * 24);
+  std::vector<double> K64(2 * 24 * 24), S64(2 * 9 * 24), Kab(2 * 24 * 24);
   std::vector<float> K32(2 * 24 * 24);
+  for (int i = 0; i < 24; i++)
+    for (int j = 0; j < 24; j++) {
+      Kab[i * 24 + j] = M.Ka[i][j];
+      Kab[576 + i * 24 + j] = M.Kb[i][j];
+    }
   const double al[2] = {p->alf1, p->alf2}, be[2] = {p->bet1, p->bet2};
   for (int m = 0; m < 2; m++) {
     for (int i = 0; i < 24; i++)
@@ -428,9 +513,11 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   if (int r = dalloc(S.get(), &S->d_K64, sizeof(double) * K64.size())) return r;
   if (int r = dalloc(S.get(), &S->d_K32, sizeof(float) * K32.size())) return r;
   if (int r = dalloc(S.get(), &S->d_S64, sizeof(double) * S64.size())) return r;
+  if (int r = dalloc(S.get(), &S->d_Kab, sizeof(double) * Kab.size())) return r;
   PS_CUDA(cudaMemcpyAsync(S->d_K64, K64.data(), sizeof(double) * K64.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_K32, K32.data(), sizeof(float) * K32.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_S64, S64.data(), sizeof(double) * S64.size(), cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaMemcpyAsync(S->d_Kab, Kab.data(), sizeof(double) * Kab.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaStreamSynchronize(S->stream));
   *handle = S.release();
   return PS_OK;
@@ -474,6 +561,10 @@ int ps_lsm_solve(void* h, double rtol, int32_t maxit, ps_lsm_result* out)
   // right-hand side of the tied system, without its translation component
   lsm::k_lsm_rhs<<<nb, kBlk, 0, S->stream>>>(G, S->pa, S->jc, 2.0 * S->p.gstrain, S->b);
   PS_CUDA(cudaGetLastError());
+  if (S->has_load) {  // fluid wall load; its net force is removed with the mean below
+    k_add<<<nb3, kBlk, 0, S->stream>>>(n3, S->fext, S->b);
+    PS_CUDA(cudaGetLastError());
+  }
   if (int e = project_mean(S, S->b)) return e;
   k_sq_norm<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->part);
   if (int e = sum_parts(S, nb3, S->scal + 17)) return e;
@@ -531,6 +622,113 @@ int ps_lsm_solve(void* h, double rtol, int32_t maxit, ps_lsm_result* out)
   S->solved = true;
   S->last = *out;
   return out->converged ? PS_OK : fail(PS_ERR_NOTCONV, "ps_lsm_solve: relative residual %.3e above %.3e", rel, rtol);
+}
+
+// Modulus gradients with respect to the four spring constants.  The
+// stiffness is linear in each constant (K = sum over cubes of alf_m Ka +
+// bet_m Kb), the converged displacement minimises the spring energy W under
+// the tie, so dW/dk = 1/2 u^T (dK/dk) u at fixed u; with modulus = 2 W /
+// (V strain^2) (periodic box under the imposed strain), d modulus / dk =
+// u^T (dK/dk) u / (V strain^2).
+int ps_lsm_gradients(void* h, double* grad)
+{
+  if (!h || !grad) return fail(PS_ERR_ARG, "ps_lsm_gradients: null argument");
+  Springs* S = static_cast<Springs*>(h);
+  if (!S->solved) return fail(PS_ERR_STATE, "ps_lsm_gradients: no solution yet");
+  if (!(S->p.gstrain != 0.0)) return fail(PS_ERR_STATE, "ps_lsm_gradients: needs a nonzero imposed strain");
+  const int nb = blocks_for(S->nvox);
+  const double jump = 2.0 * S->p.gstrain;
+  lsm::k_lsm_energy<kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->pa, S->jc, jump, S->x, S->d_Kab, S->part);
+  PS_CUDA(cudaGetLastError());
+  std::vector<double> hp((size_t)nb * 4);
+  PS_CUDA(cudaMemcpyAsync(hp.data(), S->part, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  double q[4] = {0, 0, 0, 0};  // u^T Ka u, u^T Kb u for material 1, then material 2
+  for (int b = 0; b < nb; b++)
+    for (int i = 0; i < 4; i++) q[i] += hp[(size_t)b * 4 + i];
+  const double vcell = (double)S->nx * S->ny * S->nz;
+  const double strain = jump / (S->pa == 0 ? S->nx : S->ny);
+  const double den = vcell * strain * strain;
+  for (int i = 0; i < 4; i++) grad[i] = q[i] / den;
+  // the energy form of the modulus: 2 W / (V strain^2), W = 1/2 sum k q_k
+  grad[4] = (S->p.alf1 * q[0] + S->p.bet1 * q[1] + S->p.alf2 * q[2] + S->p.bet2 * q[3]) / den;
+  return PS_OK;
+}
+
+int ps_lsm_set_wall_load(void* h, void* lattice, double rsi)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lsm_set_wall_load: null handle");
+  Springs* S = static_cast<Springs*>(h);
+  S->solved = false;
+  if (!lattice) {
+    S->has_load = false;
+    return PS_OK;
+  }
+  const double* box = nullptr;
+  int dims[3] = {0, 0, 0};
+  if (int e = lbm_wall_load_box(lattice, rsi, &box, dims)) return e;
+  if (dims[0] != S->nx || dims[1] != S->ny || dims[2] != S->nz)
+    return fail(PS_ERR_ARG, "ps_lsm_set_wall_load: lattice box %dx%dx%d differs from the network's %dx%dx%d", dims[0],
+                dims[1], dims[2], S->nx, S->ny, S->nz);
+  const int nv = S->nvox;
+  if (!S->fext)
+    if (int r = dalloc(S, &S->fext, sizeof(double) * 3 * (size_t)nv)) return r;
+  // the lost-corner counter lives in the scalar block (slot 24)
+  unsigned long long* lost = reinterpret_cast<unsigned long long*>(S->scal + 24);
+  PS_CUDA(cudaMemsetAsync(lost, 0, sizeof(unsigned long long), S->stream));
+  k_take_load<<<blocks_for(nv), kBlk, 0, S->stream>>>(nv, S->d_node, box, S->fext, lost);
+  PS_CUDA(cudaGetLastError());
+  unsigned long long nlost = 0;
+  PS_CUDA(cudaMemcpyAsync(&nlost, lost, sizeof nlost, cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  if (nlost) {
+    S->has_load = false;
+    return fail(PS_ERR_ARG, "ps_lsm_set_wall_load: %llu loaded corners are not nodes of the spring network", nlost);
+  }
+  S->has_load = true;
+  return PS_OK;
+}
+
+int ps_lsm_alpha_beta(void* h, const int32_t* lab, int32_t npores, int32_t iipore, double pres, double* alpha,
+                      double* beta)
+{
+  if (!h || !lab || !alpha || (npores > 0 && !beta)) return fail(PS_ERR_ARG, "ps_lsm_alpha_beta: null argument");
+  if (npores < 0 || !(pres != 0.0)) return fail(PS_ERR_ARG, "ps_lsm_alpha_beta: need npores >= 0 and pres != 0");
+  Springs* S = static_cast<Springs*>(h);
+  if (!S->solved) return fail(PS_ERR_STATE, "ps_lsm_alpha_beta: no solution yet");
+  const int nv = S->nvox;
+  const double vcell = (double)S->nx * S->ny * S->nz;
+  long long npore = 0;
+  for (int v = 0; v < nv; v++) npore += lab[v] == iipore;
+  const double epsi = (double)npore / vcell;
+  // alpha_i = -epsi I + asigmap / vcell / pres (S1:4257)
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) alpha[3 * r + c] = (r == c ? -epsi : 0.0) + S->last.sigma[3 * r + c] / vcell / pres;
+  if (npores == 0) return PS_OK;
+  int32_t* d_lab = nullptr;
+  PS_CUDA(cudaMallocAsync((void**)&d_lab, sizeof(int32_t) * (size_t)nv, S->stream));
+  int rc = PS_OK;
+  const int nb = (nv + 255) / 256;
+  double* part = nullptr;
+  std::vector<double> hp((size_t)nb * 32);
+  cudaError_t e = cudaMallocAsync((void**)&part, sizeof(double) * hp.size(), S->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_lab, lab, sizeof(int32_t) * (size_t)nv, cudaMemcpyHostToDevice, S->stream);
+  for (int p0 = 1; e == cudaSuccess && p0 <= npores; p0 += 32) {
+    k_beta_surface<<<nb, 256, 0, S->stream>>>(S->geom(), d_lab, p0, S->x, part);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), part, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, S->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+    for (int q = 0; e == cudaSuccess && q < 32 && p0 + q <= npores; q++) {
+      double t = 0.0;
+      for (int b = 0; b < nb; b++) t += hp[(size_t)b * 32 + q];
+      beta[p0 + q - 1] = t / vcell / pres;  // S1:4439
+    }
+  }
+  if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_alpha_beta");
+  cudaFreeAsync(part, S->stream);
+  cudaFreeAsync(d_lab, S->stream);
+  cudaStreamSynchronize(S->stream);
+  return rc;
 }
 
 int ps_lsm_get_disp(void* h, double* u)

@@ -168,6 +168,60 @@ __global__ void __launch_bounds__(BLK) k_lsm_stress(const LsmGeom G, int pa, int
   }
 }
 
+// per-block FP64 sums of the quadratic forms u_c^T Ka u_c and u_c^T Kb u_c
+// of every solid cube (24 corner displacements u_c with the jump across the
+// tie), by material: part[4 b + 2 (m - 1) + {0: Ka, 1: Kb}].  Kab holds the
+// material-independent cube matrices Ka then Kb ([2][24][24]).
+template <int BLK>
+__global__ void __launch_bounds__(BLK) k_lsm_energy(const LsmGeom G, int pa, int jc, double jump,
+                                                    const double* __restrict__ u, const double* __restrict__ Kab,
+                                                    double* __restrict__ part)
+{
+  const int v = blockIdx.x * BLK + threadIdx.x;
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  if (v < G.nvox) {
+    const int m = G.mat[v];
+    if (m) {
+      const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
+      const int c3[3] = {v % nx, (v / nx) % ny, v / (nx * ny)};
+      const int n3[3] = {nx, ny, nz};
+      double ul[24];
+      for (int b = 0; b < 8; b++) {
+        const int bb[3] = {b & 1, (b >> 1) & 1, b >> 2};
+        int w[3];
+        for (int d = 0; d < 3; d++) w[d] = wrap_add(c3[d], bb[d], n3[d]);
+        const int nb = w[0] + nx * (w[1] + ny * w[2]);
+        for (int d = 0; d < 3; d++) ul[3 * b + d] = u[d * nv + nb];
+        if (bb[pa] && c3[pa] == n3[pa] - 1) ul[3 * b + jc] += jump;
+      }
+      double ea = 0.0, eb = 0.0;
+      for (int r = 0; r < 24; r++) {
+        double ar = 0.0, br = 0.0;
+        for (int c = 0; c < 24; c++) {
+          ar += __ldg(Kab + r * 24 + c) * ul[c];
+          br += __ldg(Kab + 576 + r * 24 + c) * ul[c];
+        }
+        ea += ul[r] * ar;
+        eb += ul[r] * br;
+      }
+      s[2 * (m - 1)] = ea;
+      s[2 * (m - 1) + 1] = eb;
+    }
+  }
+  __shared__ double red[4][BLK / 32];
+  for (int i = 0; i < 4; i++) {
+    double t = s[i];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int w = 0; w < BLK / 32; w++) t += red[threadIdx.x][w];
+    part[(long long)blockIdx.x * 4 + threadIdx.x] = t;
+  }
+}
+
 // ---- CG vector kernels (device-resident scalars, no host round trips) ----
 // scal[]: 0 rr, 1 pq, 2 alpha, 3 beta, 4 rr_new, 5 bb (|b|^2), 6 done flag
 __global__ void k_sum(const double* __restrict__ part, int n, double* __restrict__ out)

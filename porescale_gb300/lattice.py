@@ -125,6 +125,10 @@ class Lattice:
         check(self._lib.ps_lbm_set_tile(self._h, tx, ty, occ))
         self.info = self.get_info()
 
+    def set_fused(self, planes: int, ahead: int = 1) -> None:
+        """Fused one-launch step over z-slabs of `planes` planes (0: two-pass)."""
+        check(self._lib.ps_lbm_set_fused(self._h, planes, ahead))
+
     def autotune(self, steps: int = 4):
         tx, ty, zc = C.c_int32(), C.c_int32(), C.c_int32()
         check(self._lib.ps_lbm_autotune(self._h, steps, C.byref(tx), C.byref(ty), C.byref(zc)))
@@ -141,3 +145,57 @@ class Lattice:
         rr, rb, cf = np.empty(self.nl), np.empty(self.nl), np.empty(self.nl)
         check(self._lib.ps_lbm_fields(self._h, dptr(rr), dptr(rb), dptr(cf)))
         return rr, rb, cf
+
+    def wall_load(self, rsi: float = 1.0) -> np.ndarray:
+        """afdat as (ns, 3): the fluid's wall load on the LSM nodes in the
+        reference's node order (S1:3849-3882)."""
+        out = np.zeros((self.info.ns, 3))
+        check(self._lib.ps_lbm_wall_load(self._h, float(rsi), dptr(out)))
+        return out
+
+
+class LatticeBatch:
+    """Many lattices (same precision and parameters) advanced by shared
+    persistent launches replayed from a CUDA graph (ps_batch_*).  The
+    lattices remain usable on their own and must outlive the batch."""
+
+    def __init__(self, lattices):
+        self.lattices = list(lattices)
+        self._lib = self.lattices[0]._lib
+        arr = (C.c_void_p * len(self.lattices))(*[L._h.value for L in self.lattices])
+        h = C.c_void_p()
+        check(self._lib.ps_batch_create(arr, len(self.lattices), C.byref(h)))
+        self._h = h
+        self.nodes = sum(L.nl for L in self.lattices)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.ps_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, n: int = 1) -> None:
+        check(self._lib.ps_batch_step(self._h, int(n)))
+
+    def set_tile(self, tx: int, ty: int, occ: int = 0) -> None:
+        check(self._lib.ps_batch_set_tile(self._h, tx, ty, occ))
+
+    def autotune(self, steps: int = 6):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        check(self._lib.ps_batch_autotune(self._h, steps, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.ps_batch_stream(self._h) or 0)

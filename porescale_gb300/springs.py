@@ -46,6 +46,10 @@ _SIGS = {
     "ps_lsm_get_disp": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ps_lsm_stream": (C.c_void_p, [C.c_void_p]),
     "ps_lsm_stress_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "ps_lsm_gradients": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "ps_lsm_set_wall_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
+    "ps_lsm_alpha_beta": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.c_double,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 _lib.SIGNATURES.update(_SIGS)
 
@@ -103,6 +107,26 @@ class SpringNetwork:
         u = np.zeros((ns, 3))
         check(self._lib.ps_lsm_get_disp(self._h, dptr(u)))
         return u
+
+    def gradients(self) -> np.ndarray:
+        """d modulus / d(alf1, bet1, alf2, bet2) at the last converged
+        solution, then the energy form of the modulus (5 values)."""
+        g = np.zeros(5)
+        check(self._lib.ps_lsm_gradients(self._h, dptr(g)))
+        return g
+
+    def set_wall_load(self, lattice, rsi: float = 1.0) -> None:
+        """Applies the wall load of `lattice` (a Lattice on the same box) in
+        the following solves; None removes it."""
+        check(self._lib.ps_lsm_set_wall_load(self._h, lattice._h if lattice is not None else None, float(rsi)))
+
+    def alpha_beta(self, lab: np.ndarray, npores: int, iipore: int, pres: float):
+        """calc_ab on the last solution: (alpha[3,3], beta[npores])."""
+        lab = np.ascontiguousarray(lab, np.int32)
+        a = np.zeros(9)
+        b = np.zeros(max(npores, 1))
+        check(self._lib.ps_lsm_alpha_beta(self._h, iptr(lab), int(npores), int(iipore), float(pres), dptr(a), dptr(b)))
+        return a.reshape(3, 3), b[:npores]
 
     @property
     def stream(self) -> int:

@@ -43,6 +43,6 @@ def test_version_and_error_without_gpu(lib):
 
 
 def test_python_bindings_cover_header():
-    from porescale_gb300 import _lib, springs  # noqa: F401  (springs registers its signatures)
+    from porescale_gb300 import _lib, gray, springs  # noqa: F401  (these register their signatures)
     missing = [n for n in _declared() if n not in _lib.SIGNATURES]
     assert not missing, missing

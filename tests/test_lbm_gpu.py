@@ -159,3 +159,23 @@ def test_plain_two_phase_64_workload(gpu, oracle_lib):
     for k in ("permr", "permb", "tmr", "tmb"):
         assert g[k] == pytest.approx(ob[k], rel=1e-11), k
     assert (g["nr"], g["nb"]) == (ob["nr"], ob["nb"])
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2, 3])
+@pytest.mark.parametrize("planes,ahead,tile", [(1, 1, (128, 256, 0)), (3, 2, (256, 256, 0)), (4, 1, (128, 256, 8))])
+def test_fused_step_matches_two_pass(gpu, prec, planes, ahead, tile):
+    """The fused one-launch step (density and collide tiles of z-slabs from
+    one work list) gives the two-pass step's state bit for bit."""
+    ind = geo.sphere_pack((22, 18, 20), 0.45, 3.0, seed=17)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    out = []
+    for fused in (False, True):
+        with Lattice(p, ind, prec) as L:
+            L.init_random(0.5)
+            L.set_tile(*tile)
+            if fused:
+                L.set_fused(planes, ahead)
+                assert L.get_info().schedule == planes + 256 * ahead
+            L.step(9)
+            out.append(L.get_state())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])

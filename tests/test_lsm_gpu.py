@@ -71,3 +71,43 @@ def test_relaxation_reaches_cg_solution(gpu, oracle_lib):
     with SpringNetwork(ind, A1, B1, A2, B2, g, LOAD_XSTRETCH, LSM_F64) as S:
         r = S.solve(1e-12, 100000)
     assert r.modulus == pytest.approx(dr, rel=1e-7)
+
+
+@pytest.mark.parametrize("load", [LOAD_XSTRETCH, LOAD_YZSHEAR])
+def test_modulus_gradients_vs_central_differences(gpu, load):
+    """d modulus / d(alf1, bet1, alf2, bet2) from the spring energies at the
+    converged displacement against FP64 central finite differences of the
+    modulus itself (h = 1e-4 relative), within 1e-4 relative; the energy
+    form of the modulus equals the stress form at equilibrium."""
+    ind = _two_phase(n=12, seed=9, r=3.0)
+    k0 = np.array([A1, B1, A2, B2])
+    g = 1e-3 * 12 / 2
+    with SpringNetwork(ind, *k0, g, load, LSM_F64) as S:
+        r = S.solve(1e-12, 100000)
+        grad = S.gradients()
+    assert grad[4] == pytest.approx(r.modulus, rel=1e-9)
+    for k in range(4):
+        h = 1e-4 * k0[k]
+        mods = []
+        for sgn in (1, -1):
+            kk = k0.copy()
+            kk[k] += sgn * h
+            with SpringNetwork(ind, *kk, g, load, LSM_F64) as S:
+                mods.append(S.solve(1e-13, 100000).modulus)
+        fd = (mods[0] - mods[1]) / (2 * h)
+        assert grad[k] == pytest.approx(fd, rel=1e-4), (k, grad[k], fd)
+    # homogeneous-limit identity: modulus = sum_k k dC/dk (C is homogeneous
+    # of degree 1 in the spring constants)
+    assert float(np.dot(k0, grad[:4])) == pytest.approx(r.modulus, rel=1e-9)
+
+
+def test_modulus_gradients_mixed_precision(gpu):
+    """The mixed-precision solution gives the same gradients within 1e-6."""
+    ind = _two_phase(n=12, seed=9, r=3.0)
+    g = 1e-3 * 6
+    out = []
+    for prec in (LSM_F64, LSM_MIXED):
+        with SpringNetwork(ind, A1, B1, A2, B2, g, LOAD_XSTRETCH, prec) as S:
+            S.solve(1e-11, 100000)
+            out.append(S.gradients())
+    assert np.allclose(out[1], out[0], rtol=1e-6, atol=0)

@@ -183,3 +183,54 @@ def test_cube_tables_match_reference(oracle_lib):
     angles = sorted([*map(int, x), float(s)] for x, s in zip(a, ab))
     assert bonds == [list(r) for r in g["cube_bonds"]]
     assert angles == [list(r) for r in g["cube_angles"]]
+
+
+def test_wall_load_of_fluid_at_rest_has_no_net_force(oracle_lib):
+    """S1:3849-3882 on a fluid at rest at uniform density (no body force):
+    every wall link carries 0.01 of its rest population (ppp = 0.99), and
+    the loads of a periodic pack sum to zero (open links pair up, so the
+    closed ones balance), while single nodes see a nonzero pressure load."""
+    ind = geo.sphere_pack((12, 10, 14), 0.45, 2.5, seed=2)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=1 / 6, wet=0.5, bfr=(0, 0, 0), bfb=(0, 0, 0))
+    o = oracle_lib.OracleLattice(p, ind)
+    t = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    fr = np.tile(t, (o.nl, 1))
+    o.set_state(fr, np.zeros_like(fr))
+    o.run(1)
+    a = o.wall_load(1.0)
+    assert np.abs(a).max() > 1e-4
+    assert np.abs(a.sum(0)).max() < 1e-13
+    # a face link gives -2 (0.01/18) c / 4 per node, an edge link -2 (0.01/36)
+    # c / 2: both 0.01/36 per component, so every nodal load is a multiple
+    k = a * 3600.0
+    assert np.abs(k - np.round(k)).max() < 1e-9
+
+
+def test_gray_adjoint_matches_central_differences(oracle_lib):
+    """The oracle's discrete adjoint of the gray partial-bounce-back lattice
+    against central finite differences of its own forward (h = 1e-5)."""
+    rng = np.random.default_rng(1)
+    s = rng.uniform(0, 1, (6, 5, 7)) ** 3
+    p = oracle_lib.gray_params(0.8, 3 / 16, (1e-5, 0, 0), 1, 60)
+    k, dk = oracle_lib.gray_gradient(p, s)
+    assert k == oracle_lib.gray_forward(p, s)[0]
+    h = 1e-5
+    for v in [(0, 0, 0), (3, 2, 4), (5, 4, 6), (1, 1, 1), (2, 3, 0)]:
+        kk = []
+        for sg in (1, -1):
+            sp = s.copy()
+            sp[v] += sg * h
+            kk.append(oracle_lib.gray_forward(p, sp)[0])
+        fd = (kk[0] - kk[1]) / (2 * h)
+        assert dk[v] == pytest.approx(fd, rel=1e-5)
+
+
+def test_gray_open_channel_permeability(oracle_lib):
+    """s = 0 everywhere: no resistance, the body force accelerates the fluid
+    uniformly (momentum gains F per step and node), so k = nu (T + 1/2)."""
+    s = np.zeros((4, 4, 4))
+    T = 40
+    p = oracle_lib.gray_params(0.9, 3 / 16, (1e-6, 0, 0), 1, T)
+    k, _ = oracle_lib.gray_forward(p, s)
+    nu = (0.9 - 0.5) / 3
+    assert k == pytest.approx(nu * (T + 0.5), rel=1e-10)
