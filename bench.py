@@ -359,10 +359,13 @@ def batch_mode(args):
     two-solid lattice-spring network of the same voxels (matrix alpha 1.0,
     beta 0.4; radius-3 inclusions at fraction 0.25 of the solid, alpha 0.3,
     beta 0.1) solved for Cxxxx and Cyzyz.  A few subvolumes are also run on
-    the plain FP64 path for the speed and error comparison."""
+    the plain FP64 path for the speed and error comparison.  Solid clusters
+    not joined to the largest one (free bodies under a wall load) are made
+    pore in both models."""
     import concurrent.futures as cf
     import torch
     from porescale_gb300 import geometry
+    from porescale_gb300._lib import PorescaleError
     from porescale_gb300.lattice import Lattice, LatticeBatch, make_params
     from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_MIXED, SpringNetwork
     specs = batch_workload(args.batch_volumes, 20240607)
@@ -371,7 +374,9 @@ def batch_mode(args):
     prec = PREC_ID[args.prec]
     inds, lats = [], []
     for sp in specs:
-        ind = geometry.sphere_pack(sp["edge"], sp["porosity"], sp["radius"], sp["seed"])
+        # solid clusters not joined to the skeleton are free bodies with no
+        # static equilibrium under a wall load: they become pore in both models
+        ind = geometry.spanning_solid(geometry.sphere_pack(sp["edge"], sp["porosity"], sp["radius"], sp["seed"]))
         L = Lattice(p, ind, prec)
         L.init_random(sp["sat"])
         inds.append(ind)
@@ -379,7 +384,7 @@ def batch_mode(args):
     nodes = sum(L.nl for L in lats)
     T = args.batch_steps
     peak, peak_kind = load_peaks()
-    bpn = {"f64": 640, "f32": 320, "f16": 168, "bf16": 168}[args.prec]
+    bpn = ALGO_BYTES[args.prec]
     with LatticeBatch(lats) as B:
         tile = B.autotune(4)
         stream = torch.cuda.ExternalStream(B.stream)
@@ -402,14 +407,46 @@ def batch_mode(args):
         for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
             with SpringNetwork(ind_s, 1.0, 0.4, 0.3, 0.1, 1e-3 * ind.shape[2] / 2, load, LSM_MIXED) as S:
                 S.set_wall_load(lats[v], 1.0)
-                r = S.solve(1e-8, 400000)
-                out[name] = r.modulus
+                try:
+                    r = S.solve(1e-8, 400000)
+                    out[name] = r.modulus
+                except PorescaleError as exc:
+                    out[name] = None
+                    out[name + "_error"] = str(exc)
         return out
 
+    # all networks of a load case in one batched solve (shared launches)
+    from porescale_gb300.springs import batch_solve
+
+    def ind_s(v):
+        ind = inds[v]
+        incl = geometry.inclusions(ind.shape, 0.25, 3.0, specs[v]["seed"] + 7)
+        return np.where(ind == 0, np.where(incl == 3, 3, 0), 1).astype(np.int32)
+
+    t0 = time.perf_counter()
+    moduli = [{} for _ in lats]
+    for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
+        nets = []
+        for v in range(len(lats)):
+            N = SpringNetwork(ind_s(v), 1.0, 0.4, 0.3, 0.1, 1e-3 * inds[v].shape[2] / 2, load, LSM_MIXED)
+            N.set_wall_load(lats[v], 1.0)
+            nets.append(N)
+        try:
+            for v, r in enumerate(batch_solve(nets, 1e-8, 400000)):
+                moduli[v][name] = r.modulus
+        except PorescaleError as exc:
+            for v in range(len(lats)):
+                moduli[v][name + "_error"] = str(exc)
+        for N in nets:
+            N.close()
+    t_lsm = time.perf_counter() - t0
+    # the same solves one network at a time on 8 host threads, for comparison
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(8) as ex:
-        moduli = list(ex.map(lsm_job, range(len(lats))))
-    t_lsm = time.perf_counter() - t0
+        moduli_ind = list(ex.map(lsm_job, range(len(lats))))
+    t_lsm_ind = time.perf_counter() - t0
+    agree = max((abs(a[k] - b[k]) / abs(b[k]) for a, b in zip(moduli, moduli_ind) for k in ("Cxxxx", "Cyzyz")
+                 if a.get(k) and b.get(k)), default=None)
     # plain per-volume FP64 path on the first few subvolumes: time and errors
     nref = min(args.batch_reference, len(lats))
     ref = []
@@ -433,11 +470,13 @@ def batch_mode(args):
     out = {"mode": "batch", "volumes": len(lats), "steps": T, "precision": args.prec, "fluid_nodes": nodes,
            "tile": list(tile), "lbm_seconds": ms * 1e-3, "lbm_wall_seconds": t_lbm, "mlups": mlups,
            "achieved_gbs": mlups * 1e6 * bpn / 1e9, "frac": mlups * 1e6 * bpn / 1e9 / peak, "peak_kind": peak_kind,
-           "lsm_seconds": t_lsm, "subvolumes_per_s": len(lats) / (ms * 1e-3 + t_lsm),
+           "lsm_seconds": t_lsm, "lsm_individual_seconds": t_lsm_ind, "lsm_batch_vs_individual_max_rel": agree,
+           "subvolumes_per_s": len(lats) / (ms * 1e-3 + t_lsm),
            "lbm_subvolumes_per_s": len(lats) / (ms * 1e-3),
            "f64_plain_mlups": f64_mlups,
            "f64_plain_subvolumes_per_s_estimate": (f64_mlups * 1e6 / (nodes * T / len(lats))) if f64_mlups else None,
-           "reference_volumes": ref, "moduli": moduli[:8], "specs": specs}
+           "lsm_failures": sum(1 for m in moduli for k in m if k.endswith("_error")),
+           "reference_volumes": ref, "moduli": moduli, "specs": specs}
     for L in lats:
         L.close()
     print(json.dumps(out))
@@ -559,6 +598,28 @@ def main():
         mlups = nl * steps / t / 1e6 * world
         launch_s = t / steps
         achieved = nl * ALGO_BYTES[q] / launch_s / 1e9
+        if q != "f64" and not args.no_autotune:
+            # the step schedules side by side on this workload (fused: slab
+            # planes x look-ahead), each from the same state
+            study = {}
+            tile = (L.info.tile_x, L.info.tile_y, L.info.occupancy, int(L.info.schedule))
+            for planes, ahead in ((0, 1), (1, 1), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2)):
+                try:
+                    L.set_fused(0, 1)
+                    L.set_tile(128, 256, 0)
+                    L.set_fused(planes, ahead)
+                except Exception as exc:  # configuration without a fused form
+                    study[f"{planes}/{ahead}"] = str(exc)
+                    continue
+                L.set_state(fr, fb)
+                study[f"{planes}/{ahead}"] = nl * 20 / time_steps(L, 20, 3, torch) / 1e6
+            L.set_fused(0, 1)
+            L.set_tile(*tile[:3])
+            if tile[3]:
+                L.set_fused(tile[3] % 256, tile[3] // 256)
+            L.set_state(fr, fb)
+            L.info = L.get_info()
+            res[q + "_schedules_mlups"] = study
         sched = int(L.info.schedule)
         res[q] = {"mlups": mlups, "ms_per_step": launch_s * 1e3, "steps": steps, "achieved_gbs": achieved,
                   "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.occupancy],
@@ -623,6 +684,7 @@ def main():
         "gpu_launches": h["steps"] * h["kernels_per_step"],
         "clocks": clocks,
         "legs": {q: res[q] for q in legs},
+        "schedules_mlups": {k[:-len("_schedules_mlups")]: v for k, v in res.items() if k.endswith("_schedules_mlups")},
         "lsm": lsm,
     }
     if "f64" in res:

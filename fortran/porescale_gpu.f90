@@ -168,6 +168,14 @@ module porescale_gpu
       integer(c_int32_t), value :: maxit
       type(ps_lsm_result), intent(out) :: res
     end function
+    ! several networks solved by shared launches (handles(n) from ps_lsm_create)
+    integer(c_int) function ps_lsm_batch_solve(handles, n, rtol, maxit, res) bind(c, name='ps_lsm_batch_solve')
+      import :: c_int, c_int32_t, c_double, c_ptr, ps_lsm_result
+      type(c_ptr), intent(in) :: handles(*)
+      integer(c_int32_t), value :: n, maxit
+      real(c_double), value :: rtol
+      type(ps_lsm_result), intent(out) :: res(*)
+    end function
     integer(c_int) function ps_lsm_get_disp(handle, u) bind(c, name='ps_lsm_get_disp')
       import :: c_int, c_double, c_ptr
       type(c_ptr), value :: handle

@@ -202,6 +202,14 @@ int ps_lsm_get_info(void *handle, ps_lsm_info *out);
  * XX:1628-1997.  Returns PS_ERR_NOTCONV (result still filled) when the
  * tolerance is not reached within maxit working-precision iterations. */
 int ps_lsm_solve(void *handle, double rtol, int32_t maxit, ps_lsm_result *out);
+/* Several networks solved together (extension): every CG kernel runs once
+ * per iteration for all of them (tile lists over their nodes, per-network
+ * scalars, a converged network stops moving), 16 iterations per captured
+ * CUDA graph.  Same precision for all (PS_LSM_F64: one batched FP64 CG;
+ * PS_LSM_MIXED: FP64 refinement rounds around a batched FP32 CG).  out[n]
+ * as ps_lsm_solve's; PS_ERR_NOTCONV names the first network above rtol.
+ * At most 64 networks. */
+int ps_lsm_batch_solve(void *const *handles, int32_t n, double rtol, int32_t maxit, ps_lsm_result *out);
 /* Displacements (3, ns) in the reference node order (k-j-i over the padded
  * grid, duplicate plane included, as LSM_displ_field) after a solve. */
 int ps_lsm_get_disp(void *handle, double *u);

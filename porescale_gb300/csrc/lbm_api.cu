@@ -80,6 +80,7 @@ struct Lattice {
     g.ny = ny;
     g.nz = nz;
     g.nwords = nwords;
+    g.cplane = cplane();
     g.nvox = nvox;
     g.nl = nl;
     g.pitch = pitch;
@@ -110,6 +111,8 @@ struct Lattice {
     return a;
   }
   size_t elem() const { return prec == 0 ? 8 : (prec == 1 ? 4 : 2); }
+  // plane stride of the step colour field: whole 128-byte lines per plane
+  int cplane() const { return (nx * ny + 31) / 32 * 32; }
 };
 
 template <typename T>
@@ -698,14 +701,15 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   // by every step before they are read
   {
     const size_t cs = precision == 0 ? sizeof(double) : sizeof(float);
-    if (int r = dalloc(L.get(), (char**)&L->d_col, cs * nv)) return r;
+    const size_t nc = (size_t)L->cplane() * L->nz;  // padded planes
+    if (int r = dalloc(L.get(), (char**)&L->d_col, cs * nc)) return r;
     if (precision == 0) {
-      std::vector<double> w(nv, p->wet);
-      PS_CUDA(cudaMemcpyAsync(L->d_col, w.data(), cs * nv, cudaMemcpyHostToDevice, L->stream));
+      std::vector<double> w(nc, p->wet);
+      PS_CUDA(cudaMemcpyAsync(L->d_col, w.data(), cs * nc, cudaMemcpyHostToDevice, L->stream));
       PS_CUDA(cudaStreamSynchronize(L->stream));
     } else {
-      std::vector<float> w(nv, (float)p->wet);
-      PS_CUDA(cudaMemcpyAsync(L->d_col, w.data(), cs * nv, cudaMemcpyHostToDevice, L->stream));
+      std::vector<float> w(nc, (float)p->wet);
+      PS_CUDA(cudaMemcpyAsync(L->d_col, w.data(), cs * nc, cudaMemcpyHostToDevice, L->stream));
       PS_CUDA(cudaStreamSynchronize(L->stream));
     }
   }
@@ -1180,6 +1184,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   if (L->prec >= 1) {
     PS_CUDA(cudaMalloc((void**)&saver, rhob));
     PS_CUDA(cudaMemcpyAsync(saver, L->d_rho[L->cur], rhob, cudaMemcpyDeviceToDevice, L->stream));
+
   }
   struct Cfg {
     int tx, ty, zc, planes, ahead;

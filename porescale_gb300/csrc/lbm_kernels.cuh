@@ -87,6 +87,7 @@ constexpr int kCoordBits = 10;  // coord packing: x, y in 10 bits, z in 12
 
 struct GeomDev {
   int nx, ny, nz, nwords;  // box; 32-voxel words per row
+  int cplane;              // plane stride of the step colour field (nx*ny rounded up to 32)
   long long nvox;
   long long nl;            // fluid nodes
   long long pitch;         // elements per direction array (>= nl)
@@ -101,7 +102,7 @@ struct GeomDev {
 // (red, blue) FP32 reference densities (16-bit storage only)
 struct BufDev {
   void* pop;
-  float2* rho;
+  float2* rho;  // (red, blue) reference densities (deviation storage)
 };
 
 // ---- storage policies ----------------------------------------------------
@@ -397,7 +398,7 @@ __device__ __forceinline__ void unpack(uint32_t c, int& x, int& y, int& z)
 struct NbOff {
   int x[3], y[3], z[3];
 };
-__device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int nz)
+__device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int zs, int nz)
 {
   NbOff o;
   o.x[0] = (m & (1u << (kWrapShift + 0))) ? nx - 1 : -1;
@@ -406,9 +407,9 @@ __device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int nz)
   o.y[0] = (m & (1u << (kWrapShift + 2))) ? nxy - nx : -nx;
   o.y[1] = 0;
   o.y[2] = (m & (1u << (kWrapShift + 3))) ? nx - nxy : nx;
-  o.z[0] = (m & (1u << (kWrapShift + 4))) ? (nz - 1) * nxy : -nxy;
+  o.z[0] = (m & (1u << (kWrapShift + 4))) ? (nz - 1) * zs : -zs;
   o.z[1] = 0;
-  o.z[2] = (m & (1u << (kWrapShift + 5))) ? (1 - nz) * nxy : nxy;
+  o.z[2] = (m & (1u << (kWrapShift + 5))) ? (1 - nz) * zs : zs;
   return o;
 }
 
@@ -442,7 +443,7 @@ __device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R
   }
   int x, y, z;
   unpack(__ldg(G.coord + i), x, y, z);
-  cc[x + G.nx * (y + G.ny * z)] = stencil_colour(rr, rb, K.wet);
+  cc[x + G.nx * y + G.cplane * z] = stencil_colour(rr, rb, K.wet);
 }
 
 // collision, CSF force, recolouring of fluid node i; pushes the
@@ -458,17 +459,18 @@ __device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R
   const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
   int x, y, z;
   unpack(c, x, y, z);
-  const int nxy = G.nx * G.ny;
-  const int v = x + G.nx * y + nxy * z;
-  const NbOff o = nb_offsets(m, G.nx, nxy, G.nz);
-  auto col = [&](int a, int b, int e) -> R {
-    const R* p = cc + (v + o.x[a] + o.y[b] + o.z[e]);
-    if constexpr (kCoh)
-      return __ldcg(p);
-    else
-      return *p;
-  };
-  if constexpr (Store<PREC>::kDev) {
+  const int v = x + G.nx * y + G.cplane * z;
+  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.cplane, G.nz);
+  // plain (L1-cached) loads also in the fused schedule: every colour plane
+  // starts on a 128-byte line, and a collide tile reads only planes whose
+  // density tiles have all completed, so no line it caches is written later
+  // in the launch
+  auto col = [&](int a, int b, int e) -> R { return cc[v + o.x[a] + o.y[b] + o.z[e]]; };
+  // FP32 storage: shifted arithmetic on the deviations (the storage is
+  // precise enough for it to matter).  16-bit storage: its rounding (~1e-3
+  // relative on the deviations) dominates either way, so the full-value
+  // form, ~10% fewer instructions, is used.
+  if constexpr (PREC == 1) {
     float gr[19], gb[19], Zr[19], Zb[19], Sr, Sb;
     const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
     const float2 rn = ld_step(dst.rho + i, kCoh);  // this step's densities (density pass)
@@ -558,19 +560,21 @@ __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
 // The fluid nodes are cut into z-slabs; a work list holds the density tiles
 // of every slab and the collide tiles of every slab, ordered so that the
 // collide tiles of slab k follow the density tiles of slabs k-1, k, k+1
-// (periodic).  CTAs take items in list order from a ticket counter; a
-// density tile publishes its completion on its slab's counter, and a
-// collide tile first waits (bounded) for the three counters it needs.  A
-// CTA only waits for items handed out before its own, to CTAs already
-// running, so the waits end.  The collide tiles re-read populations that
-// the density tiles of the same slab read shortly before (L2 hits), and
+// (periodic).  CTA b takes items b, b + G, b + 2G, ... of the list (G the
+// grid, launched cooperatively so that every CTA is resident); a density
+// tile publishes its completion on its slab's counter, and a collide tile
+// first waits (bounded) for the three counters it needs.  Every item waits
+// only for items earlier in the list, each held by a resident CTA that has
+// finished its own earlier items, so the lowest unfinished item can always
+// proceed and the waits end.  The collide tiles re-read populations that the
+// density tiles of the same slab read shortly before (L2 hits), and
 // memory-bound density work overlaps compute-bound collide work.
 struct FusedArgs {
   const int4* items;     // x = kind (0 density, 1 collide) | slab << 1, y = first node, z = end node
   int nitems;
   int nslab;
   const int* ntd;        // density tiles per slab
-  unsigned int* ctr;     // [0] ticket, [1 + s] completed density tiles of slab s (zeroed before the launch)
+  unsigned int* ctr;     // [1 + s] completed density tiles of slab s (zeroed before the launch)
   int* err;              // set to 1 when a wait gave up
 };
 constexpr unsigned kFusedSpinLimit = 1u << 22;
@@ -587,13 +591,7 @@ __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
     k_lbm_fused(const __grid_constant__ LbmConst<typename Store<PREC>::R> K, const __grid_constant__ GeomDev G,
                 const BufDev src, const BufDev dst, typename Store<PREC>::R* __restrict__ cc, const FusedArgs F)
 {
-  __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = (int)atomicAdd(F.ctr, 1u);
-    __syncthreads();
-    const int it = s_item;
-    __syncthreads();
-    if (it >= F.nitems) break;
+  for (int it = blockIdx.x; it < F.nitems; it += gridDim.x) {
     const int4 w = __ldg(F.items + it);
     const int slab = w.x >> 1;
     const int i = w.y + threadIdx.x;
@@ -615,10 +613,9 @@ __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
               ok = false;
               break;
             }
-            __nanosleep(64);
+            __nanosleep(32);
           }
         }
-        __threadfence();
       }
       __syncthreads();
       if (i < w.z) coll_node<PREC, true>(K, G, src, dst, cc, i);
@@ -769,7 +766,7 @@ __global__ void __launch_bounds__(256) k_lbm_obs(const __grid_constant__ LbmCons
     }
     const int nxy = G.nx * G.ny;
     const int v = x + G.nx * y + nxy * z;
-    const NbOff o = nb_offsets(m, G.nx, nxy, G.nz);
+    const NbOff o = nb_offsets(m, G.nx, nxy, nxy, G.nz);
     auto ccf = [&](int a, int b, int c) -> double { return cc[v + o.x[a] + o.y[b] + o.z[c]]; };
     double n[3], Fs[3];
     csf_force(D, ccf, n, Fs);

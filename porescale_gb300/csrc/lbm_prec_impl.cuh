@@ -51,12 +51,21 @@ cudaError_t step_fused_blk(const LbmLaunchArgs& a, const FusedArgs& f)
 {
   using R = typename Store<PREC>::R;
   if (f.nitems == 0) return cudaSuccess;
+  // every CTA resident: the cooperative launch refuses a larger grid
   static const int gmax = persistent_grid(k_lbm_fused<PREC, BLK, MINB>, BLK);
   cudaError_t e = cudaMemsetAsync(f.ctr, 0, sizeof(unsigned) * (size_t)(1 + f.nslab), a.stream);
   if (e != cudaSuccess) return e;
-  k_lbm_fused<PREC, BLK, MINB><<<std::min(gmax, f.nitems), BLK, 0, a.stream>>>(
-      *static_cast<const LbmConst<R>*>(a.K), a.G, a.src, a.dst, static_cast<R*>(a.cc), f);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)std::min(gmax, f.nitems));
+  cfg.blockDim = dim3(BLK);
+  cfg.stream = a.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_lbm_fused<PREC, BLK, MINB>, *static_cast<const LbmConst<R>*>(a.K), a.G, a.src,
+                            a.dst, static_cast<R*>(a.cc), f);
 }
 
 template <int PREC>

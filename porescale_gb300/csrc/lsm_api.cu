@@ -425,6 +425,136 @@ __global__ void __launch_bounds__(256) k_beta_surface(const LsmGeom G, const int
   }
 }
 
+// right-hand side of the tied system (imposed jump plus any wall load),
+// without its translation component; |b|^2 to *bb; x = 0
+int prepare(Springs* S, double* bb)
+{
+  const int nv = S->nvox, n3 = 3 * nv;
+  const int nb = blocks_for(nv), nb3 = blocks_for(n3);
+  lsm::k_lsm_rhs<<<nb, kBlk, 0, S->stream>>>(S->geom(), S->pa, S->jc, 2.0 * S->p.gstrain, S->b);
+  PS_CUDA(cudaGetLastError());
+  if (S->has_load) {  // fluid wall load; its net force is removed with the mean below
+    k_add<<<nb3, kBlk, 0, S->stream>>>(n3, S->fext, S->b);
+    PS_CUDA(cudaGetLastError());
+  }
+  if (int e = project_mean(S, S->b)) return e;
+  k_sq_norm<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->part);
+  if (int e = sum_parts(S, nb3, S->scal + 17)) return e;
+  PS_CUDA(cudaMemcpyAsync(bb, S->scal + 17, sizeof(double), cudaMemcpyDeviceToHost, S->stream));
+  PS_CUDA(cudaMemsetAsync(S->x, 0, sizeof(double) * n3, S->stream));
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  return PS_OK;
+}
+
+// true FP64 residual, stress and modulus of the current solution into *out
+int finish(Springs* S, double bb, double rtol, ps_lsm_result* out)
+{
+  double rn2 = 0.0;
+  if (int e = residual(S, &rn2)) return e;
+  const double rel = bb > 0.0 ? std::sqrt(rn2 / bb) : 0.0;
+  out->relres = rel;
+  out->converged = rel <= rtol * 1.0000001 ? 1 : 0;
+  out->nnode = S->nnode;
+  out->ncube = S->ncube;
+  if (int e = compute_stress(S, out)) return e;
+  S->solved = true;
+  S->last = *out;
+  return PS_OK;
+}
+
+// ---- batched CG over several networks ---------------------------------------
+// CG on A x = r0 (x = 0, p = r0 set by the caller) for every network of the
+// list at once: the iteration of cg<T> with each kernel launched once for
+// all networks (tile lists over their nodes / elements), 16 iterations per
+// captured graph, until every network has converged or maxit is reached.
+template <typename T>
+int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cudaStream_t st)
+{
+  const int n = (int)sys.size();
+  lsm::LsmTable tab;
+  memset(&tab, 0, sizeof tab);
+  tab.n = n;
+  std::vector<int2> t1, t3;
+  for (int s = 0; s < n; s++) {
+    Springs* S = sys[s];
+    lsm::LsmSys& d = tab.s[s];
+    d.G = S->geom();
+    if (sizeof(T) == 8) {
+      d.x = S->x;
+      d.r = S->r;
+      d.p = S->p64;
+      d.q = S->q64;
+    } else {
+      d.x = S->x32;
+      d.r = S->r32;
+      d.p = S->p32;
+      d.q = S->q32;
+    }
+    d.part = S->part;
+    d.scal = S->scal;
+    d.n3 = 3 * S->nvox;
+    d.nt1 = blocks_for(S->nvox);
+    d.nt3 = blocks_for(d.n3);
+    for (int b = 0; b < d.nt1; b++) t1.push_back(make_int2(s, b * kBlk));
+    for (int b = 0; b < d.nt3; b++) t3.push_back(make_int2(s, b * kBlk));
+    // |r0|^2 into scal[0] on the network's own stream
+    lsm::k_sq_norm_t<T, kBlk><<<d.nt3, kBlk, 0, S->stream>>>(d.n3, static_cast<const T*>(d.r), S->part);
+    if (int e = sum_parts(S, d.nt3, S->scal)) return e;
+    PS_CUDA(cudaStreamSynchronize(S->stream));
+  }
+  int2 *d1 = nullptr, *d3 = nullptr;
+  double* ddone = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  auto release = [&]() {
+    cudaFree(d1);
+    cudaFree(d3);
+    cudaFree(ddone);
+    if (exec) cudaGraphExecDestroy(exec);
+  };
+  auto run = [&]() -> int {
+    PS_CUDA(cudaMalloc((void**)&d1, sizeof(int2) * t1.size()));
+    PS_CUDA(cudaMalloc((void**)&d3, sizeof(int2) * t3.size()));
+    PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * n));
+    PS_CUDA(cudaMemcpyAsync(d1, t1.data(), sizeof(int2) * t1.size(), cudaMemcpyHostToDevice, st));
+    PS_CUDA(cudaMemcpyAsync(d3, t3.data(), sizeof(int2) * t3.size(), cudaMemcpyHostToDevice, st));
+    lsm::k_cg_init_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab);
+    PS_CUDA(cudaGetLastError());
+    const double tol2 = tol * tol;
+    const int batch = 16;
+    cudaGraph_t graph = nullptr;
+    PS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < batch; k++) {
+      lsm::k_lsm_matvec_batch<T, kBlk><<<(unsigned)t1.size(), kBlk, 0, st>>>(tab, d1);
+      lsm::k_sum_batch<<<n, 1024, 0, st>>>(tab, 1, 1);
+      lsm::k_cg_alpha_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, tol2);
+      lsm::k_cg_xr_batch<T, kBlk><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
+      lsm::k_sum_batch<<<n, 1024, 0, st>>>(tab, 4, 0);
+      lsm::k_cg_beta_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab);
+      lsm::k_cg_p_batch<T><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
+    }
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "batched CG capture");
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "batched CG instantiate");
+    std::vector<double> done((size_t)n, 0.0);
+    for (long long it = 0; it < maxit; it += batch) {
+      PS_CUDA(cudaGraphLaunch(exec, st));
+      lsm::k_cg_done_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, ddone);
+      PS_CUDA(cudaMemcpyAsync(done.data(), ddone, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+      PS_CUDA(cudaStreamSynchronize(st));
+      bool all = true;
+      for (double v : done) all = all && v > 0.0;
+      if (all) break;
+    }
+    return PS_OK;
+  };
+  const int r = run();
+  cudaStreamSynchronize(st);
+  release();
+  return r;
+}
+
 }  // namespace
 }  // namespace ps
 
@@ -555,23 +685,10 @@ int ps_lsm_solve(void* h, double rtol, int32_t maxit, ps_lsm_result* out)
   if (!(rtol > 0.0) || maxit < 1) return fail(PS_ERR_ARG, "ps_lsm_solve: need rtol > 0 and maxit >= 1");
   Springs* S = static_cast<Springs*>(h);
   memset(out, 0, sizeof *out);
-  const int nv = S->nvox, n3 = 3 * nv;
-  const int nb = blocks_for(nv), nb3 = blocks_for(n3);
-  const LsmGeom G = S->geom();
-  // right-hand side of the tied system, without its translation component
-  lsm::k_lsm_rhs<<<nb, kBlk, 0, S->stream>>>(G, S->pa, S->jc, 2.0 * S->p.gstrain, S->b);
-  PS_CUDA(cudaGetLastError());
-  if (S->has_load) {  // fluid wall load; its net force is removed with the mean below
-    k_add<<<nb3, kBlk, 0, S->stream>>>(n3, S->fext, S->b);
-    PS_CUDA(cudaGetLastError());
-  }
-  if (int e = project_mean(S, S->b)) return e;
-  k_sq_norm<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->part);
-  if (int e = sum_parts(S, nb3, S->scal + 17)) return e;
+  const int n3 = 3 * S->nvox;
+  const int nb3 = blocks_for(n3);
   double bb = 0.0;
-  PS_CUDA(cudaMemcpyAsync(&bb, S->scal + 17, sizeof(double), cudaMemcpyDeviceToHost, S->stream));
-  PS_CUDA(cudaMemsetAsync(S->x, 0, sizeof(double) * n3, S->stream));
-  PS_CUDA(cudaStreamSynchronize(S->stream));
+  if (int e = prepare(S, &bb)) return e;
   long long iters = 0, inner = 0;
   double rel = 0.0;
   int refinements = 0;
@@ -607,20 +724,11 @@ int ps_lsm_solve(void* h, double rtol, int32_t maxit, ps_lsm_result* out)
       iters++;
     }
   }
-  // true FP64 residual of the final solution
-  double rn2 = 0.0;
-  if (int e = residual(S, &rn2)) return e;
-  rel = bb > 0.0 ? std::sqrt(rn2 / bb) : 0.0;
   out->iterations = iters;
   out->inner_iterations = inner;
   out->refinements = refinements;
-  out->relres = rel;
-  out->converged = rel <= rtol * 1.0000001 ? 1 : 0;
-  out->nnode = S->nnode;
-  out->ncube = S->ncube;
-  if (int e = compute_stress(S, out)) return e;
-  S->solved = true;
-  S->last = *out;
+  if (int e = finish(S, bb, rtol, out)) return e;
+  rel = out->relres;
   return out->converged ? PS_OK : fail(PS_ERR_NOTCONV, "ps_lsm_solve: relative residual %.3e above %.3e", rel, rtol);
 }
 
@@ -729,6 +837,104 @@ int ps_lsm_alpha_beta(void* h, const int32_t* lab, int32_t npores, int32_t iipor
   cudaFreeAsync(d_lab, S->stream);
   cudaStreamSynchronize(S->stream);
   return rc;
+}
+
+int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t maxit, ps_lsm_result* out)
+{
+  if (!handles || !out) return fail(PS_ERR_ARG, "ps_lsm_batch_solve: null argument");
+  if (n < 1 || n > lsm::kLsmBatchMax) return fail(PS_ERR_ARG, "ps_lsm_batch_solve: %d networks (1..%d)", n, lsm::kLsmBatchMax);
+  if (!(rtol > 0.0) || maxit < 1) return fail(PS_ERR_ARG, "ps_lsm_batch_solve: need rtol > 0 and maxit >= 1");
+  std::vector<Springs*> sys;
+  for (int s = 0; s < n; s++) {
+    if (!handles[s]) return fail(PS_ERR_ARG, "ps_lsm_batch_solve: network %d is null", s);
+    Springs* S = static_cast<Springs*>(handles[s]);
+    for (Springs* o : sys)
+      if (o == S) return fail(PS_ERR_ARG, "ps_lsm_batch_solve: network %d appears twice", s);
+    if (S->p.precision != static_cast<Springs*>(handles[0])->p.precision)
+      return fail(PS_ERR_ARG, "ps_lsm_batch_solve: networks differ in precision");
+    sys.push_back(S);
+    memset(out + s, 0, sizeof(ps_lsm_result));
+  }
+  std::vector<double> bb((size_t)n, 0.0);
+  for (int s = 0; s < n; s++)
+    if (int e = prepare(sys[s], &bb[s])) return e;
+  cudaStream_t st = nullptr;
+  PS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = PS_OK;
+  if (sys[0]->p.precision == PS_LSM_F64) {
+    for (int s = 0; s < n && rc == PS_OK; s++) {
+      Springs* S = sys[s];
+      const size_t b3 = sizeof(double) * 3 * (size_t)S->nvox;
+      cudaError_t e = cudaMemcpyAsync(S->r, S->b, b3, cudaMemcpyDeviceToDevice, S->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(S->p64, S->b, b3, cudaMemcpyDeviceToDevice, S->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
+    }
+    if (rc == PS_OK) rc = batch_cg<double>(sys, rtol, maxit, st);
+    for (int s = 0; s < n && rc == PS_OK; s++) {
+      double h8[8];
+      if ((rc = read_scal(sys[s], h8, 8))) break;
+      out[s].iterations = out[s].inner_iterations = (long long)h8[7];
+    }
+  } else {
+    // FP64 refinement rounds around one batched FP32 CG per round over the
+    // networks that have not reached rtol
+    std::vector<int> rounds((size_t)n, 0);
+    long long budget = maxit;
+    for (int round = 0; round < 60 && rc == PS_OK && budget > 0; round++) {
+      std::vector<Springs*> act;
+      std::vector<double> rns;
+      for (int s = 0; s < n && rc == PS_OK; s++) {
+        Springs* S = sys[s];
+        const int n3 = 3 * S->nvox;
+        double rn2 = 0.0;
+        if (round == 0) {
+          cudaError_t e = cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream);
+          if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
+          rn2 = bb[s];
+        } else if ((rc = residual(S, &rn2))) {
+          break;
+        }
+        if (!(bb[s] > 0.0) || rn2 <= rtol * rtol * bb[s]) continue;
+        const double rn = std::sqrt(rn2);
+        k_ir_start<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, 1.0 / rn, S->r, S->r32, S->p32, S->x32);
+        cudaError_t e = cudaStreamSynchronize(S->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
+        act.push_back(S);
+        rns.push_back(rn);
+        rounds[s]++;
+      }
+      if (rc != PS_OK || act.empty()) break;
+      if ((rc = batch_cg<float>(act, 1e-4, budget, st))) break;
+      long long most = 0;
+      for (size_t a = 0; a < act.size() && rc == PS_OK; a++) {
+        Springs* S = act[a];
+        double h8[8];
+        if ((rc = read_scal(S, h8, 8))) break;
+        const long long it = (long long)h8[7];
+        most = std::max(most, it);
+        const int si = (int)(std::find(sys.begin(), sys.end(), S) - sys.begin());
+        out[si].inner_iterations += it;
+        out[si].iterations++;
+        const int n3 = 3 * S->nvox;
+        k_ir_update<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, rns[a], S->x32, S->x);
+        cudaError_t e = cudaStreamSynchronize(S->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
+      }
+      budget -= most;
+    }
+    for (int s = 0; s < n; s++) out[s].refinements = rounds[s];
+  }
+  cudaStreamDestroy(st);
+  if (rc != PS_OK) return rc;
+  int bad = -1;
+  for (int s = 0; s < n; s++) {
+    if (int e = finish(sys[s], bb[s], rtol, out + s)) return e;
+    if (!out[s].converged && bad < 0) bad = s;
+  }
+  return bad < 0 ? PS_OK
+                 : fail(PS_ERR_NOTCONV, "ps_lsm_batch_solve: network %d at relative residual %.3e above %.3e", bad,
+                        out[bad].relres, rtol);
 }
 
 int ps_lsm_get_disp(void* h, double* u)

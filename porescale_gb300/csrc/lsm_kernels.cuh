@@ -39,15 +39,12 @@ __device__ __forceinline__ float kval<float>(const LsmGeom& G, int m, int r, int
 
 __device__ __forceinline__ int wrap_add(int c, int d, int n) { return c + d < 0 ? c + d + n : (c + d >= n ? c + d - n : c + d); }
 
-// q = A p on every node, with the FP64 partial sums of p.q per block
-// (dot[blockIdx]).  T = storage / arithmetic type of p and q.
-template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __restrict__ p, T* __restrict__ q,
-                                                    double* __restrict__ dot)
+// (A p) at node v, written to q; returns p_v . (A p)_v in FP64
+template <typename T>
+__device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v)
 {
-  const int v = blockIdx.x * BLK + threadIdx.x;
   double pq = 0.0;
-  if (v < G.nvox) {
+  {
     const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
     const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
     T acc[3] = {T(0), T(0), T(0)};
@@ -79,16 +76,33 @@ __global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __
     q[nv + v] = acc[1];
     q[2 * nv + v] = acc[2];
   }
-  // block sum of p.q
+  return pq;
+}
+
+// FP64 sum of one value per thread over the CTA, stored by thread 0 to *out
+template <int BLK>
+__device__ __forceinline__ void block_sum_to(double t, double* out)
+{
   __shared__ double red[BLK / 32];
-  for (int o = 16; o > 0; o >>= 1) pq += __shfl_xor_sync(0xffffffffu, pq, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = pq;
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < BLK / 32; w++) s += red[w];
-    dot[blockIdx.x] = s;
+    *out = s;
   }
+}
+
+// q = A p on every node, with the FP64 partial sums of p.q per block
+// (dot[blockIdx]).  T = storage / arithmetic type of p and q.
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __restrict__ p, T* __restrict__ q,
+                                                    double* __restrict__ dot)
+{
+  const int v = blockIdx.x * BLK + threadIdx.x;
+  const double pq = v < G.nvox ? matvec_node<T>(G, p, q, v) : 0.0;
+  block_sum_to<BLK>(pq, dot + blockIdx.x);
 }
 
 // b = -sum over cubes of K * (jump of the cube's corners): the right-hand
@@ -308,6 +322,130 @@ __global__ void k_cg_p(int n3, const double* __restrict__ scal, const T* __restr
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n3 || scal[6] > 0.0) return;
   p[i] = r[i] + (T)scal[3] * p[i];
+}
+
+// ---- batched CG: many networks advanced by the same launches ------------
+// The descriptor table (kernel parameter) holds each network's geometry,
+// CG vectors, partial-sum buffer and scalar block; tiles list (network,
+// first element) for the node-wise matvec and the element-wise vector
+// kernels.  Every network runs the single-network iteration above on its
+// own scalars: a converged network gets alpha = 0 and stops moving.
+constexpr int kLsmBatchMax = 64;
+struct LsmSys {
+  LsmGeom G;
+  void *x, *r, *p, *q;
+  double* part;   // per-tile partial sums
+  double* scal;   // CG scalars (layout of k_cg_alpha)
+  int n3, nt1, nt3;  // 3 nvox, node tiles, element tiles
+};
+struct LsmTable {
+  LsmSys s[kLsmBatchMax];
+  int n;
+};
+
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_lsm_matvec_batch(const __grid_constant__ LsmTable B,
+                                                          const int2* __restrict__ tiles)
+{
+  const int2 tl = __ldg(tiles + blockIdx.x);
+  const LsmSys& S = B.s[tl.x];
+  if (S.scal[6] > 0.0) return;  // converged network: nothing moves (whole CTA)
+  const int v = tl.y + threadIdx.x;
+  const double pq =
+      v < S.G.nvox ? matvec_node<T>(S.G, static_cast<const T*>(S.p), static_cast<T*>(S.q), v) : 0.0;
+  block_sum_to<BLK>(pq, S.part + tl.y / BLK);
+}
+
+// scal[which] = sum of the network's first n partials (n = nt1 or nt3)
+__global__ void k_sum_batch(const __grid_constant__ LsmTable B, int which, int node_tiles)
+{
+  const LsmSys& S = B.s[blockIdx.x];
+  if (S.scal[6] > 0.0) return;  // converged network: its scalars stay
+  const int n = node_tiles ? S.nt1 : S.nt3;
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += S.part[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) t += red[w];
+    S.scal[which] = t;
+  }
+}
+
+__global__ void k_cg_alpha_batch(const __grid_constant__ LsmTable B, double tol2)
+{
+  const int s = threadIdx.x;
+  if (s >= B.n) return;
+  double* scal = B.s[s].scal;
+  const double rr = scal[0], pq = scal[1];
+  const bool done = scal[6] > 0.0 || rr <= tol2 * scal[5] || !(pq > 0.0);
+  scal[6] = done ? 1.0 : 0.0;
+  scal[2] = done ? 0.0 : rr / pq;
+  if (!done) scal[7] += 1.0;
+}
+
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_cg_xr_batch(const __grid_constant__ LsmTable B,
+                                                     const int2* __restrict__ tiles)
+{
+  const int2 tl = __ldg(tiles + blockIdx.x);
+  const LsmSys& S = B.s[tl.x];
+  if (S.scal[6] > 0.0) return;  // converged network (alpha = 0): x, r unchanged
+  const int i = tl.y + threadIdx.x;
+  double rr = 0.0;
+  if (i < S.n3) {
+    const T al = (T)S.scal[2];
+    T* x = static_cast<T*>(S.x);
+    T* r = static_cast<T*>(S.r);
+    const T xi = x[i] + al * static_cast<const T*>(S.p)[i];
+    const T ri = r[i] - al * static_cast<const T*>(S.q)[i];
+    x[i] = xi;
+    r[i] = ri;
+    rr = (double)ri * (double)ri;
+  }
+  block_sum_to<BLK>(rr, S.part + tl.y / BLK);
+}
+
+__global__ void k_cg_beta_batch(const __grid_constant__ LsmTable B)
+{
+  const int s = threadIdx.x;
+  if (s >= B.n) return;
+  double* scal = B.s[s].scal;
+  const double rn = scal[4], ro = scal[0];
+  scal[3] = scal[6] > 0.0 || !(ro > 0.0) ? 0.0 : rn / ro;
+  if (scal[6] == 0.0) scal[0] = rn;
+}
+
+template <typename T>
+__global__ void k_cg_p_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles)
+{
+  const int2 tl = __ldg(tiles + blockIdx.x);
+  const LsmSys& S = B.s[tl.x];
+  const int i = tl.y + threadIdx.x;
+  if (i >= S.n3 || S.scal[6] > 0.0) return;
+  T* p = static_cast<T*>(S.p);
+  p[i] = static_cast<const T*>(S.r)[i] + (T)S.scal[3] * p[i];
+}
+
+// |r0|^2 (already in scal[0]) becomes the reference |b|^2 of the tolerance
+__global__ void k_cg_init_batch(const __grid_constant__ LsmTable B)
+{
+  const int s = threadIdx.x;
+  if (s >= B.n) return;
+  double* scal = B.s[s].scal;
+  scal[5] = scal[0];
+  scal[6] = 0.0;
+  scal[7] = 0.0;
+}
+
+// done flags of every network into out[s]
+__global__ void k_cg_done_batch(const __grid_constant__ LsmTable B, double* out)
+{
+  const int s = threadIdx.x;
+  if (s < B.n) out[s] = B.s[s].scal[6];
 }
 
 }  // namespace lsm

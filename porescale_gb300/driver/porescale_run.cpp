@@ -9,10 +9,15 @@
 // of itw steps, and after each block the iteration / iteration2 checkpoint
 // and the check_state record (check_state_19 and one output.m row).  The
 // lattice-spring half of the coupled program (lsm_step, calc_stress,
-// calc_ab) is not part of this driver.
+// calc_ab) is not part of this mode.
 //
-// Options: -p f64|f32|f16|bf16 (population storage, default f64, the
-// reference's arithmetic), -d DIR (run directory, default .), -q (quiet).
+// With -m xx or -m yz it is instead the lattice-spring program of
+// LSM2S/Cxxxx/XX_P.f or LSM2S/Cyzyz/YZ_P.f: their INPUT_PARAMETERS, the
+// static solve, and their output files (run_lsm below).
+//
+// Options: -m lbm|xx|yz (default lbm), -p f64|f32|f16|bf16 (population
+// storage, default f64, the reference's arithmetic) or f64|mixed (spring
+// solve), -d DIR (run directory, default .), -q (quiet).
 #include <sys/stat.h>
 
 #include <cmath>
@@ -136,21 +141,21 @@ void check_velocities()
 }
 
 // ind: one line per (j, k), k outer, a leading blank then ncx digits
-std::vector<int32_t> read_ind(const Input& in)
+std::vector<int32_t> read_ind(int ncx, int ncy, int ncz)
 {
   std::ifstream f(path("ind"));
   if (!f) die("ind not found in " + g_dir);
-  std::vector<int32_t> ind((size_t)in.ncx * in.ncy * in.ncz);
+  std::vector<int32_t> ind((size_t)ncx * ncy * ncz);
   std::string ln;
-  for (int k = 0; k < in.ncz; k++)
-    for (int j = 0; j < in.ncy; j++) {
+  for (int k = 0; k < ncz; k++)
+    for (int j = 0; j < ncy; j++) {
       if (!std::getline(f, ln)) die("ind has fewer than ncy*ncz lines");
       size_t p = ln.find_first_not_of(' ');
-      if (p == std::string::npos || ln.size() < p + (size_t)in.ncx) die("short line in ind");
-      for (int i = 0; i < in.ncx; i++) {
+      if (p == std::string::npos || ln.size() < p + (size_t)ncx) die("short line in ind");
+      for (int i = 0; i < ncx; i++) {
         const char c = ln[p + i];
         if (c < '0' || c > '9') die("non-digit in ind");
-        ind[(size_t)i + (size_t)in.ncx * (j + (size_t)in.ncy * k)] = c - '0';
+        ind[(size_t)i + (size_t)ncx * (j + (size_t)ncy * k)] = c - '0';
       }
     }
   return ind;
@@ -217,30 +222,223 @@ bool read_state(int& it1, std::vector<double>& fr, std::vector<double>& fb)
   return true;
 }
 
+// ---- the lattice-spring driver (LSM2S/Cxxxx/XX_P.f, LSM2S/Cyzyz/YZ_P.f) ----
+struct LsmInput {
+  int ncx, ncy, ncz;
+  double Em1, nu1, Em2, nu2, rs, dt, dl;
+  int itm, its;
+  double gstrain;
+  int nthread, icon;
+};
+
+// INPUT_PARAMETERS of XX_P.f / YZ_P.f: one value per line (XX:364-382)
+LsmInput read_lsm_input()
+{
+  std::ifstream f(path("INPUT_PARAMETERS"));
+  if (!f) die("INPUT_PARAMETERS not found in " + g_dir);
+  std::string ln;
+  auto one = [&]() {
+    if (!std::getline(f, ln)) die("INPUT_PARAMETERS ends early");
+    std::istringstream ss(ln);
+    std::string t;
+    if (!(ss >> t)) die("empty line in INPUT_PARAMETERS");
+    return fnum(t);
+  };
+  LsmInput in{};
+  in.ncx = (int)one();
+  in.ncy = (int)one();
+  in.ncz = (int)one();
+  in.Em1 = one();
+  in.nu1 = one();
+  in.Em2 = one();
+  in.nu2 = one();
+  in.rs = one();
+  in.dt = one();
+  in.dl = one();
+  in.itm = (int)one();
+  in.its = (int)one();
+  in.gstrain = one();
+  in.nthread = (int)one();
+  in.icon = (int)one();
+  return in;
+}
+
+// Static solve of the spring network with the imposed strain, then the
+// reference program's output files: lsm_settings (XX:1316-1346), the
+// LSM_coord / displ / velocity / force fields over the node grid (XX:1548-
+// 1575; the static equilibrium has zero velocities and, to the solver's
+// tolerance, zero net forces), iteration2 (positions, velocities,
+// accelerations, XX:1599-1609) and the stress_tensor record appended by
+// calc_stress (XX:1754, 1963-1994).
+int run_lsm(int load, int prec, bool quiet)
+{
+  const LsmInput in = read_lsm_input();
+  std::vector<int32_t> ind = read_ind(in.ncx, in.ncy, in.ncz);
+  ps_lsm_params p{};
+  // spring constants of the two solids (XX:411-414)
+  p.alf1 = in.dl * in.Em1 / (5.0 - 10.0 * in.nu1);
+  p.bet1 = in.dl * in.dl * in.dl * in.Em1 * (4 * in.nu1 - 1) / (20.0 * (2 * in.nu1 * in.nu1 + in.nu1 - 1));
+  p.alf2 = in.dl * in.Em2 / (5.0 - 10.0 * in.nu2);
+  p.bet2 = in.dl * in.dl * in.dl * in.Em2 * (4 * in.nu2 - 1) / (20.0 * (2 * in.nu2 * in.nu2 + in.nu2 - 1));
+  p.gstrain = in.gstrain;
+  p.load = load;
+  p.precision = prec;
+  void* h = nullptr;
+  check(ps_lsm_create(&p, ind.data(), in.ncx, in.ncy, in.ncz, &h), "ps_lsm_create");
+  ps_lsm_result r{};
+  check(ps_lsm_solve(h, 1e-10, 2000000000, &r), "ps_lsm_solve");
+  // reference node numbering: k-j-i over the node grid whose loaded axis has
+  // planes 1..N+1 (plane N+1 tied to plane 1); a node exists when one of
+  // its cubes is solid, no cube beyond the ends of the loaded axis
+  const int pa = load == PS_LOAD_XSTRETCH ? 0 : 1;
+  const int N[3] = {in.ncx, in.ncy, in.ncz};
+  int M[3] = {in.ncx, in.ncy, in.ncz};
+  M[pa] += 1;
+  auto solid = [&](int x, int y, int z) {
+    const int c[3] = {x, y, z};
+    int w[3];
+    for (int d = 0; d < 3; d++) {
+      if (d == pa && (c[d] < 0 || c[d] >= N[d])) return false;
+      w[d] = ((c[d] % N[d]) + N[d]) % N[d];
+    }
+    const int v = ind[(size_t)w[0] + (size_t)N[0] * (w[1] + (size_t)N[1] * w[2])];
+    return v == 0 || v == 3;
+  };
+  std::vector<long long> num((size_t)M[0] * M[1] * M[2], 0);
+  long long ns = 0;
+  for (int z = 0; z < M[2]; z++)
+    for (int y = 0; y < M[1]; y++)
+      for (int x = 0; x < M[0]; x++) {
+        bool e = false;
+        for (int q = 0; q < 8 && !e; q++) e = solid(x - (q & 1), y - ((q >> 1) & 1), z - (q >> 2));
+        if (e) num[(size_t)x + (size_t)M[0] * (y + (size_t)M[1] * z)] = ++ns;
+      }
+  std::vector<double> u((size_t)3 * ns);
+  check(ps_lsm_get_disp(h, u.data()), "ps_lsm_get_disp");
+  ps_lsm_info info{};
+  check(ps_lsm_get_info(h, &info), "ps_lsm_get_info");
+  {
+    FILE* f = std::fopen(path("lsm_settings").c_str(), "w");
+    std::fprintf(f, " Initial program settings\n Physical parameters\n");
+    std::fprintf(f, " Young modulus Em1 of component solid 1 = %.16E\n Poissons ratio nu1 = %.16E\n", in.Em1, in.nu1);
+    std::fprintf(f, " linear spring parameter alf = %.16E\n angular spring parameter bet = %.16E\n", p.alf1, p.bet1);
+    std::fprintf(f, " Young modulus Em1 of component solid 2 = %.16E\n Poissons ratio nu2 = %.16E\n", in.Em2, in.nu2);
+    std::fprintf(f, " linear spring parameter alf = %.16E\n angular spring parameter bet = %.16E\n", p.alf2, p.bet2);
+    std::fprintf(f, " solid medium density rs = %.16E\n integration time step dt = %.16E\n", in.rs, in.dt);
+    std::fprintf(f, " lattice unit step dl = %.16E\n Computational domain properties\n", in.dl);
+    std::fprintf(f, " x unit cell size ncx = %d\n y unit cell size ncy = %d\n z unit cell size ncz = %d\n", in.ncx,
+                 in.ncy, in.ncz);
+    std::fprintf(f, " number of solid points ns = %lld\n static solve: conjugate gradient, %s\n", ns,
+                 prec == PS_LSM_F64 ? "FP64" : "FP32 in FP64 refinement");
+    std::fprintf(f, " iterations = %lld\n relative residual = %.6E\n", (long long)r.inner_iterations, r.relres);
+    std::fclose(f);
+  }
+  {
+    FILE* fc = std::fopen(path("LSM_coord_field").c_str(), "w");
+    FILE* fd = std::fopen(path("LSM_displ_field").c_str(), "w");
+    FILE* fv = std::fopen(path("LSM_velocity_field").c_str(), "w");
+    FILE* ff = std::fopen(path("LSM_force_field").c_str(), "w");
+    for (int k = 1; k <= in.ncz; k++)
+      for (int j = 1; j <= in.ncy; j++)
+        for (int i = 1; i <= in.ncx; i++) {
+          const long long l = num[(size_t)(i - 1) + (size_t)M[0] * ((j - 1) + (size_t)M[1] * (k - 1))];
+          if (l) {
+            const double* ul = &u[(size_t)3 * (l - 1)];
+            std::fprintf(fc, " %24.16E %24.16E %24.16E\n", i + ul[0], j + ul[1], k + ul[2]);
+            std::fprintf(fd, " %24.16E %24.16E %24.16E\n", ul[0], ul[1], ul[2]);
+          } else {
+            std::fprintf(fc, " %12d %12d %12d\n", i, j, k);
+            std::fprintf(fd, " %24.16E %24.16E %24.16E\n", 0.0, 0.0, 0.0);
+          }
+          std::fprintf(fv, " %24.16E %24.16E %24.16E\n", 0.0, 0.0, 0.0);
+          std::fprintf(ff, " %24.16E %24.16E %24.16E\n", 0.0, 0.0, 0.0);
+        }
+    std::fclose(fc);
+    std::fclose(fd);
+    std::fclose(fv);
+    std::fclose(ff);
+  }
+  {  // iteration2: positions (node coordinates + displacement), velocities, accelerations
+    const std::string tmp = path("iteration2.tmp");
+    FILE* f = std::fopen(tmp.c_str(), "w");
+    std::vector<int> cx((size_t)ns), cy((size_t)ns), cz((size_t)ns);
+    for (int z = 0; z < M[2]; z++)
+      for (int y = 0; y < M[1]; y++)
+        for (int x = 0; x < M[0]; x++) {
+          const long long l = num[(size_t)x + (size_t)M[0] * (y + (size_t)M[1] * z)];
+          if (l) {
+            cx[l - 1] = x + 1;
+            cy[l - 1] = y + 1;
+            cz[l - 1] = z + 1;
+          }
+        }
+    for (long long l = 0; l < ns; l++)
+      std::fprintf(f, " %24.16E %24.16E %24.16E\n", cx[l] + u[3 * l], cy[l] + u[3 * l + 1], cz[l] + u[3 * l + 2]);
+    for (int rep = 0; rep < 2; rep++)
+      for (long long l = 0; l < ns; l++) std::fprintf(f, " %24.16E %24.16E %24.16E\n", 0.0, 0.0, 0.0);
+    std::fclose(f);
+    if (std::rename(tmp.c_str(), path("iteration2").c_str()) != 0) die("cannot rename iteration2");
+  }
+  {  // calc_stress record (XX:1963-1994 / YZ likewise)
+    FILE* f = std::fopen(path("stress_tensor").c_str(), "a");
+    const double Em = in.Em1, nu = in.nu1;
+    std::fprintf(f, " Elastic medium properties\n Ypung modulus Em = %.16E\n Poisson ratio nu = %.16E\n", Em, nu);
+    std::fprintf(f, " Stiffness coefficients\n C_xxxx = %.16E\n C_yyxx = %.16E\n C_xyxy = %.16E\n",
+                 Em * (nu - 1.0) / (2.0 * nu * nu + nu - 1.0), Em * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)),
+                 Em / (2.0 * (1.0 + nu)));
+    std::fprintf(f, " Simulation parameters\n Cell volume vcell = %.16E\n", (double)in.ncx * in.ncy * in.ncz);
+    std::fprintf(f, " Solid part volume(elementary cubes) rncub = %.16E\n", (double)r.ncube);
+    std::fprintf(f, " Global strain = %.16E\n Simulation results\n averaged stress tensor over ALL the cell\n asigmap = \n",
+                 r.strain);
+    for (int c = 0; c < 3; c++)  // asigmap(1:3, c), Fortran column order
+      std::fprintf(f, " %.16E %.16E %.16E\n", r.sigma[c] / r.ncube, r.sigma[3 + c] / r.ncube, r.sigma[6 + c] / r.ncube);
+    std::fprintf(f, " Effective stiffness coefficients\n %s = %.16E\n", load == PS_LOAD_XSTRETCH ? "Exxxx" : "Eyzyz",
+                 r.modulus);
+    std::fclose(f);
+  }
+  if (!quiet)
+    std::printf("%s = %.10e  (%lld iterations, relative residual %.3e)\n", load == PS_LOAD_XSTRETCH ? "Exxxx" : "Eyzyz",
+                r.modulus, (long long)r.inner_iterations, r.relres);
+  ps_lsm_destroy(h);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv)
 {
-  int prec = PS_PREC_F64;
+  int prec = PS_PREC_F64, lsm_load = -1;
   bool quiet = false;
+  std::string pname = "f64";
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     if (s == "-d" && a + 1 < argc) {
       g_dir = argv[++a];
     } else if (s == "-p" && a + 1 < argc) {
-      const std::string p = argv[++a];
-      prec = p == "f64" ? PS_PREC_F64 : p == "f32" ? PS_PREC_F32 : p == "f16" ? PS_PREC_F16 : p == "bf16" ? PS_PREC_BF16 : -1;
-      if (prec < 0) die("unknown precision " + p);
+      pname = argv[++a];
+    } else if (s == "-m" && a + 1 < argc) {
+      const std::string m = argv[++a];
+      if (m == "lbm") lsm_load = -1;
+      else if (m == "xx") lsm_load = PS_LOAD_XSTRETCH;
+      else if (m == "yz") lsm_load = PS_LOAD_YZSHEAR;
+      else die("unknown mode " + m);
     } else if (s == "-q") {
       quiet = true;
     } else {
-      die("usage: porescale_run [-d DIR] [-p f64|f32|f16|bf16] [-q]");
+      die("usage: porescale_run [-d DIR] [-m lbm|xx|yz] [-p f64|f32|f16|bf16 (lbm) | f64|mixed (xx, yz)] [-q]");
     }
   }
+  if (lsm_load >= 0) {
+    const int lp = pname == "f64" ? PS_LSM_F64 : pname == "mixed" ? PS_LSM_MIXED : -1;
+    if (lp < 0) die("unknown spring-solve precision " + pname);
+    return run_lsm(lsm_load, lp, quiet);
+  }
+  prec = pname == "f64" ? PS_PREC_F64 : pname == "f32" ? PS_PREC_F32 : pname == "f16" ? PS_PREC_F16 : pname == "bf16" ? PS_PREC_BF16 : -1;
+  if (prec < 0) die("unknown precision " + pname);
   const Input in = read_input();
   if (in.mtype != 0) die("mtype = 1 (interpolation rule) is not supported: the reference's own path is dead code");
   check_velocities();
-  std::vector<int32_t> ind = read_ind(in);
+  std::vector<int32_t> ind = read_ind(in.ncx, in.ncy, in.ncz);
 
   ps_lbm_params p{};
   p.cr2 = in.cr2;

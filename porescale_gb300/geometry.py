@@ -140,3 +140,49 @@ def gray_field(n, sigma: float, slope: float, quantile: float, seed: int) -> np.
     sm = (sm - sm.mean()) / sm.std()
     c = np.quantile(sm, quantile)
     return 1.0 / (1.0 + np.exp(-slope * (sm - c)))
+
+
+def spanning_solid(ind: np.ndarray) -> np.ndarray:
+    """ind with every solid cluster except the largest turned into pore (1).
+
+    Solid voxels (0 and 3) belong to one cluster when they share a face,
+    periodic in every axis.  The lattice-spring network couples cubes that
+    share only a corner or an edge through no angular spring, so such a
+    joint is a hinge, and a cluster not face-joined to the largest one is a
+    free body or a mechanism: under a fluid wall load it has no static
+    equilibrium."""
+    from scipy import ndimage
+    solid = (ind == 0) | (ind == 3)
+    pad = np.pad(solid, 1, mode="wrap")
+    lab, n = ndimage.label(pad, structure=ndimage.generate_binary_structure(3, 1))
+    parent = np.arange(n + 1)
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    # every padded voxel is a copy of an interior one: join their labels
+    core = lab[1:-1, 1:-1, 1:-1]
+    nz, ny, nx = solid.shape
+    zi = (np.arange(nz + 2) - 1) % nz
+    yi = (np.arange(ny + 2) - 1) % ny
+    xi = (np.arange(nx + 2) - 1) % nx
+    ref = core[np.ix_(zi, yi, xi)]
+    shell = np.ones(pad.shape, bool)
+    shell[1:-1, 1:-1, 1:-1] = False
+    for a, b in zip(lab[shell & pad], ref[shell & pad]):
+        ra, rb = find(int(a)), find(int(b))
+        if ra != rb:
+            parent[ra] = rb
+    roots = np.array([find(int(c)) if c else 0 for c in range(n + 1)])
+    comp = roots[core]
+    if not solid.any():
+        return ind.copy()
+    counts = np.bincount(comp[solid])
+    counts[0] = 0
+    keep = int(np.argmax(counts))
+    out = ind.copy()
+    out[solid & (comp != keep)] = 1
+    return out

@@ -47,6 +47,7 @@ _SIGS = {
     "ps_lsm_stream": (C.c_void_p, [C.c_void_p]),
     "ps_lsm_stress_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "ps_lsm_gradients": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "ps_lsm_batch_solve": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_double, C.c_int32, C.POINTER(LsmResult)]),
     "ps_lsm_set_wall_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
     "ps_lsm_alpha_beta": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.c_double,
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -131,3 +132,13 @@ class SpringNetwork:
     @property
     def stream(self) -> int:
         return int(self._lib.ps_lsm_stream(self._h) or 0)
+
+
+def batch_solve(networks, rtol=1e-10, maxit=200000):
+    """Solves several SpringNetworks together (ps_lsm_batch_solve); returns
+    their LsmResults in order."""
+    lib = networks[0]._lib
+    arr = (C.c_void_p * len(networks))(*[N._h.value for N in networks])
+    res = (LsmResult * len(networks))()
+    check(lib.ps_lsm_batch_solve(arr, len(networks), float(rtol), int(maxit), res))
+    return list(res)

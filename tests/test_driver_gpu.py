@@ -116,3 +116,39 @@ def test_driver_restart_continues_exactly(gpu, oracle_lib, tmp_path):
     gr, gb = o.get_state()
     assert it1 == 4 and np.array_equal(fr2, gr) and np.array_equal(fb2, gb)
     assert not os.path.exists(os.path.join(d, "iteration"))
+
+
+def _write_lsm_case(d, ind, Em1, nu1, Em2, nu2, g):
+    nz, ny, nx = ind.shape
+    vals = [nx, ny, nz, Em1, nu1, Em2, nu2, 2.65, 1.0, 1.0, 1, 1, g, 1, 0]
+    open(os.path.join(d, "INPUT_PARAMETERS"), "w").write("\n".join(f"{v}" for v in vals) + "\n")
+    with open(os.path.join(d, "ind"), "w") as f:
+        for k in range(nz):
+            for j in range(ny):
+                f.write(" " + "".join(str(v) for v in ind[k, j]) + "\n")
+
+
+@pytest.mark.parametrize("mode", ["xx", "yz"])
+def test_driver_lsm_mode_matches_api(gpu, tmp_path, mode):
+    """porescale_run -m xx|yz: the reference program's INPUT_PARAMETERS in,
+    stress_tensor and LSM_displ_field out, equal to the C ABI's solve."""
+    from porescale_gb300 import _build
+    from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, SpringNetwork, spring_constants
+    _build.build_driver()
+    ind = geo.inclusions(10, 0.25, 2.5, seed=8)
+    d = str(tmp_path)
+    g = 0.004
+    _write_lsm_case(d, ind, 18.0, 0.3, 6.0, 0.25, g)
+    _run(d, "-m", mode)
+    txt = open(os.path.join(d, "stress_tensor")).read()
+    key = "Exxxx" if mode == "xx" else "Eyzyz"
+    got = float(txt.split(key + " =")[1].split()[0])
+    a1, b1 = spring_constants(18.0, 0.3)
+    a2, b2 = spring_constants(6.0, 0.25)
+    load = LOAD_XSTRETCH if mode == "xx" else LOAD_YZSHEAR
+    with SpringNetwork(ind, a1, b1, a2, b2, g, load, LSM_F64) as S:
+        r = S.solve(1e-10, 200000)
+    assert got == pytest.approx(r.modulus, rel=1e-12)
+    disp = np.loadtxt(os.path.join(d, "LSM_displ_field"))
+    assert disp.shape == (ind.size, 3) and np.abs(disp).max() > 0
+    assert os.path.exists(os.path.join(d, "iteration2")) and os.path.exists(os.path.join(d, "lsm_settings"))

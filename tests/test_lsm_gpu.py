@@ -111,3 +111,23 @@ def test_modulus_gradients_mixed_precision(gpu):
             S.solve(1e-11, 100000)
             out.append(S.gradients())
     assert np.allclose(out[1], out[0], rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("prec", [LSM_F64, LSM_MIXED])
+def test_batch_solve_matches_individual(gpu, prec):
+    """ps_lsm_batch_solve: three networks of different boxes and loads
+    solved by shared launches give the moduli of their individual solves."""
+    from porescale_gb300.springs import batch_solve
+    cases = [(geo.inclusions(10, 0.25, 2.5, 3), LOAD_XSTRETCH), (geo.inclusions((12, 8, 14), 0.2, 2.0, 4), LOAD_YZSHEAR),
+             (geo.inclusions(16, 0.3, 3.0, 5), LOAD_XSTRETCH)]
+    nets = [SpringNetwork(ind, A1, B1, A2, B2, 0.002 * ind.shape[2], load, prec) for ind, load in cases]
+    try:
+        got = batch_solve(nets, 1e-11, 200000)
+        for N, r in zip(nets, got):
+            alone = N.solve(1e-11, 200000)
+            assert r.converged == 1
+            assert r.modulus == pytest.approx(alone.modulus, rel=1e-12 if prec == LSM_F64 else 1e-9)
+            assert np.allclose(r.sigma[:], alone.sigma[:], rtol=1e-9, atol=1e-12 * max(abs(v) for v in alone.sigma))
+    finally:
+        for N in nets:
+            N.close()
