@@ -883,7 +883,8 @@ int ps_lbm_init_random(void* h, double sat)
   if (!h) return fail(PS_ERR_ARG, "ps_lbm_init_random: null handle");
   Lattice* L = as_lattice(h);
   // Park-Miller minimal standard generator on doubles (S1:2828-2843)
-  std::vector<double> fr((size_t)19 * L->nl), fb((size_t)19 * L->nl);
+  // (at least one element, so that an empty lattice passes valid pointers)
+  std::vector<double> fr((size_t)19 * std::max(1LL, L->nl)), fb((size_t)19 * std::max(1LL, L->nl));
   double seed = 13.081984;
   const double m31 = 2147483647.0, p31 = 2147483648.0;
   for (long long i = 0; i < L->nl; i++) {

@@ -46,3 +46,39 @@ def test_python_bindings_cover_header():
     from porescale_gb300 import _lib, gray, springs  # noqa: F401  (these register their signatures)
     missing = [n for n in _declared() if n not in _lib.SIGNATURES]
     assert not missing, missing
+
+
+def test_argument_errors_and_missing_device(lib):
+    """Entry points validate their arguments before touching the device and
+    fail with a code and a message (never a CPU fallback): bad boxes and
+    precisions are PS_ERR_ARG; on a machine without a GPU a valid lattice
+    request is PS_ERR_NODEVICE."""
+    import numpy as np
+    from porescale_gb300 import _lib
+    from porescale_gb300.lattice import make_params
+
+    for name, (res, args) in _lib.SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype, fn.argtypes = res, args
+    p = make_params(vir=0.1, vib=0.1, wet=0.5)
+    h = ctypes.c_void_p()
+    ind = np.ones((4, 4, 4), np.int32)
+    ip = ind.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    assert lib.ps_lbm_create(ctypes.byref(p), ip, 1025, 4, 4, 0, ctypes.byref(h)) == 1
+    assert lib.ps_lbm_create(ctypes.byref(p), ip, 4, 4, 4, 7, ctypes.byref(h)) == 1
+    assert lib.ps_lbm_create(ctypes.byref(p), ip, 0, 4, 4, 0, ctypes.byref(h)) == 1
+    assert lib.ps_lbm_create(None, ip, 4, 4, 4, 0, ctypes.byref(h)) == 1
+    assert lib.ps_batch_create(None, 0, ctypes.byref(h)) == 1
+    assert lib.ps_lbm_step(None, 1) == 1
+    buf = ctypes.create_string_buffer(256)
+    lib.ps_last_error(buf, 256)
+    assert b"null" in buf.value
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        assert lib.ps_lbm_create(ctypes.byref(p), ip, 4, 4, 4, 0, ctypes.byref(h)) == 6  # PS_ERR_NODEVICE
+        lib.ps_last_error(buf, 256)
+        assert b"device" in buf.value

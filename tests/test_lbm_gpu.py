@@ -179,3 +179,31 @@ def test_fused_step_matches_two_pass(gpu, prec, planes, ahead, tile):
             L.step(9)
             out.append(L.get_state())
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_edge_geometries(gpu, oracle_lib, prec):
+    """No fluid at all (every call succeeds, observables of an empty lattice),
+    no solid at all (periodic box: FP64 still bit-exact), and a 2x3x2 box
+    (every neighbour is a periodic image)."""
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    with Lattice(p, np.zeros((6, 5, 4), np.int32), prec) as L:
+        assert L.nl == 0
+        L.init_random(0.5)
+        L.step(3)
+        o = L.observables()
+        assert o.tmr == 0.0 and o.tmb == 0.0
+    for ind in (np.ones((6, 5, 4), np.int32), np.ones((2, 3, 2), np.int32)):
+        o = oracle_lib.OracleLattice(p, ind)
+        o.init_random(0.5)
+        fr, fb = o.get_state()
+        o.run(6)
+        with Lattice(p, ind, prec) as L:
+            L.set_state(fr, fb)
+            L.step(6)
+            gr, gb = L.get_state()
+        want_r, want_b = o.get_state()
+        if prec == 0:
+            assert np.array_equal(gr, want_r) and np.array_equal(gb, want_b)
+        else:
+            assert max(np.abs(gr - want_r).max(), np.abs(gb - want_b).max()) < 5e-4
