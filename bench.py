@@ -418,52 +418,62 @@ def batch_mode(args):
         ms = e0.elapsed_time(e1)
     mlups = nodes * T / (ms * 1e-3) / 1e6
 
-    def lsm_job(v):
+    # the spring networks of every subvolume and load case, built on 8 host
+    # threads (geometry, node tables, wall load); the solves below start
+    # from x = 0 each time, so both solve paths use the same networks
+    from porescale_gb300.springs import batch_solve
+    cases = ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz"))
+
+    def build_nets(v):
         ind = inds[v]
         incl = geometry.inclusions(ind.shape, 0.25, 3.0, specs[v]["seed"] + 7)
         ind_s = np.where(ind == 0, np.where(incl == 3, 3, 0), 1).astype(np.int32)
-        out = {}
-        for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
-            with SpringNetwork(ind_s, 1.0, 0.4, 0.3, 0.1, 1e-3 * ind.shape[2] / 2, load, LSM_MIXED) as S:
-                S.set_wall_load(lats[v], 1.0)
-                try:
-                    r = S.solve(1e-8, 400000)
-                    out[name] = r.modulus
-                except PorescaleError as exc:
-                    out[name] = None
-                    out[name + "_error"] = str(exc)
-        return out
-
-    # all networks of a load case in one batched solve (shared launches)
-    from porescale_gb300.springs import batch_solve
-
-    def ind_s(v):
-        ind = inds[v]
-        incl = geometry.inclusions(ind.shape, 0.25, 3.0, specs[v]["seed"] + 7)
-        return np.where(ind == 0, np.where(incl == 3, 3, 0), 1).astype(np.int32)
-
-    t0 = time.perf_counter()
-    moduli = [{} for _ in lats]
-    for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
         nets = []
-        for v in range(len(lats)):
-            N = SpringNetwork(ind_s(v), 1.0, 0.4, 0.3, 0.1, 1e-3 * inds[v].shape[2] / 2, load, LSM_MIXED)
+        for load, _ in cases:
+            N = SpringNetwork(ind_s, 1.0, 0.4, 0.3, 0.1, 1e-3 * ind.shape[2] / 2, load, LSM_MIXED)
             N.set_wall_load(lats[v], 1.0)
             nets.append(N)
+        return nets
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(8) as ex:
+        nets = list(ex.map(build_nets, range(len(lats))))
+    t_lsm_setup = time.perf_counter() - t0
+
+    # all networks of a load case in one batched solve (shared launches)
+    t0 = time.perf_counter()
+    moduli = [{} for _ in lats]
+    for c, (_, name) in enumerate(cases):
         try:
-            for v, r in enumerate(batch_solve(nets, 1e-8, 400000)):
+            for v, r in enumerate(batch_solve([n[c] for n in nets], 1e-8, 400000)):
                 moduli[v][name] = r.modulus
+                moduli[v][name + "_inner"] = int(r.inner_iterations)
         except PorescaleError as exc:
             for v in range(len(lats)):
                 moduli[v][name + "_error"] = str(exc)
-        for N in nets:
-            N.close()
     t_lsm = time.perf_counter() - t0
+
     # the same solves one network at a time on 8 host threads, for comparison
+    def lsm_job(v):
+        out = {}
+        for c, (_, name) in enumerate(cases):
+            try:
+                r = nets[v][c].solve(1e-8, 400000)
+                out[name] = r.modulus
+                out[name + "_inner"] = int(r.inner_iterations)
+            except PorescaleError as exc:
+                out[name] = None
+                out[name + "_error"] = str(exc)
+        return out
+
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(8) as ex:
         moduli_ind = list(ex.map(lsm_job, range(len(lats))))
     t_lsm_ind = time.perf_counter() - t0
+    for n in nets:
+        for N in n:
+            N.close()
     agree = max((abs(a[k] - b[k]) / abs(b[k]) for a, b in zip(moduli, moduli_ind) for k in ("Cxxxx", "Cyzyz")
                  if a.get(k) and b.get(k)), default=None)
     # plain per-volume FP64 path on the first few subvolumes: time and errors
@@ -489,8 +499,10 @@ def batch_mode(args):
     out = {"mode": "batch", "volumes": len(lats), "steps": T, "precision": args.prec, "fluid_nodes": nodes,
            "tile": list(tile), "lbm_seconds": ms * 1e-3, "lbm_wall_seconds": t_lbm, "mlups": mlups,
            "achieved_gbs": mlups * 1e6 * bpn / 1e9, "frac": mlups * 1e6 * bpn / 1e9 / peak, "peak_kind": peak_kind,
-           "lsm_seconds": t_lsm, "lsm_individual_seconds": t_lsm_ind, "lsm_batch_vs_individual_max_rel": agree,
-           "subvolumes_per_s": len(lats) / (ms * 1e-3 + t_lsm),
+           "lsm_setup_seconds": t_lsm_setup, "lsm_seconds": t_lsm, "lsm_individual_seconds": t_lsm_ind, "lsm_batch_vs_individual_max_rel": agree,
+           "lsm_inner_iterations_batched": sum(m.get(k, 0) for m in moduli for k in ("Cxxxx_inner", "Cyzyz_inner")),
+           "lsm_inner_iterations_individual": sum(m.get(k, 0) for m in moduli_ind for k in ("Cxxxx_inner", "Cyzyz_inner")),
+           "subvolumes_per_s": len(lats) / (ms * 1e-3 + t_lsm_setup + min(t_lsm, t_lsm_ind)),
            "lbm_subvolumes_per_s": len(lats) / (ms * 1e-3),
            "f64_plain_mlups": f64_mlups,
            "f64_plain_subvolumes_per_s_estimate": (f64_mlups * 1e6 / (nodes * T / len(lats))) if f64_mlups else None,
@@ -533,6 +545,7 @@ def main():
     ap.add_argument("--accuracy-ref", default="", help="a previous accuracy JSON whose FP64 history is reused")
     ap.add_argument("--accuracy-legs", default="", help="comma list of legs besides f64 (default f64p,f32,f16,bf16)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default step configuration")
+    ap.add_argument("--tile", default="", help="tx,ty,occ: pin the step configuration instead of autotuning")
     ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -598,7 +611,10 @@ def main():
         L = Lattice(p, ind, PREC_ID[q])
         nl = L.nl
         L.set_state(fr, fb)
-        if not args.no_autotune:
+        if args.tile:
+            L.set_tile(*[int(v) for v in args.tile.split(",")])
+            L.info = L.get_info()
+        elif not args.no_autotune:
             L.autotune(4 if q != "f64" else 2)
             L.set_state(fr, fb)
         if world > 1:
@@ -618,7 +634,7 @@ def main():
         mlups = nl * steps / t / 1e6 * world
         launch_s = t / steps
         achieved = nl * ALGO_BYTES[q] / launch_s / 1e9
-        if q != "f64" and not args.no_autotune:
+        if q != "f64" and not args.no_autotune and not args.tile:
             # the step schedules side by side on this workload (fused: slab
             # planes x look-ahead), each from the same state
             study = {}

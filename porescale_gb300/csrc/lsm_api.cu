@@ -61,7 +61,11 @@ struct Springs {
   ps_lsm_result last{};
   long long dev_bytes = 0;
 
-  LsmGeom geom() const { return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_K32, d_S64}; }
+  LsmGeom geom() const
+  {
+    return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_K32, d_S64, {(float)p.alf1, (float)p.alf2},
+                   {(float)p.bet1, (float)p.bet2}};
+  }
 };
 
 void free_springs(Springs* S)
@@ -602,12 +606,11 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   S->nnode = nn;
   S->ncube = nc;
   // cube matrices, per material
-  static lsm::CubeMatrices M;
-  static bool built = false;
-  if (!built) {
-    lsm::build_cube_matrices(M);
-    built = true;
-  }
+  static const lsm::CubeMatrices M = [] {  // built once, thread-safe
+    lsm::CubeMatrices m;
+    lsm::build_cube_matrices(m);
+    return m;
+  }();
   std::vector<double> K64(2 * 24 * 24), S64(2 * 9 * 24), Kab(2 * 24 * 24);
   std::vector<float> K32(2 * 24 * 24);
   for (int i = 0; i < 24; i++)

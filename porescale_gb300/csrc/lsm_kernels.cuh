@@ -12,6 +12,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "lsm_cube_const.h"
+
 namespace ps {
 namespace lsm {
 
@@ -22,6 +24,31 @@ struct LsmGeom {
   const double* K64;    // per-material cube stiffness [2][24][24]
   const float* K32;
   const double* S64;    // per-material cube stress rows [2][9][24]
+  float alf[2], bet[2];  // spring constants of the two materials (FP32 matvec)
+};
+
+// the generated cube matrices in device-readable form; every read below
+// has indices fixed by full unrolling, so it folds to a literal and the
+// zero entries drop out
+__device__ const double kKa[24][24] = {
+#define PS_ROW(i) {kCubeKa[i][0], kCubeKa[i][1], kCubeKa[i][2], kCubeKa[i][3], kCubeKa[i][4], kCubeKa[i][5], \
+    kCubeKa[i][6], kCubeKa[i][7], kCubeKa[i][8], kCubeKa[i][9], kCubeKa[i][10], kCubeKa[i][11], kCubeKa[i][12], \
+    kCubeKa[i][13], kCubeKa[i][14], kCubeKa[i][15], kCubeKa[i][16], kCubeKa[i][17], kCubeKa[i][18], kCubeKa[i][19], \
+    kCubeKa[i][20], kCubeKa[i][21], kCubeKa[i][22], kCubeKa[i][23]}
+    PS_ROW(0), PS_ROW(1), PS_ROW(2), PS_ROW(3), PS_ROW(4), PS_ROW(5), PS_ROW(6), PS_ROW(7),
+    PS_ROW(8), PS_ROW(9), PS_ROW(10), PS_ROW(11), PS_ROW(12), PS_ROW(13), PS_ROW(14), PS_ROW(15),
+    PS_ROW(16), PS_ROW(17), PS_ROW(18), PS_ROW(19), PS_ROW(20), PS_ROW(21), PS_ROW(22), PS_ROW(23)
+#undef PS_ROW
+};
+__device__ const double kKb[24][24] = {
+#define PS_ROW(i) {kCubeKb[i][0], kCubeKb[i][1], kCubeKb[i][2], kCubeKb[i][3], kCubeKb[i][4], kCubeKb[i][5], \
+    kCubeKb[i][6], kCubeKb[i][7], kCubeKb[i][8], kCubeKb[i][9], kCubeKb[i][10], kCubeKb[i][11], kCubeKb[i][12], \
+    kCubeKb[i][13], kCubeKb[i][14], kCubeKb[i][15], kCubeKb[i][16], kCubeKb[i][17], kCubeKb[i][18], kCubeKb[i][19], \
+    kCubeKb[i][20], kCubeKb[i][21], kCubeKb[i][22], kCubeKb[i][23]}
+    PS_ROW(0), PS_ROW(1), PS_ROW(2), PS_ROW(3), PS_ROW(4), PS_ROW(5), PS_ROW(6), PS_ROW(7),
+    PS_ROW(8), PS_ROW(9), PS_ROW(10), PS_ROW(11), PS_ROW(12), PS_ROW(13), PS_ROW(14), PS_ROW(15),
+    PS_ROW(16), PS_ROW(17), PS_ROW(18), PS_ROW(19), PS_ROW(20), PS_ROW(21), PS_ROW(22), PS_ROW(23)
+#undef PS_ROW
 };
 
 template <typename T>
@@ -58,16 +85,39 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
         const int cv = xs[1 - ex] + nx * (ys[1 - ey] + ny * zs[1 - ez]);
         const int m = G.mat[cv];
         if (m == 0) continue;
+        if constexpr (sizeof(T) == 4) {
+          // FP32: K = alf Ka + bet Kb with Ka, Kb literal (zeros skipped)
+          T ta[3] = {T(0), T(0), T(0)}, tb[3] = {T(0), T(0), T(0)};
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
-          if (b == (e ^ 7)) continue;  // no spring couples opposite corners
-          const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
-          const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
-          const T u0 = p[nvb], u1 = p[nv + nvb], u2 = p[2 * nv + nvb];
+          for (int b = 0; b < 8; b++) {
+            if (b == (e ^ 7)) continue;  // no spring couples opposite corners
+            const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
+            const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
+            const T u[3] = {p[nvb], p[nv + nvb], p[2 * nv + nvb]};
 #pragma unroll
-          for (int r = 0; r < 3; r++)
-            acc[r] += kval<T>(G, m - 1, 3 * e + r, 3 * b) * u0 + kval<T>(G, m - 1, 3 * e + r, 3 * b + 1) * u1 +
-                      kval<T>(G, m - 1, 3 * e + r, 3 * b + 2) * u2;
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+              for (int c = 0; c < 3; c++) {
+                const T ka = (T)kKa[3 * e + r][3 * b + c], kb = (T)kKb[3 * e + r][3 * b + c];
+                if (ka != T(0)) ta[r] += ka * u[c];
+                if (kb != T(0)) tb[r] += kb * u[c];
+              }
+          }
+          const T al = m == 1 ? G.alf[0] : G.alf[1], be = m == 1 ? G.bet[0] : G.bet[1];
+#pragma unroll
+          for (int r = 0; r < 3; r++) acc[r] += al * ta[r] + be * tb[r];
+        } else {
+#pragma unroll
+          for (int b = 0; b < 8; b++) {
+            if (b == (e ^ 7)) continue;  // no spring couples opposite corners
+            const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
+            const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
+            const T u0 = p[nvb], u1 = p[nv + nvb], u2 = p[2 * nv + nvb];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+              acc[r] += kval<T>(G, m - 1, 3 * e + r, 3 * b) * u0 + kval<T>(G, m - 1, 3 * e + r, 3 * b + 1) * u1 +
+                        kval<T>(G, m - 1, 3 * e + r, 3 * b + 2) * u2;
+          }
         }
       }
       pq = (double)p[v] * (double)acc[0] + (double)p[nv + v] * (double)acc[1] + (double)p[2 * nv + v] * (double)acc[2];

@@ -7,6 +7,7 @@ conservation, the TRT magic parameter, Poiseuille-type flow, and the damped
 Verlet relaxation of the reference reaching the CG solution.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -234,3 +235,18 @@ def test_gray_open_channel_permeability(oracle_lib):
     k, _ = oracle_lib.gray_forward(p, s)
     nu = (0.9 - 0.5) / 3
     assert k == pytest.approx(nu * (T + 0.5), rel=1e-10)
+
+
+def test_generated_cube_constants_are_current(tmp_path):
+    """lsm_cube_const.h (the cube matrices as literals for the FP32 matvec)
+    is the output of its generator on the current lsm_cube.h."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "porescale_gb300", "csrc")
+    exe = str(tmp_path / "gen")
+    subprocess.run([cxx, "-O2", "-I" + csrc, os.path.join(csrc, "gen_cube_const.cpp"), "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    assert out == open(os.path.join(csrc, "lsm_cube_const.h")).read()
