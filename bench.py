@@ -125,24 +125,28 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(prec: str, nl: int, fused: bool = False):
+def load_traffic(prec: str, nl: int, kind: str = "two-pass"):
     """DRAM bytes of one step from the committed ncu summary (scaled to this
     workload's fluid-node count; key "<prec>" for the two-pass step,
-    "<prec>_fused" for the fused one), or None."""
+    "<prec>_fused" / "<prec>_wave" for the other schedules), or None."""
     path = os.path.join(ROOT, "profiles", "lbm_step_dram.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    e = d.get(prec + ("_fused" if fused else ""))
+    e = d.get(prec + ("" if kind == "two-pass" else "_" + kind))
     if not e:
         return None
     return float(e["dram_bytes_per_fluid_node"]) * nl
 
 
 def time_steps(L, steps, warmup, torch):
-    """Device time of `steps` step launches on the lattice's stream (CUDA events)."""
+    """Device time of `steps` step launches on the lattice's stream (CUDA events).
+    Under the wavefront schedule the warm-up is whole 8-step graphs, so the
+    graph of the timed steps' starting buffer is built before the timing."""
     stream = torch.cuda.ExternalStream(L.stream)
+    if int(L.get_info().wave):
+        warmup = max(8, -(-warmup // 8) * 8)
     L.step(warmup)
     L.sync()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -174,13 +178,14 @@ def cpu_oracle_mlups(ind, p, fr, fb, threads: int, budget_s: float):
     return nl * n / dt / 1e6, n, dt
 
 
-def lsm_leg(size=64, seed=20240601):
+def lsm_leg(size=64, seed=20240601, cpu_iters=0):
     """Lattice-spring static solve on the two-solid cube (matrix alpha 1.0,
     beta 0.4; radius-5 inclusions at volume fraction 0.25, alpha 0.3, beta
     0.1; strain 1e-3): Cxxxx and Cyzyz by FP64 CG and by FP32 CG in FP64
     refinement, CG iterations per second and the inner iteration's
     bandwidth (133 algorithmic bytes per node per FP32 iteration, 265 for
-    FP64)."""
+    FP64).  cpu_iters > 0 also times that many iterations of the oracle's
+    FP64 CG (one host thread) on the Cxxxx system as the CPU baseline."""
     from porescale_gb300 import geometry
     from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, LSM_MIXED, SpringNetwork
     ind = geometry.inclusions(size, 0.25, 5.0, seed)
@@ -203,6 +208,17 @@ def lsm_leg(size=64, seed=20240601):
                                           "frac": its * r.nnode * bpn / dt / 1e9 / peak}
         out[f"{name}_rel_diff_mixed_vs_f64"] = abs(out[f"{name}_mixed"]["modulus"] - out[f"{name}_f64"]["modulus"]) / \
             abs(out[f"{name}_f64"]["modulus"])
+    if cpu_iters > 0:
+        import oracle
+        o = oracle.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+        t = time.perf_counter()
+        its, _ = o.cg(1e-10, cpu_iters)
+        dt = time.perf_counter() - t
+        o.close()
+        out["cpu_baseline"] = {"value": its / dt, "unit": "CG iterations/s", "cores": 1, "kind": "port",
+                               "sample": f"first {its} FP64 CG iterations of the Cxxxx system ({dt:.1f} s, "
+                                         "C restatement of the spring forces)"}
+        out["f64_vs_cpu"] = out["Cxxxx_f64"]["cg_iters_per_s"] / out["cpu_baseline"]["value"]
     return out
 
 
@@ -546,6 +562,7 @@ def main():
     ap.add_argument("--accuracy-legs", default="", help="comma list of legs besides f64 (default f64p,f32,f16,bf16)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default step configuration")
     ap.add_argument("--tile", default="", help="tx,ty,occ: pin the step configuration instead of autotuning")
+    ap.add_argument("--wave", default="", help="planes,window: with --tile, pin the wavefront schedule")
     ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -613,6 +630,8 @@ def main():
         L.set_state(fr, fb)
         if args.tile:
             L.set_tile(*[int(v) for v in args.tile.split(",")])
+            if args.wave:
+                L.set_wave(*[int(v) for v in args.wave.split(",")])
             L.info = L.get_info()
         elif not args.no_autotune:
             L.autotune(4 if q != "f64" else 2)
@@ -638,9 +657,10 @@ def main():
             # the step schedules side by side on this workload (fused: slab
             # planes x look-ahead), each from the same state
             study = {}
-            tile = (L.info.tile_x, L.info.tile_y, L.info.occupancy, int(L.info.schedule))
+            tile = (L.info.tile_x, L.info.tile_y, L.info.occupancy, int(L.info.schedule), int(L.info.wave))
             for planes, ahead in ((0, 1), (1, 1), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2)):
                 try:
+                    L.set_wave(0)
                     L.set_fused(0, 1)
                     L.set_tile(128, 256, 0)
                     L.set_fused(planes, ahead)
@@ -649,19 +669,35 @@ def main():
                     continue
                 L.set_state(fr, fb)
                 study[f"{planes}/{ahead}"] = nl * 20 / time_steps(L, 20, 3, torch) / 1e6
+            # wavefront graphs (slab planes / window) on the collide tile 128 x 6
             L.set_fused(0, 1)
+            L.set_tile(128, 256, 6)
+            for planes, window in ((2, 0), (4, 0), (8, 0), (16, 0), (32, 0), (64, 0), (4, 3), (8, 3)):
+                L.set_wave(planes, window)
+                L.set_state(fr, fb)
+                study[f"w{planes}/{window}"] = nl * 48 / time_steps(L, 48, 8, torch) / 1e6
+            L.set_wave(0)
             L.set_tile(*tile[:3])
             if tile[3]:
                 L.set_fused(tile[3] % 256, tile[3] // 256)
+            if tile[4]:
+                L.set_wave(tile[4] % 256, tile[4] // 256)
             L.set_state(fr, fb)
             L.info = L.get_info()
             res[q + "_schedules_mlups"] = study
-        sched = int(L.info.schedule)
+        sched, wave = int(L.info.schedule), int(L.info.wave)
+        if sched:
+            schedule, kps = {"kind": "fused", "slab_planes": sched % 256, "lookahead": sched // 256}, 1
+        elif wave:
+            nslab = -(-int(L.info.nz) // (wave % 256))
+            schedule = {"kind": "wave", "slab_planes": wave % 256, "window": wave // 256, "steps_per_graph": 8,
+                        "slabs": nslab}
+            kps = 2 * nslab
+        else:
+            schedule, kps = {"kind": "two-pass"}, 2
         res[q] = {"mlups": mlups, "ms_per_step": launch_s * 1e3, "steps": steps, "achieved_gbs": achieved,
                   "frac": achieved / peak, "tile": [L.info.tile_x, L.info.tile_y, L.info.occupancy],
-                  "schedule": ({"kind": "fused", "slab_planes": sched % 256, "lookahead": sched // 256} if sched
-                               else {"kind": "two-pass"}),
-                  "kernels_per_step": 1 if sched else 2}
+                  "schedule": schedule, "kernels_per_step": kps}
         if q == args.prec:
             # e2e through the C ABI with host buffers (pinned)
             hfr = torch.empty((nl, 19), dtype=torch.float64, pin_memory=True).numpy()
@@ -702,9 +738,9 @@ def main():
 
     lsm = None
     if rank == 0 and not args.no_lsm:
-        lsm = lsm_leg()
+        lsm = lsm_leg(cpu_iters=0 if args.no_cpu_baseline else 40)
     h = res[args.prec]
-    traffic = load_traffic(args.prec, nl, h["schedule"]["kind"] == "fused")
+    traffic = load_traffic(args.prec, nl, h["schedule"]["kind"])
     line = {
         "metric": metric, "value": h["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": h["steps"],
         "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -717,7 +753,8 @@ def main():
                      "algo_bytes_per_node": ALGO_BYTES[args.prec]},
         "e2e": res.get("e2e"),
         "cpu_baseline": cpu,
-        "gpu_launches": h["steps"] * h["kernels_per_step"],
+        "gpu_launches": (h["steps"] // 8 * 8 * h["kernels_per_step"] + h["steps"] % 8 * 2
+                         if h["schedule"]["kind"] == "wave" else h["steps"] * h["kernels_per_step"]),
         "clocks": clocks,
         "legs": {q: res[q] for q in legs},
         "schedules_mlups": {k[:-len("_schedules_mlups")]: v for k, v in res.items() if k.endswith("_schedules_mlups")},

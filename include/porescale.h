@@ -65,6 +65,7 @@ typedef struct {
   int32_t nx, ny, nz, precision;
   int32_t tile_x, tile_y, occupancy;  /* step-kernel configuration */
   int32_t schedule;     /* 0: two-pass step; else fused: slab planes + 256 x look-ahead */
+  int32_t wave;         /* 0: off; else wavefront graph: slab planes + 256 x window */
   int64_t device_bytes; /* device memory held by the handle */
 } ps_lbm_info;
 
@@ -132,9 +133,21 @@ int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
  * whose wait gives up (bounded) makes the next synchronising call return
  * PS_ERR_TIMEOUT. */
 int ps_lbm_set_fused(void *handle, int32_t planes, int32_t ahead);
-/* Times the candidate configurations (two-pass and fused) on the current
+/* Wavefront schedule: planes > 0 runs the steps in graphs of 8 steps whose
+ * density and collide launches each cover one z-slab of `planes` planes,
+ * ordered only by their data dependencies (density of slab k after the
+ * previous step's collides of slabs k-1..k+1; collide of slab k after the
+ * densities of k-1..k+1).  Later steps then follow earlier ones a few
+ * slabs behind, so populations are re-read from L2 soon after they were
+ * written.  window (0, or 2..64) additionally holds a step's collides at
+ * most `window` slabs ahead of the next step's densities.  Results are
+ * identical to the two-pass step; step counts that are not a multiple of 8
+ * finish with two-pass steps.  Turns the fused schedule off (and
+ * ps_lbm_set_fused with planes > 0 turns this one off). */
+int ps_lbm_set_wave(void *handle, int32_t planes, int32_t window);
+/* Times the candidate configurations (two-pass, fused, wavefront) on the current
  * state (restored afterwards) and keeps the fastest; writes its tile to
- * *tx, *ty, *occ (the schedule is in ps_lbm_info.schedule). */
+ * *tx, *ty, *occ (the schedules are in ps_lbm_info.schedule and .wave). */
 int ps_lbm_autotune(void *handle, int32_t steps, int32_t *tx, int32_t *ty, int32_t *occ);
 
 /* ---- batches of lattices (extension; no counterpart in the reference) ----

@@ -67,6 +67,11 @@ struct Lattice {
   unsigned* d_ctr = nullptr;
   int* d_err = nullptr;
   int nitems = 0, nslab = 0, sched_tx = 0, sched_planes = 0, sched_ahead = 0;
+  // wavefront schedule (0 planes: off): z-slab launches in a graph of
+  // kWaveSteps steps, one executable per starting buffer
+  int wave_planes = 0, wave_window = 0;
+  cudaGraphExec_t wave_exec[2] = {nullptr, nullptr};
+  int wave_key[5] = {0, 0, 0, 0, 0};  // (tx, ty, occ, planes, window) of wave_exec
   int obs_blocks = 0;
   int cur = 0;           // buffer holding the current state
   bool have_state = false;
@@ -129,6 +134,8 @@ void free_lattice(Lattice* L)
   if (!L) return;
   cudaFree(L->d_coord);
   cudaFree(L->d_wall);
+  for (cudaGraphExec_t x : L->wave_exec)
+    if (x) cudaGraphExecDestroy(x);
   cudaFree(L->d_items);
   cudaFree(L->d_ntd);
   cudaFree(L->d_ctr);
@@ -430,11 +437,52 @@ int ensure_schedule(Lattice* L)
   return PS_OK;
 }
 
+constexpr int kWaveSteps = 8;  // steps per wavefront graph (even: the buffers end where they began)
+
+// the wavefront graph starting from buffer L->cur for the current
+// (tx, ty, occ, planes, window); executables of an older key are dropped
+int ensure_wave(Lattice* L)
+{
+  const int key[5] = {L->tx, L->ty, L->zchunk, L->wave_planes, L->wave_window};
+  if (!std::equal(key, key + 5, L->wave_key)) {
+    for (cudaGraphExec_t& x : L->wave_exec) {
+      if (x) cudaGraphExecDestroy(x);
+      x = nullptr;
+    }
+    std::copy(key, key + 5, L->wave_key);
+  }
+  if (L->wave_exec[L->cur]) return PS_OK;
+  const int P = L->wave_planes, S = (L->nz + P - 1) / P;
+  std::vector<int> first(S + 1);
+  for (int k = 0; k <= S; k++) first[k] = L->rowstart_h[(size_t)std::min(L->nz, k * P) * L->ny];
+  LbmLaunchArgs a[kWaveSteps];
+  for (int s = 0; s < kWaveSteps; s++) {
+    const int b = L->cur ^ (s & 1);
+    a[s] = L->args(b, 1 - b);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = PREC_DISPATCH(lbm_wave_graph, L->prec, L->tx, L->ty, L->zchunk, a, kWaveSteps, first.data(), S,
+                                L->wave_window, &g);
+  if (e != cudaSuccess) return cuda_fail(e, "wavefront graph");
+  e = cudaGraphInstantiate(&L->wave_exec[L->cur], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    L->wave_exec[L->cur] = nullptr;
+    return cuda_fail(e, "wavefront graph instantiate");
+  }
+  return PS_OK;
+}
+
 int launch_steps(Lattice* L, int n)
 {
   if (L->fused_planes > 0)
     if (int r = ensure_schedule(L)) return r;
-  for (int s = 0; s < n; s++) {
+  int done = 0;
+  if (L->wave_planes > 0 && n >= kWaveSteps) {
+    if (int r = ensure_wave(L)) return r;
+    for (; n - done >= kWaveSteps; done += kWaveSteps) PS_CUDA(cudaGraphLaunch(L->wave_exec[L->cur], L->stream));
+  }
+  for (int s = done; s < n; s++) {
     LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
     cudaError_t e;
     if (L->fused_planes > 0) {
@@ -759,6 +807,7 @@ int ps_lbm_get_info(void* h, ps_lbm_info* o)
   o->tile_y = L->ty;
   o->occupancy = L->zchunk;
   o->schedule = L->fused_planes > 0 ? L->fused_planes + 256 * L->fused_ahead : 0;
+  o->wave = L->wave_planes > 0 ? L->wave_planes + 256 * L->wave_window : 0;
   o->device_bytes = L->dev_bytes;
   return PS_OK;
 }
@@ -1150,6 +1199,19 @@ int ps_lbm_set_fused(void* h, int32_t planes, int32_t ahead)
     return fail(PS_ERR_ARG, "ps_lbm_set_fused: the step configuration (%d, %d, %d) has no fused form", L->tx, L->ty, L->zchunk);
   L->fused_planes = planes;
   L->fused_ahead = ahead;
+  if (planes > 0) L->wave_planes = 0;
+  return PS_OK;
+}
+
+int ps_lbm_set_wave(void* h, int32_t planes, int32_t window)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_wave: null handle");
+  Lattice* L = as_lattice(h);
+  if (planes < 0 || (window != 0 && (window < 2 || window > 64)))
+    return fail(PS_ERR_ARG, "ps_lbm_set_wave: need planes >= 0 and window 0 or 2..64");
+  L->wave_planes = planes;
+  L->wave_window = window;
+  if (planes > 0) L->fused_planes = 0;
   return PS_OK;
 }
 
@@ -1188,18 +1250,21 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
 
   }
   struct Cfg {
-    int tx, ty, zc, planes, ahead;
+    int tx, ty, zc, planes, ahead, wplanes, window;
   };
-  // two-pass configurations, then fused ones (slab planes, look-ahead)
-  const std::vector<Cfg> cand = {{128, 256, 0, 0, 1}, {256, 256, 0, 0, 1}, {128, 128, 0, 0, 1}, {256, 512, 0, 0, 1},
-                                 {128, 256, 6, 0, 1}, {128, 256, 8, 0, 1}, {256, 256, 3, 0, 1}, {128, 256, 0, 2, 1},
-                                 {128, 256, 0, 4, 1}, {128, 256, 0, 8, 1}, {128, 256, 0, 4, 2}, {256, 256, 0, 4, 1},
-                                 {128, 256, 6, 4, 1}, {128, 256, 8, 4, 1}};
+  // two-pass configurations, fused ones (slab planes, look-ahead), then
+  // wavefront graphs (slab planes, window)
+  const std::vector<Cfg> cand = {
+      {128, 256, 0, 0, 1, 0, 0}, {256, 256, 0, 0, 1, 0, 0},  {128, 128, 0, 0, 1, 0, 0}, {256, 512, 0, 0, 1, 0, 0},
+      {128, 256, 6, 0, 1, 0, 0}, {128, 256, 8, 0, 1, 0, 0},  {256, 256, 3, 0, 1, 0, 0}, {128, 256, 0, 2, 1, 0, 0},
+      {128, 256, 0, 4, 1, 0, 0}, {128, 256, 0, 8, 1, 0, 0},  {128, 256, 0, 4, 2, 0, 0}, {256, 256, 0, 4, 1, 0, 0},
+      {128, 256, 6, 4, 1, 0, 0}, {128, 256, 8, 4, 1, 0, 0},  {128, 256, 6, 0, 1, 16, 0}, {128, 256, 6, 0, 1, 32, 0},
+      {128, 256, 8, 0, 1, 32, 0}, {128, 256, 0, 0, 1, 32, 0}, {128, 256, 6, 0, 1, 64, 0}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead};
+  Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead, L->wave_planes, L->wave_window};
   const int saved_cur = L->cur;
   int rc = PS_OK;
   for (const Cfg& c : cand) {
@@ -1208,16 +1273,21 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
     L->zchunk = c.zc;
     L->fused_planes = c.planes;
     L->fused_ahead = c.ahead;
-    rc = launch_steps(L, 2);  // warm-up
+    L->wave_planes = c.wplanes;
+    L->wave_window = c.window;
+    // a wavefront candidate runs whole graphs (and builds its graph in the warm-up)
+    const int n = c.wplanes > 0 ? std::max(steps, kWaveSteps) / kWaveSteps * kWaveSteps : steps;
+    rc = launch_steps(L, c.wplanes > 0 ? kWaveSteps : 2);  // warm-up
     if (rc) break;
     cudaEventRecord(e0, L->stream);
-    rc = launch_steps(L, steps);
+    rc = launch_steps(L, n);
     cudaEventRecord(e1, L->stream);
     cudaEventSynchronize(e1);
     if (rc == PS_OK) rc = check_fused(L);
     if (rc) break;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)n;
     if (ms < best) {
       best = ms;
       bc = c;
@@ -1237,6 +1307,8 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   L->zchunk = bc.zc;
   L->fused_planes = bc.planes;
   L->fused_ahead = bc.ahead;
+  L->wave_planes = bc.wplanes;
+  L->wave_window = bc.window;
   if (tx_out) *tx_out = bc.tx;
   if (ty_out) *ty_out = bc.ty;
   if (zc_out) *zc_out = bc.zc;

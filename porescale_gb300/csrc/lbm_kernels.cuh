@@ -491,13 +491,17 @@ __device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R
   }
 }
 
+// Both step kernels work on the fluid nodes [i0, i1): the whole lattice,
+// or one z-slab of the wavefront schedule (slabs are contiguous ranges of
+// the compact numbering, z being the slowest coordinate).
 template <int PREC, int BLK>
 __global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                   const __grid_constant__ GeomDev G, const BufDev src,
-                                                  const BufDev dst, typename Store<PREC>::R* __restrict__ cc)
+                                                  const BufDev dst, typename Store<PREC>::R* __restrict__ cc,
+                                                  int i0, int i1)
 {
-  const int i = blockIdx.x * BLK + threadIdx.x;
-  if (i < G.nl) dens_node<PREC>(K, G, src, dst, cc, i);
+  const int i = i0 + blockIdx.x * BLK + threadIdx.x;
+  if (i < i1) dens_node<PREC>(K, G, src, dst, cc, i);
 }
 
 // MINB > 0 asks the register allocator for MINB resident CTAs per SM;
@@ -506,10 +510,11 @@ __global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmCon
 template <int PREC, int BLK, int MINB>
 __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK) k_lbm_coll(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                   const __grid_constant__ GeomDev G, const BufDev src,
-                                                  const BufDev dst, const typename Store<PREC>::R* __restrict__ cc)
+                                                  const BufDev dst, const typename Store<PREC>::R* __restrict__ cc,
+                                                  int i0, int i1)
 {
-  const int i = blockIdx.x * BLK + threadIdx.x;
-  if (i < G.nl) coll_node<PREC>(K, G, src, dst, cc, i);
+  const int i = i0 + blockIdx.x * BLK + threadIdx.x;
+  if (i < i1) coll_node<PREC>(K, G, src, dst, cc, i);
 }
 
 // ---- batched step kernels: many lattices (subvolumes) per launch ----------

@@ -2,6 +2,7 @@
 // Included by lbm_prec_f64.cu (PREC 0) and lbm_prec_lp.cu (PREC 1..3).
 #pragma once
 #include <algorithm>
+#include <vector>
 
 #include "lbm_launch.h"
 
@@ -16,9 +17,79 @@ cudaError_t step_blk(const LbmLaunchArgs& a)
   if (n == 0) return cudaSuccess;
   const LbmConst<R>& C = *static_cast<const LbmConst<R>*>(a.K);
   R* cc = static_cast<R*>(a.cc);
-  k_lbm_dens<PREC, BD><<<(unsigned)((n + BD - 1) / BD), BD, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
-  k_lbm_coll<PREC, BC, MINB><<<(unsigned)((n + BC - 1) / BC), BC, 0, a.stream>>>(C, a.G, a.src, a.dst, cc);
+  const int i1 = (int)n;
+  k_lbm_dens<PREC, BD><<<(unsigned)((n + BD - 1) / BD), BD, 0, a.stream>>>(C, a.G, a.src, a.dst, cc, 0, i1);
+  k_lbm_coll<PREC, BC, MINB><<<(unsigned)((n + BC - 1) / BC), BC, 0, a.stream>>>(C, a.G, a.src, a.dst, cc, 0, i1);
   return cudaGetLastError();
+}
+
+// Wavefront graph of `steps` steps over z-slabs (slab k = fluid nodes
+// [first[k], first[k+1])), a[s] the buffers of step s.  Only the true
+// dependencies order the launches:
+//   density(s, k)  after collide(s-1, k-1..k+1)  (their pushes land in slab
+//                  k; it also overwrites the colour and reference densities
+//                  those collides read);
+//   collide(s, k)  after density(s, k-1..k+1)    (27-point colour stencil,
+//                  receivers' reference densities).
+// Slab indices wrap (periodic z).  So step s+1 follows step s a few slabs
+// behind, and a density launch reads the populations the collides before
+// it have just written while they are still in L2, and the collide after it
+// re-reads them from there.  window >= 2 adds collide(s, k) after
+// density(s+1, k - window) for k > window, which keeps the collides of a
+// step from running far ahead of the next step's densities (those targets
+// depend only on lower slabs, so no cycle forms).  Empty slabs are empty
+// graph nodes.
+template <int PREC, int BC, int BD, int MINB = 0>
+cudaError_t wave_graph(const LbmLaunchArgs* a, int steps, const int* first, int S, int window, cudaGraph_t* out)
+{
+  using R = typename Store<PREC>::R;
+  *out = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  std::vector<cudaGraphNode_t> dn((size_t)S * steps), cn((size_t)S * steps);
+  auto add = [&](cudaGraphNode_t* node, const std::vector<cudaGraphNode_t>& deps, void* fn, int blk, int i0, int i1,
+                 const LbmLaunchArgs& la) -> cudaError_t {
+    if (i1 <= i0) return cudaGraphAddEmptyNode(node, g, deps.data(), deps.size());
+    R* cc = static_cast<R*>(la.cc);
+    const LbmConst<R>& C = *static_cast<const LbmConst<R>*>(la.K);
+    GeomDev G = la.G;
+    BufDev src = la.src, dst = la.dst;
+    void* args[] = {(void*)&C, (void*)&G, (void*)&src, (void*)&dst, (void*)&cc, (void*)&i0, (void*)&i1};
+    cudaKernelNodeParams kp = {};
+    kp.func = fn;
+    kp.gridDim = dim3((unsigned)((i1 - i0 + blk - 1) / blk));
+    kp.blockDim = dim3((unsigned)blk);
+    kp.kernelParams = args;
+    return cudaGraphAddKernelNode(node, g, deps.data(), deps.size(), &kp);
+  };
+  auto nb3 = [&](const std::vector<cudaGraphNode_t>& v, int s, int k) {
+    std::vector<cudaGraphNode_t> d;
+    for (int o = -1; o <= 1; o++) {
+      const cudaGraphNode_t n = v[(size_t)s * S + (k + o + S) % S];
+      if (std::find(d.begin(), d.end(), n) == d.end()) d.push_back(n);
+    }
+    return d;
+  };
+  for (int s = 0; s < steps && e == cudaSuccess; s++) {
+    for (int k = 0; k < S && e == cudaSuccess; k++) {
+      std::vector<cudaGraphNode_t> deps;
+      if (s > 0) deps = nb3(cn, s - 1, k);
+      e = add(&dn[(size_t)s * S + k], deps, (void*)k_lbm_dens<PREC, BD>, BD, first[k], first[k + 1], a[s]);
+      // the window edges of the previous step's collides that wait for this density
+      if (e == cudaSuccess && s > 0 && window > 0 && k >= 1 && k + window < S)
+        e = cudaGraphAddDependencies(g, &dn[(size_t)s * S + k], &cn[(size_t)(s - 1) * S + k + window], nullptr, 1);
+    }
+    for (int k = 0; k < S && e == cudaSuccess; k++)
+      e = add(&cn[(size_t)s * S + k], nb3(dn, s, k), (void*)k_lbm_coll<PREC, BC, MINB>, BC, first[k], first[k + 1],
+              a[s]);
+  }
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return e;
+  }
+  *out = g;
+  return cudaSuccess;
 }
 
 // resident CTAs per SM x SMs: the persistent grid of a batched kernel
@@ -145,6 +216,20 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
     if (tx == 128 && ty == 256 && occ == 6) return detail::step_blk<P, 128, 256, 6>(a);                    \
     if (tx == 128 && ty == 256 && occ == 8) return detail::step_blk<P, 128, 256, 8>(a);                    \
     if (tx == 256 && ty == 256 && occ == 3) return detail::step_blk<P, 256, 256, 3>(a);                    \
+    return cudaErrorInvalidValue;                                                                          \
+  }                                                                                                        \
+  cudaError_t lbm_wave_graph_##P(int tx, int ty, int occ, const LbmLaunchArgs* a, int steps, const int* first, \
+                                 int S, int window, cudaGraph_t* g)                                         \
+  {                                                                                                        \
+    if (occ == 0) {                                                                                        \
+      if (tx == 128 && ty == 256) return detail::wave_graph<P, 128, 256>(a, steps, first, S, window, g);   \
+      if (tx == 256 && ty == 256) return detail::wave_graph<P, 256, 256>(a, steps, first, S, window, g);   \
+      if (tx == 128 && ty == 128) return detail::wave_graph<P, 128, 128>(a, steps, first, S, window, g);   \
+      if (tx == 256 && ty == 512) return detail::wave_graph<P, 256, 512>(a, steps, first, S, window, g);   \
+    }                                                                                                      \
+    if (tx == 128 && ty == 256 && occ == 6) return detail::wave_graph<P, 128, 256, 6>(a, steps, first, S, window, g); \
+    if (tx == 128 && ty == 256 && occ == 8) return detail::wave_graph<P, 128, 256, 8>(a, steps, first, S, window, g); \
+    if (tx == 256 && ty == 256 && occ == 3) return detail::wave_graph<P, 256, 256, 3>(a, steps, first, S, window, g); \
     return cudaErrorInvalidValue;                                                                          \
   }                                                                                                        \
   cudaError_t lbm_fused_launch_##P(int tx, int occ, const LbmLaunchArgs& a, const FusedArgs& f)           \

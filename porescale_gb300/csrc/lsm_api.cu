@@ -56,6 +56,7 @@ struct Springs {
   // FP32 inner vectors
   float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
   double *part = nullptr, *scal = nullptr;
+  unsigned* ctr = nullptr;  // last-CTA counter of the CG reductions
   int nblk = 0;
   bool solved = false;
   ps_lsm_result last{};
@@ -87,6 +88,7 @@ void free_springs(Springs* S)
   cudaFree(S->r32);
   cudaFree(S->p32);
   cudaFree(S->q32);
+  cudaFree(S->ctr);
   cudaFree(S->part);
   cudaFree(S->scal);
   if (S->g64.exec) cudaGraphExecDestroy(S->g64.exec);
@@ -191,12 +193,16 @@ __global__ void k_ir_update(int n3, double s, const float* x32, double* x)
 __global__ void k_set_scal(double* scal, double rr, double bb)
 {
   scal[0] = rr;
+  scal[3] = 0.0;
   scal[5] = bb;
   scal[6] = 0.0;
   scal[7] = 0.0;
 }
 
 int blocks_for(long long n) { return (int)((n + kBlk - 1) / kBlk); }
+// CTAs of the CG kernels: one per tile of kMvPer (kVecPer) elements per thread
+int mv_tiles(long long n) { return (int)((n + lsm::kMvPer * kBlk - 1) / (lsm::kMvPer * kBlk)); }
+int vec_tiles(long long n) { return (int)((n + lsm::kVecPer * kBlk - 1) / (lsm::kVecPer * kBlk)); }
 
 // ---- host-side solve ---------------------------------------------------------
 int sum_parts(Springs* S, int n, double* d_out)
@@ -252,14 +258,11 @@ int cg(Springs* S, T* x, T* r, T* p, T* q, double tol, long long maxit, long lon
     cgg.exec = nullptr;
     cudaGraph_t graph = nullptr;
     PS_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+    const int tm = mv_tiles(S->nvox), tv = vec_tiles(n3);
     for (int k = 0; k < batch; k++) {
-      lsm::k_lsm_matvec<T, kBlk><<<nb, kBlk, 0, S->stream>>>(G, p, q, S->part);
-      lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, nb, S->scal + 1);
-      lsm::k_cg_alpha<<<1, 1, 0, S->stream>>>(S->scal, tol2);
-      lsm::k_cg_xr<T, kBlk><<<nb3, kBlk, 0, S->stream>>>(n3, S->scal, x, r, p, q, S->part);
-      lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, nb3, S->scal + 4);
-      lsm::k_cg_beta<<<1, 1, 0, S->stream>>>(S->scal);
-      lsm::k_cg_p<T><<<nb3, kBlk, 0, S->stream>>>(n3, S->scal, r, p);
+      lsm::k_cg_mv<T, kBlk><<<tm, kBlk, 0, S->stream>>>(G, S->scal, p, q, S->part, S->ctr, tol2);
+      lsm::k_cg_xr<T, kBlk><<<tv, kBlk, 0, S->stream>>>(n3, S->scal, x, r, p, q, S->part, S->ctr);
+      lsm::k_cg_p<T, kBlk><<<tv, kBlk, 0, S->stream>>>(n3, S->scal, r, p);
     }
     cudaError_t ce = cudaStreamEndCapture(S->stream, &graph);
     if (ce != cudaSuccess) return cuda_fail(ce, "CG batch capture");
@@ -471,6 +474,10 @@ int finish(Springs* S, double bb, double rtol, ps_lsm_result* out)
 // list at once: the iteration of cg<T> with each kernel launched once for
 // all networks (tile lists over their nodes / elements), 16 iterations per
 // captured graph, until every network has converged or maxit is reached.
+// When the networks still running hold under 3/4 of the node tiles the
+// graph was captured with, the tile lists are rebuilt over them (and the
+// graph re-captured), so the slowest networks' last iterations do not
+// launch the finished networks' tiles.
 template <typename T>
 int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cudaStream_t st)
 {
@@ -496,14 +503,15 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
     }
     d.part = S->part;
     d.scal = S->scal;
+    d.ctr = S->ctr;
     d.n3 = 3 * S->nvox;
-    d.nt1 = blocks_for(S->nvox);
-    d.nt3 = blocks_for(d.n3);
-    for (int b = 0; b < d.nt1; b++) t1.push_back(make_int2(s, b * kBlk));
-    for (int b = 0; b < d.nt3; b++) t3.push_back(make_int2(s, b * kBlk));
+    d.nt1 = mv_tiles(S->nvox);
+    d.nt3 = vec_tiles(d.n3);
+    t1.resize(t1.size() + d.nt1);
+    t3.resize(t3.size() + d.nt3);
     // |r0|^2 into scal[0] on the network's own stream
-    lsm::k_sq_norm_t<T, kBlk><<<d.nt3, kBlk, 0, S->stream>>>(d.n3, static_cast<const T*>(d.r), S->part);
-    if (int e = sum_parts(S, d.nt3, S->scal)) return e;
+    lsm::k_sq_norm_t<T, kBlk><<<blocks_for(d.n3), kBlk, 0, S->stream>>>(d.n3, static_cast<const T*>(d.r), S->part);
+    if (int e = sum_parts(S, blocks_for(d.n3), S->scal)) return e;
     PS_CUDA(cudaStreamSynchronize(S->stream));
   }
   int2 *d1 = nullptr, *d3 = nullptr;
@@ -515,41 +523,59 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
     cudaFree(ddone);
     if (exec) cudaGraphExecDestroy(exec);
   };
-  auto run = [&]() -> int {
-    PS_CUDA(cudaMalloc((void**)&d1, sizeof(int2) * t1.size()));
-    PS_CUDA(cudaMalloc((void**)&d3, sizeof(int2) * t3.size()));
-    PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * n));
+  const double tol2 = tol * tol;
+  const int batch = 16;
+  std::vector<double> done((size_t)n, 0.0);
+  // tile lists of the networks not yet converged, and the graph over them
+  auto rebuild = [&]() -> int {
+    t1.clear();
+    t3.clear();
+    for (int s = 0; s < n; s++) {
+      if (done[s] > 0.0) continue;
+      for (int b = 0; b < tab.s[s].nt1; b++) t1.push_back(make_int2(s, b * lsm::kMvPer * kBlk));
+      for (int b = 0; b < tab.s[s].nt3; b++) t3.push_back(make_int2(s, b * lsm::kVecPer * kBlk));
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    if (t1.empty()) return PS_OK;
     PS_CUDA(cudaMemcpyAsync(d1, t1.data(), sizeof(int2) * t1.size(), cudaMemcpyHostToDevice, st));
     PS_CUDA(cudaMemcpyAsync(d3, t3.data(), sizeof(int2) * t3.size(), cudaMemcpyHostToDevice, st));
-    lsm::k_cg_init_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab);
-    PS_CUDA(cudaGetLastError());
-    const double tol2 = tol * tol;
-    const int batch = 16;
     cudaGraph_t graph = nullptr;
     PS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < batch; k++) {
-      lsm::k_lsm_matvec_batch<T, kBlk><<<(unsigned)t1.size(), kBlk, 0, st>>>(tab, d1);
-      lsm::k_sum_batch<<<n, 1024, 0, st>>>(tab, 1, 1);
-      lsm::k_cg_alpha_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, tol2);
+      lsm::k_cg_mv_batch<T, kBlk><<<(unsigned)t1.size(), kBlk, 0, st>>>(tab, d1, tol2);
       lsm::k_cg_xr_batch<T, kBlk><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
-      lsm::k_sum_batch<<<n, 1024, 0, st>>>(tab, 4, 0);
-      lsm::k_cg_beta_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab);
-      lsm::k_cg_p_batch<T><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
+      lsm::k_cg_p_batch<T, kBlk><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
     if (ce != cudaSuccess) return cuda_fail(ce, "batched CG capture");
     ce = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) return cuda_fail(ce, "batched CG instantiate");
-    std::vector<double> done((size_t)n, 0.0);
-    for (long long it = 0; it < maxit; it += batch) {
+    if (ce != cudaSuccess) {
+      exec = nullptr;
+      return cuda_fail(ce, "batched CG instantiate");
+    }
+    return PS_OK;
+  };
+  auto run = [&]() -> int {
+    PS_CUDA(cudaMalloc((void**)&d1, sizeof(int2) * t1.size()));
+    PS_CUDA(cudaMalloc((void**)&d3, sizeof(int2) * t3.size()));
+    PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * n));
+    lsm::k_cg_init_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab);
+    PS_CUDA(cudaGetLastError());
+    if (int e = rebuild()) return e;
+    for (long long it = 0; it < maxit && exec; it += batch) {
       PS_CUDA(cudaGraphLaunch(exec, st));
       lsm::k_cg_done_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, ddone);
-      PS_CUDA(cudaMemcpyAsync(done.data(), ddone, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+      std::vector<double> now((size_t)n, 0.0);
+      PS_CUDA(cudaMemcpyAsync(now.data(), ddone, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
       PS_CUDA(cudaStreamSynchronize(st));
-      bool all = true;
-      for (double v : done) all = all && v > 0.0;
-      if (all) break;
+      size_t live = 0;  // node tiles of the networks still running
+      for (int s = 0; s < n; s++)
+        if (!(now[s] > 0.0)) live += (size_t)tab.s[s].nt1;
+      done = now;
+      if (live == 0 || 4 * live < 3 * t1.size())
+        if (int e = rebuild()) return e;
     }
     return PS_OK;
   };
@@ -640,6 +666,8 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   if (p->precision == PS_LSM_MIXED)
     for (float** v : {&S->x32, &S->r32, &S->p32, &S->q32})
       if (int r = dalloc(S.get(), v, b32)) return r;
+  if (int r = dalloc(S.get(), &S->ctr, sizeof(unsigned))) return r;
+  PS_CUDA(cudaMemsetAsync(S->ctr, 0, sizeof(unsigned), S->stream));
   if (int r = dalloc(S.get(), &S->part, sizeof(double) * 9 * (size_t)(S->nblk + 1))) return r;
   if (int r = dalloc(S.get(), &S->scal, sizeof(double) * 32)) return r;
   PS_CUDA(cudaMemsetAsync(S->scal, 0, sizeof(double) * 32, S->stream));

@@ -128,6 +128,12 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
   }
   return pq;
 }
+// CG direction update p' = r + beta p (one expression for every caller)
+template <typename T>
+__device__ __forceinline__ T next_dir(T r, T beta, T p)
+{
+  return r + beta * p;
+}
 
 // FP64 sum of one value per thread over the CTA, stored by thread 0 to *out
 template <int BLK>
@@ -303,16 +309,6 @@ __global__ void k_sum(const double* __restrict__ part, int n, double* __restrict
   }
 }
 
-// alpha = rr / pq (0 once converged); scal[7] counts the iterations taken
-__global__ void k_cg_alpha(double* scal, double tol2)
-{
-  const double rr = scal[0], pq = scal[1];
-  const bool done = scal[6] > 0.0 || rr <= tol2 * scal[5] || !(pq > 0.0);
-  scal[6] = done ? 1.0 : 0.0;
-  scal[2] = done ? 0.0 : rr / pq;
-  if (!done) scal[7] += 1.0;
-}
-
 // per-block partial sums of |r|^2
 template <typename T, int BLK>
 __global__ void __launch_bounds__(BLK) k_sq_norm_t(int n3, const T* __restrict__ r, double* __restrict__ part)
@@ -330,154 +326,202 @@ __global__ void __launch_bounds__(BLK) k_sq_norm_t(int n3, const T* __restrict__
   }
 }
 
-// x += alpha p; r -= alpha q; partial |r|^2
-template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_cg_xr(int n3, const double* __restrict__ scal, T* __restrict__ x,
-                                               T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
-                                               double* __restrict__ part)
+// Sum over all nblk CTAs of a launch of one FP64 value per thread: each CTA
+// stores its partial in part[slot] and counts itself in *ctr; the CTA that
+// counts last adds the partials in index order (the same order every
+// time), resets *ctr for the next launch and returns true in its thread 0
+// with the sum in *total.  No CTA waits for another.
+template <int BLK>
+__device__ __forceinline__ bool grid_sum_last(double t, double* part, int slot, unsigned* ctr, int nblk, double* total)
 {
-  const int i = blockIdx.x * BLK + threadIdx.x;
-  const T al = (T)scal[2];
-  double rr = 0.0;
-  if (i < n3) {
-    const T xi = x[i] + al * p[i];
-    const T ri = r[i] - al * q[i];
-    x[i] = xi;
-    r[i] = ri;
-    rr = (double)ri * (double)ri;
-  }
   __shared__ double red[BLK / 32];
-  for (int o = 16; o > 0; o >>= 1) rr += __shfl_xor_sync(0xffffffffu, rr, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = rr;
+  __shared__ int last;
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < BLK / 32; w++) s += red[w];
-    part[blockIdx.x] = s;
+    part[slot] = s;
+    __threadfence();
+    last = atomicAdd(ctr, 1u) == (unsigned)(nblk - 1);
   }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double a = 0.0;
+  int i = threadIdx.x;
+  for (; i + 3 * BLK < nblk; i += 4 * BLK) {  // four independent loads in flight
+    const double a0 = __ldcg(part + i), a1 = __ldcg(part + i + BLK), a2 = __ldcg(part + i + 2 * BLK),
+                 a3 = __ldcg(part + i + 3 * BLK);
+    a += a0;
+    a += a1;
+    a += a2;
+    a += a3;
+  }
+  for (; i < nblk; i += BLK) a += __ldcg(part + i);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x != 0) return false;
+  double s = 0.0;
+  for (int w = 0; w < BLK / 32; w++) s += red[w];
+  *total = s;
+  *ctr = 0u;
+  return true;
 }
 
+// alpha = rr / pq, or the stop flag (|r|^2 <= tol2 |b|^2, or pq <= 0);
+// scal[7] counts the iterations taken
+__device__ __forceinline__ void cg_alpha_fin(double* scal, double pq, double tol2)
+{
+  const double rr = scal[0];
+  const bool done = rr <= tol2 * scal[5] || !(pq > 0.0);
+  scal[1] = pq;
+  scal[6] = done ? 1.0 : 0.0;
+  scal[2] = done ? 0.0 : rr / pq;
+  if (!done) scal[7] += 1.0;
+}
 // beta = rr_new / rr; rr = rr_new
-__global__ void k_cg_beta(double* scal)
+__device__ __forceinline__ void cg_beta_fin(double* scal, double rn)
 {
-  const double rn = scal[4], ro = scal[0];
-  scal[3] = scal[6] > 0.0 || !(ro > 0.0) ? 0.0 : rn / ro;
-  if (scal[6] == 0.0) scal[0] = rn;
+  const double ro = scal[0];
+  scal[4] = rn;
+  scal[3] = !(ro > 0.0) ? 0.0 : rn / ro;
+  scal[0] = rn;
 }
 
-// p = r + beta p (p unchanged once converged)
-template <typename T>
-__global__ void k_cg_p(int n3, const double* __restrict__ scal, const T* __restrict__ r, T* __restrict__ p)
+// One CG iteration is three launches: k_cg_mv (q = A p, p.q over the grid,
+// its last CTA sets alpha or the stop flag), k_cg_xr (x and r along p, |r|^2
+// over the grid, its last CTA sets beta) and k_cg_p (p = r + beta p).  A
+// converged system (scal[6] set) returns at once, so replayed iterations
+// past convergence change nothing.  (Forming p on the fly inside the matvec
+// would save the third launch but repeats the update for every neighbour
+// read; the matvec is arithmetic-bound, so that is slower.)
+// Each CTA covers one tile of kMvTile nodes / kVecTile elements (threads
+// striding by BLK): few CTAs, so few partials and counter updates per
+// reduction.  The batched kernels use the same tiles, so a network sums in
+// the same order either way.
+constexpr int kMvPer = 1, kVecPer = 8;  // nodes / elements per thread
+
+template <typename T, int BLK>
+__device__ __forceinline__ double cg_mv_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v0)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n3 || scal[6] > 0.0) return;
-  p[i] = r[i] + (T)scal[3] * p[i];
+  double pq = 0.0;
+  const int v1 = min(v0 + kMvPer * BLK, G.nvox);
+  for (int v = v0 + (int)threadIdx.x; v < v1; v += BLK) pq += matvec_node<T>(G, p, q, v);
+  return pq;
+}
+template <typename T, int BLK>
+__device__ __forceinline__ double cg_xr_tile(int n3, T al, T* __restrict__ x, T* __restrict__ r,
+                                             const T* __restrict__ p, const T* __restrict__ q, int i0)
+{
+  double rr = 0.0;
+  const int i1 = min(i0 + kVecPer * BLK, n3);
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += BLK) {
+    const T xi = x[i] + al * p[i];
+    const T ri = r[i] - al * q[i];
+    x[i] = xi;
+    r[i] = ri;
+    rr += (double)ri * (double)ri;
+  }
+  return rr;
+}
+template <typename T, int BLK>
+__device__ __forceinline__ void cg_p_tile(int n3, T beta, const T* __restrict__ r, T* __restrict__ p, int i0)
+{
+  const int i1 = min(i0 + kVecPer * BLK, n3);
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += BLK) p[i] = next_dir(r[i], beta, p[i]);
+}
+
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_cg_mv(const LsmGeom G, double* __restrict__ scal, const T* __restrict__ p,
+                                               T* __restrict__ q, double* __restrict__ part,
+                                               unsigned* __restrict__ ctr, double tol2)
+{
+  if (scal[6] > 0.0) return;
+  const double pq = cg_mv_tile<T, BLK>(G, p, q, blockIdx.x * kMvPer * BLK);
+  double tot;
+  if (grid_sum_last<BLK>(pq, part, blockIdx.x, ctr, gridDim.x, &tot)) cg_alpha_fin(scal, tot, tol2);
+}
+
+// x += alpha p; r -= alpha q; |r|^2 over the grid, then beta
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_cg_xr(int n3, double* __restrict__ scal, T* __restrict__ x,
+                                               T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
+                                               double* __restrict__ part, unsigned* __restrict__ ctr)
+{
+  if (scal[6] > 0.0) return;
+  const double rr = cg_xr_tile<T, BLK>(n3, (T)scal[2], x, r, p, q, blockIdx.x * kVecPer * BLK);
+  double tot;
+  if (grid_sum_last<BLK>(rr, part, blockIdx.x, ctr, gridDim.x, &tot)) cg_beta_fin(scal, tot);
+}
+
+// p = r + beta p
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_cg_p(int n3, const double* __restrict__ scal, const T* __restrict__ r,
+                                              T* __restrict__ p)
+{
+  if (scal[6] > 0.0) return;
+  cg_p_tile<T, BLK>(n3, (T)scal[3], r, p, blockIdx.x * kVecPer * BLK);
 }
 
 // ---- batched CG: many networks advanced by the same launches ------------
 // The descriptor table (kernel parameter) holds each network's geometry,
-// CG vectors, partial-sum buffer and scalar block; tiles list (network,
-// first element) for the node-wise matvec and the element-wise vector
-// kernels.  Every network runs the single-network iteration above on its
-// own scalars: a converged network gets alpha = 0 and stops moving.
+// CG vectors, partial-sum buffer, counter and scalar block; tiles list
+// (network, first element) for the node-wise and the element-wise kernels.
+// Every network runs the single-network iteration above on its own
+// scalars, its last tile finishing its sums; a converged network's tiles
+// return at once.
 constexpr int kLsmBatchMax = 64;
 struct LsmSys {
   LsmGeom G;
   void *x, *r, *p, *q;
   double* part;   // per-tile partial sums
-  double* scal;   // CG scalars (layout of k_cg_alpha)
-  int n3, nt1, nt3;  // 3 nvox, node tiles, element tiles
+  double* scal;   // CG scalars (layout of cg_alpha_fin / cg_beta_fin)
+  unsigned* ctr;  // last-tile counter
+  int n3, nt1, nt3;  // 3 nvox, node tiles (kMvPer BLK nodes), element tiles (kVecPer BLK elements)
 };
 struct LsmTable {
   LsmSys s[kLsmBatchMax];
   int n;
 };
 
+// k_cg_mv over the node tiles of every network (tile = (network, first node))
 template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_lsm_matvec_batch(const __grid_constant__ LsmTable B,
-                                                          const int2* __restrict__ tiles)
+__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_cg_mv_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles,
+                                                     double tol2)
 {
   const int2 tl = __ldg(tiles + blockIdx.x);
   const LsmSys& S = B.s[tl.x];
-  if (S.scal[6] > 0.0) return;  // converged network: nothing moves (whole CTA)
-  const int v = tl.y + threadIdx.x;
-  const double pq =
-      v < S.G.nvox ? matvec_node<T>(S.G, static_cast<const T*>(S.p), static_cast<T*>(S.q), v) : 0.0;
-  block_sum_to<BLK>(pq, S.part + tl.y / BLK);
+  if (S.scal[6] > 0.0) return;  // converged network (whole CTA)
+  const double pq = cg_mv_tile<T, BLK>(S.G, static_cast<const T*>(S.p), static_cast<T*>(S.q), tl.y);
+  double tot;
+  if (grid_sum_last<BLK>(pq, S.part, tl.y / (kMvPer * BLK), S.ctr, S.nt1, &tot)) cg_alpha_fin(S.scal, tot, tol2);
 }
 
-// scal[which] = sum of the network's first n partials (n = nt1 or nt3)
-__global__ void k_sum_batch(const __grid_constant__ LsmTable B, int which, int node_tiles)
-{
-  const LsmSys& S = B.s[blockIdx.x];
-  if (S.scal[6] > 0.0) return;  // converged network: its scalars stay
-  const int n = node_tiles ? S.nt1 : S.nt3;
-  __shared__ double red[32];
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += S.part[i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) t += red[w];
-    S.scal[which] = t;
-  }
-}
-
-__global__ void k_cg_alpha_batch(const __grid_constant__ LsmTable B, double tol2)
-{
-  const int s = threadIdx.x;
-  if (s >= B.n) return;
-  double* scal = B.s[s].scal;
-  const double rr = scal[0], pq = scal[1];
-  const bool done = scal[6] > 0.0 || rr <= tol2 * scal[5] || !(pq > 0.0);
-  scal[6] = done ? 1.0 : 0.0;
-  scal[2] = done ? 0.0 : rr / pq;
-  if (!done) scal[7] += 1.0;
-}
-
+// k_cg_xr over the element tiles of every network
 template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_cg_xr_batch(const __grid_constant__ LsmTable B,
-                                                     const int2* __restrict__ tiles)
+__global__ void __launch_bounds__(BLK) k_cg_xr_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles)
 {
   const int2 tl = __ldg(tiles + blockIdx.x);
   const LsmSys& S = B.s[tl.x];
-  if (S.scal[6] > 0.0) return;  // converged network (alpha = 0): x, r unchanged
-  const int i = tl.y + threadIdx.x;
-  double rr = 0.0;
-  if (i < S.n3) {
-    const T al = (T)S.scal[2];
-    T* x = static_cast<T*>(S.x);
-    T* r = static_cast<T*>(S.r);
-    const T xi = x[i] + al * static_cast<const T*>(S.p)[i];
-    const T ri = r[i] - al * static_cast<const T*>(S.q)[i];
-    x[i] = xi;
-    r[i] = ri;
-    rr = (double)ri * (double)ri;
-  }
-  block_sum_to<BLK>(rr, S.part + tl.y / BLK);
+  if (S.scal[6] > 0.0) return;
+  const double rr = cg_xr_tile<T, BLK>(S.n3, (T)S.scal[2], static_cast<T*>(S.x), static_cast<T*>(S.r),
+                                       static_cast<const T*>(S.p), static_cast<const T*>(S.q), tl.y);
+  double tot;
+  if (grid_sum_last<BLK>(rr, S.part, tl.y / (kVecPer * BLK), S.ctr, S.nt3, &tot)) cg_beta_fin(S.scal, tot);
 }
 
-__global__ void k_cg_beta_batch(const __grid_constant__ LsmTable B)
-{
-  const int s = threadIdx.x;
-  if (s >= B.n) return;
-  double* scal = B.s[s].scal;
-  const double rn = scal[4], ro = scal[0];
-  scal[3] = scal[6] > 0.0 || !(ro > 0.0) ? 0.0 : rn / ro;
-  if (scal[6] == 0.0) scal[0] = rn;
-}
-
-template <typename T>
-__global__ void k_cg_p_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles)
+// k_cg_p over the element tiles of every network
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_cg_p_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles)
 {
   const int2 tl = __ldg(tiles + blockIdx.x);
   const LsmSys& S = B.s[tl.x];
-  const int i = tl.y + threadIdx.x;
-  if (i >= S.n3 || S.scal[6] > 0.0) return;
-  T* p = static_cast<T*>(S.p);
-  p[i] = static_cast<const T*>(S.r)[i] + (T)S.scal[3] * p[i];
+  if (S.scal[6] > 0.0) return;
+  cg_p_tile<T, BLK>(S.n3, (T)S.scal[3], static_cast<const T*>(S.r), static_cast<T*>(S.p), tl.y);
 }
 
 // |r0|^2 (already in scal[0]) becomes the reference |b|^2 of the tolerance
@@ -486,6 +530,7 @@ __global__ void k_cg_init_batch(const __grid_constant__ LsmTable B)
   const int s = threadIdx.x;
   if (s >= B.n) return;
   double* scal = B.s[s].scal;
+  scal[3] = 0.0;
   scal[5] = scal[0];
   scal[6] = 0.0;
   scal[7] = 0.0;

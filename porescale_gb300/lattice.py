@@ -129,6 +129,11 @@ class Lattice:
         """Fused one-launch step over z-slabs of `planes` planes (0: two-pass)."""
         check(self._lib.ps_lbm_set_fused(self._h, planes, ahead))
 
+    def set_wave(self, planes: int, window: int = 0) -> None:
+        """Wavefront schedule: 8-step graphs of z-slab launches of `planes`
+        planes ordered by their data dependencies (0: off)."""
+        check(self._lib.ps_lbm_set_wave(self._h, planes, window))
+
     def autotune(self, steps: int = 4):
         tx, ty, zc = C.c_int32(), C.c_int32(), C.c_int32()
         check(self._lib.ps_lbm_autotune(self._h, steps, C.byref(tx), C.byref(ty), C.byref(zc)))

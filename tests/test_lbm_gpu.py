@@ -10,6 +10,7 @@ import pytest
 
 from porescale_gb300 import PREC_BF16, PREC_F16, PREC_F32, PREC_F64
 from porescale_gb300 import geometry as geo
+from porescale_gb300._lib import PorescaleError
 from porescale_gb300.lattice import Lattice, make_params
 
 pytestmark = pytest.mark.gpu
@@ -179,6 +180,46 @@ def test_fused_step_matches_two_pass(gpu, prec, planes, ahead, tile):
             L.step(9)
             out.append(L.get_state())
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2, 3])
+@pytest.mark.parametrize("planes,window,tile", [(1, 0, (128, 256, 0)), (2, 3, (128, 256, 6)),
+                                                (7, 0, (256, 256, 0)), (32, 0, (128, 256, 8))])
+def test_wave_schedule_matches_two_pass(gpu, prec, planes, window, tile):
+    """The wavefront schedule (8-step graphs of z-slab launches ordered by
+    their data dependencies) gives the two-pass step's state bit for bit,
+    also with solid-only slabs (empty launches), a single slab and a step
+    count that ends with two-pass steps."""
+    ind = geo.sphere_pack((22, 18, 20), 0.45, 3.0, seed=17)
+    ind[:, :, 8:10] = 1  # two solid planes: slabs without fluid nodes
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    out = []
+    for wave in (False, True):
+        with Lattice(p, ind, prec) as L:
+            L.init_random(0.5)
+            L.set_tile(*tile)
+            if wave:
+                L.set_wave(planes, window)
+                assert L.get_info().wave == planes + 256 * window
+            L.step(19)
+            L.step(8)
+            out.append(L.get_state())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_wave_and_fused_exclusive(gpu):
+    ind = geo.sphere_pack((12, 12, 12), 0.45, 3.0, seed=3)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    with Lattice(p, ind, 2) as L:
+        L.set_wave(2)
+        L.set_fused(2, 1)
+        i = L.get_info()
+        assert i.wave == 0 and i.schedule == 2 + 256
+        L.set_wave(3, 2)
+        i = L.get_info()
+        assert i.wave == 3 + 512 and i.schedule == 0
+        with pytest.raises(PorescaleError):
+            L.set_wave(2, 1)
 
 
 @pytest.mark.parametrize("prec", [0, 2])
