@@ -36,8 +36,8 @@ sys.path.insert(0, ROOT)
 # algorithmic bytes per fluid-node update: 2 components x 19 populations x
 # (1 read + 1 write) x storage size + the per-node density field (1 write +
 # 1 read per component)
-ALGO_BYTES = {"f64": 640, "f32": 320, "f16": 168, "bf16": 168, "f16c": 168}
-PREC_ID = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3, "f16c": 4}
+ALGO_BYTES = {"f64": 640, "f32": 320, "f16": 168, "bf16": 168}
+PREC_ID = {"f64": 0, "f32": 1, "f16": 2, "bf16": 3}
 
 
 def workload_config(size: int):

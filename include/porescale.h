@@ -43,9 +43,6 @@ extern "C" {
 #define PS_PREC_F32 1   /* FP32 storage, FP32 arithmetic                         */
 #define PS_PREC_F16 2   /* FP16 deviations from rest equilibrium, FP32 arithmetic */
 #define PS_PREC_BF16 3  /* BF16 deviations from rest equilibrium, FP32 arithmetic */
-#define PS_PREC_F16C 4  /* per population: FP16 deviation of the total f_r + f_b and
-                           its colour (f_r - f_b) / (f_r + f_b) in 16-bit fixed point;
-                           FP32 arithmetic */
 
 /* Physical parameters of the two-phase LBM, as read from INPUT_PARAMETERS
  * (S1:435-469).  `sig` is the value in the file (the library applies the

@@ -16,12 +16,12 @@ is no CPU fallback: if the library is missing, importing the bindings raises.
 """
 from __future__ import annotations
 
-from ._lib import (PREC_BF16, PREC_F16, PREC_F16C, PREC_F32, PREC_F64, PREC_NAMES, LbmInfo, LbmObs, LbmParams, PorescaleError,
+from ._lib import (PREC_BF16, PREC_F16, PREC_F32, PREC_F64, PREC_NAMES, LbmInfo, LbmObs, LbmParams, PorescaleError,
                    library, library_path)
 from .lattice import Lattice, LatticeBatch
 from .springs import SpringNetwork, spring_constants
 
 __all__ = [
     "Lattice", "LatticeBatch", "SpringNetwork", "spring_constants", "LbmParams", "LbmInfo", "LbmObs", "PorescaleError", "library", "library_path",
-    "PREC_F64", "PREC_F32", "PREC_F16", "PREC_BF16", "PREC_F16C", "PREC_NAMES",
+    "PREC_F64", "PREC_F32", "PREC_F16", "PREC_BF16", "PREC_NAMES",
 ]

@@ -7,8 +7,8 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIBNAME = "libporescale_gpu.so"
 
-PREC_F64, PREC_F32, PREC_F16, PREC_BF16, PREC_F16C = 0, 1, 2, 3, 4
-PREC_NAMES = {PREC_F64: "f64", PREC_F32: "f32", PREC_F16: "f16", PREC_BF16: "bf16", PREC_F16C: "f16c"}
+PREC_F64, PREC_F32, PREC_F16, PREC_BF16 = 0, 1, 2, 3
+PREC_NAMES = {PREC_F64: "f64", PREC_F32: "f32", PREC_F16: "f16", PREC_BF16: "bf16"}
 
 PS_OK = 0
 ERRORS = {1: "PS_ERR_ARG", 2: "PS_ERR_CUDA", 3: "PS_ERR_NOMEM", 4: "PS_ERR_TIMEOUT", 5: "PS_ERR_NOTCONV",

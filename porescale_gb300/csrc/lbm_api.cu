@@ -378,8 +378,7 @@ int ensure_fields(Lattice* L)
   ((prec) == 0   ? fn##_0(__VA_ARGS__)                                      \
    : (prec) == 1 ? fn##_1(__VA_ARGS__)                                      \
    : (prec) == 2 ? fn##_2(__VA_ARGS__)                                      \
-   : (prec) == 3 ? fn##_3(__VA_ARGS__)                                      \
-                 : fn##_4(__VA_ARGS__))
+                 : fn##_3(__VA_ARGS__))
 
 Lattice* as_lattice(void* h) { return static_cast<Lattice*>(h); }
 
@@ -714,7 +713,7 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   if ((long long)nx * ny * nz > (1LL << 31) - 1) return fail(PS_ERR_ARG, "ps_lbm_create: box too large for int32 voxel ids");
   if (nx > 1024 || ny > 1024 || nz > 4096)
     return fail(PS_ERR_ARG, "ps_lbm_create: box %d x %d x %d exceeds 1024 x 1024 x 4096", nx, ny, nz);
-  if (precision < 0 || precision > 4) return fail(PS_ERR_ARG, "ps_lbm_create: precision %d not in 0..4", precision);
+  if (precision < 0 || precision > 3) return fail(PS_ERR_ARG, "ps_lbm_create: precision %d not in 0..3", precision);
   if (!(p->dt > 0.0) || !(p->rb0 != 0.0)) return fail(PS_ERR_ARG, "ps_lbm_create: dt must be > 0 and rb0 != 0");
   if (p->idir < 1 || p->idir > 3) return fail(PS_ERR_ARG, "ps_lbm_create: idir %d not in 1..3", p->idir);
   int ndev = 0;

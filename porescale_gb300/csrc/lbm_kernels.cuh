@@ -108,55 +108,34 @@ struct BufDev {
 // ---- storage policies ----------------------------------------------------
 template <int PREC>
 struct Store;
-// kColour: the pair is not (red, blue) but (total, colour), HalfCol below
 template <>
 struct Store<0> {  // FP64
   using T = double;
   using T2 = double2;
   using R = double;
-  static constexpr bool kDev = false, kColour = false;
+  static constexpr bool kDev = false;
 };
 template <>
 struct Store<1> {  // FP32 deviation
   using T = float;
   using T2 = float2;
   using R = float;
-  static constexpr bool kDev = true, kColour = false;
+  static constexpr bool kDev = true;
 };
 template <>
 struct Store<2> {  // FP16 deviation
   using T = __half;
   using T2 = __half2;
   using R = float;
-  static constexpr bool kDev = true, kColour = false;
+  static constexpr bool kDev = true;
 };
 template <>
 struct Store<3> {  // BF16 deviation
   using T = __nv_bfloat16;
   using T2 = __nv_bfloat162;
   using R = float;
-  static constexpr bool kDev = true, kColour = false;
+  static constexpr bool kDev = true;
 };
-// 16-bit total + colour: population d of a node as its total f_r + f_b, an
-// FP16 deviation (x 2^10) from t^r_d rho_r' + t^b_d rho_b' of the
-// receiving node, and its colour phi = (f_r - f_b) / (f_r + f_b) in 16-bit
-// fixed point (x 2^14, range [-2, 2)).  The total is smooth across an
-// interface, so its deviation stays small there, and the colour split has a
-// uniform 3e-5 resolution instead of the FP16 rounding of a large
-// per-component deviation; phi = +-1 (a bulk node's populations) is exact,
-// so the absent component stays exactly zero.
-struct __align__(4) HalfCol {
-  __half tot;
-  short col;
-};
-template <>
-struct Store<4> {
-  using T = __half;
-  using T2 = HalfCol;
-  using R = float;
-  static constexpr bool kDev = true, kColour = true;
-};
-constexpr float kColScale = 16384.f, kColMax = 32767.f / 16384.f;
 
 // FP16 deviations are stored scaled by 2^10 to keep them in the normal range
 template <typename T>
@@ -195,14 +174,7 @@ struct Pop {
                                               float2 rho, R& vr, R& vb)
   {
     const T2* p = static_cast<const T2*>(b.pop) + (long long)d * pitch + i;
-    if constexpr (S::kColour) {
-      const HalfCol h = *p;
-      const int w = wcls(d);
-      const float tot = (K.t[0][w] * rho.x + K.t[1][w] * rho.y) + __half2float(h.tot) * (1.0f / 1024.0f);
-      const float phi = (float)h.col * (1.0f / kColScale);
-      vr = tot * (0.5f + 0.5f * phi);
-      vb = tot - vr;
-    } else if constexpr (S::kDev) {
+    if constexpr (S::kDev) {
       const float2 v = to_f2(*p);
       vr = K.t[0][wcls(d)] * rho.x + v.x * DevScale<T>::down;
       vb = K.t[1][wcls(d)] * rho.y + v.y * DevScale<T>::down;
@@ -229,15 +201,7 @@ struct Pop {
                                              R vr, R vb, float2 rho)
   {
     T2* p = static_cast<T2*>(b.pop) + (long long)d * pitch + i;
-    if constexpr (S::kColour) {
-      const int w = wcls(d);
-      const float tot = vr + vb;
-      const float phi = vb == 0.f ? 1.f : (vr == 0.f ? -1.f : __fdividef(vr - vb, tot));
-      HalfCol h;
-      h.tot = __float2half_rn((tot - (K.t[0][w] * rho.x + K.t[1][w] * rho.y)) * 1024.0f);
-      h.col = (short)__float2int_rn(fminf(fmaxf(phi, -2.f), kColMax) * kColScale);
-      *p = h;
-    } else if constexpr (S::kDev) {
+    if constexpr (S::kDev) {
       *p = from_f2<T2>((vr - K.t[0][wcls(d)] * rho.x) * DevScale<T>::up,
                        (vb - K.t[1][wcls(d)] * rho.y) * DevScale<T>::up);
     } else {
@@ -460,7 +424,7 @@ __device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R
 {
   using R = typename Store<PREC>::R;
   R rr, rb;
-  if constexpr (Store<PREC>::kDev && !Store<PREC>::kColour) {
+  if constexpr (Store<PREC>::kDev) {
     float gr[19], gb[19];
     const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
     R sr = gr[0], sb = gb[0];
@@ -476,7 +440,6 @@ __device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R
     R f[38];
     read_node<PREC>(K, G, src, i, f);
     densities(f, rr, rb);
-    if constexpr (Store<PREC>::kDev) dst.rho[i] = make_float2(rr, rb);
   }
   int x, y, z;
   unpack(__ldg(G.coord + i), x, y, z);
@@ -699,7 +662,7 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
   const long long r = G.ref[i];
-  if constexpr (Store<PREC>::kDev && !Store<PREC>::kColour) {  // decode t_d rho + g in FP64
+  if constexpr (Store<PREC>::kDev) {  // decode t_d rho + g in FP64
     float gr[19], gb[19];
     const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
 #pragma unroll
@@ -730,17 +693,7 @@ __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
   const long long me = G.ref[i];
-  if constexpr (S::kColour) {
-    // the node's own densities are the reference
-    double sr = fr[19 * me], sb = fb[19 * me];
-    for (int d = 1; d < 19; d++) {
-      sr += fr[19 * me + d];
-      sb += fb[19 * me + d];
-    }
-    const float2 rho = make_float2((float)sr, (float)sb);
-    dst.rho[i] = rho;
-    for (int d = 0; d < 19; d++) Pop<PREC>::put(K, dst, d, i, G.pitch, (R)fr[19 * me + d], (R)fb[19 * me + d], rho);
-  } else if constexpr (S::kDev) {
+  if constexpr (S::kDev) {
     // the node's own densities are the reference; deviations formed in FP64
     double sr = fr[19 * me], sb = fb[19 * me];
     for (int d = 1; d < 19; d++) {

@@ -60,7 +60,6 @@ PS_DECL_PREC(0)
 PS_DECL_PREC(1)
 PS_DECL_PREC(2)
 PS_DECL_PREC(3)
-PS_DECL_PREC(4)
 #undef PS_DECL_PREC
 
 }  // namespace ps

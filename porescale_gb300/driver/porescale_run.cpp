@@ -15,7 +15,7 @@
 // LSM2S/Cxxxx/XX_P.f or LSM2S/Cyzyz/YZ_P.f: their INPUT_PARAMETERS, the
 // static solve, and their output files (run_lsm below).
 //
-// Options: -m lbm|xx|yz (default lbm), -p f64|f32|f16|bf16|f16c (population
+// Options: -m lbm|xx|yz (default lbm), -p f64|f32|f16|bf16 (population
 // storage, default f64, the reference's arithmetic) or f64|mixed (spring
 // solve), -d DIR (run directory, default .), -q (quiet).
 #include <sys/stat.h>
@@ -425,7 +425,7 @@ int main(int argc, char** argv)
     } else if (s == "-q") {
       quiet = true;
     } else {
-      die("usage: porescale_run [-d DIR] [-m lbm|xx|yz] [-p f64|f32|f16|bf16|f16c (lbm) | f64|mixed (xx, yz)] [-q]");
+      die("usage: porescale_run [-d DIR] [-m lbm|xx|yz] [-p f64|f32|f16|bf16 (lbm) | f64|mixed (xx, yz)] [-q]");
     }
   }
   if (lsm_load >= 0) {
@@ -433,7 +433,7 @@ int main(int argc, char** argv)
     if (lp < 0) die("unknown spring-solve precision " + pname);
     return run_lsm(lsm_load, lp, quiet);
   }
-  prec = pname == "f64" ? PS_PREC_F64 : pname == "f32" ? PS_PREC_F32 : pname == "f16" ? PS_PREC_F16 : pname == "bf16" ? PS_PREC_BF16 : pname == "f16c" ? PS_PREC_F16C : -1;
+  prec = pname == "f64" ? PS_PREC_F64 : pname == "f32" ? PS_PREC_F32 : pname == "f16" ? PS_PREC_F16 : pname == "bf16" ? PS_PREC_BF16 : -1;
   if (prec < 0) die("unknown precision " + pname);
   const Input in = read_input();
   if (in.mtype != 0) die("mtype = 1 (interpolation rule) is not supported: the reference's own path is dead code");
@@ -500,7 +500,7 @@ int main(int argc, char** argv)
     std::fprintf(f, " Lattice Boltzmann algorithm parameters\n interface width parameter B = %.16E\n", in.B);
     std::fprintf(f, " direction of the body force idir = %d\n number of steps in the main loop itm = %d\n", in.idir, in.itm);
     std::fprintf(f, " number of steps in the inner loop itw = %d\n population storage = %s\n", in.itw,
-                 prec == PS_PREC_F64 ? "f64" : prec == PS_PREC_F32 ? "f32" : prec == PS_PREC_F16 ? "f16" : prec == PS_PREC_BF16 ? "bf16" : "f16c");
+                 prec == PS_PREC_F64 ? "f64" : prec == PS_PREC_F32 ? "f32" : prec == PS_PREC_F16 ? "f16" : "bf16");
     std::fclose(f);
   }
   check(ps_lbm_step(h, 2), "ps_lbm_step (initialisation)");  // S1:3454-3621

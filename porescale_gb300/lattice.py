@@ -38,7 +38,7 @@ class Lattice:
     ----------
     params : LbmParams (see :func:`make_params`)
     ind : int array [nz, ny, nx] with the reference's ``ind`` values
-    precision : PREC_F64 / PREC_F32 / PREC_F16 / PREC_BF16 / PREC_F16C
+    precision : PREC_F64 / PREC_F32 / PREC_F16 / PREC_BF16
     """
 
     def __init__(self, params: LbmParams, ind: np.ndarray, precision: int = _lib.PREC_F64):

@@ -5,7 +5,7 @@ individual steps; the autotuner restores the states it times on."""
 import numpy as np
 import pytest
 
-from porescale_gb300 import PREC_BF16, PREC_F16, PREC_F16C, PREC_F32, PREC_F64, Lattice, LatticeBatch
+from porescale_gb300 import PREC_BF16, PREC_F16, PREC_F32, PREC_F64, Lattice, LatticeBatch
 from porescale_gb300 import geometry as geo
 from porescale_gb300.lattice import make_params
 
@@ -28,7 +28,7 @@ def _lattices(prec):
     return out
 
 
-@pytest.mark.parametrize("prec", [PREC_F64, PREC_F32, PREC_F16, PREC_BF16, PREC_F16C])
+@pytest.mark.parametrize("prec", [PREC_F64, PREC_F32, PREC_F16, PREC_BF16])
 def test_batch_matches_individual_lattices(gpu, prec):
     solo, grouped = _lattices(prec), _lattices(prec)
     with LatticeBatch(grouped) as B:

@@ -4,7 +4,7 @@ calc_ab's alpha / beta (S1:4008-4468)."""
 import numpy as np
 import pytest
 
-from porescale_gb300 import PREC_BF16, PREC_F16, PREC_F16C, PREC_F32, PREC_F64, Lattice
+from porescale_gb300 import PREC_BF16, PREC_F16, PREC_F32, PREC_F64, Lattice
 from porescale_gb300 import geometry as geo
 from porescale_gb300.lattice import make_params
 from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, LSM_MIXED, SpringNetwork
@@ -39,7 +39,7 @@ def test_wall_load_f64_bit_exact(gpu, oracle_lib):
     assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("prec,rtol", [(PREC_F32, 1e-4), (PREC_F16, 2e-2), (PREC_BF16, 1e-1), (PREC_F16C, 2e-2)])
+@pytest.mark.parametrize("prec,rtol", [(PREC_F32, 1e-4), (PREC_F16, 2e-2), (PREC_BF16, 1e-1)])
 def test_wall_load_low_precision(gpu, oracle_lib, prec, rtol):
     """One step from the same state: the load of the 32/16-bit forms within
     rtol of the largest nodal load.  q = f - 0.99 fq is a difference of two
