@@ -53,7 +53,6 @@ struct Lattice {
   void* d_col = nullptr;  // colour field of the step kernels (R per voxel)
   void* d_pop[2] = {nullptr, nullptr};    // per buffer: 19 x pitch (red, blue) pairs
   float2* d_rho[2] = {nullptr, nullptr};  // per buffer: (red, blue) reference densities
-  LbmConst<double>* d_Kd = nullptr;
   double *d_fr = nullptr, *d_fb = nullptr;                       // state staging (reference layout)
   double *d_rr = nullptr, *d_rb = nullptr, *d_cf = nullptr, *d_cc = nullptr;  // dense fields
   double* d_partial = nullptr;
@@ -107,7 +106,6 @@ struct Lattice {
   {
     LbmLaunchArgs a;
     a.K = prec == 0 ? (const void*)&Kd : (const void*)&Kf;
-    a.Kd_dev = d_Kd;
     a.G = geom();
     a.src = buf(src);
     a.dst = buf(dst);
@@ -149,7 +147,6 @@ void free_lattice(Lattice* L)
     cudaFree(L->d_pop[b]);
     cudaFree(L->d_rho[b]);
   }
-  cudaFree(L->d_Kd);
   cudaFree(L->d_fr);
   cudaFree(L->d_fb);
   cudaFree(L->d_rr);
@@ -771,8 +768,6 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
       PS_CUDA(cudaMemsetAsync(L->d_rho[b], 0, sizeof(float2) * pitch, L->stream));
     }
   }
-  if (int r = dalloc(L.get(), &L->d_Kd, sizeof(LbmConst<double>))) return r;
-  PS_CUDA(cudaMemcpyAsync(L->d_Kd, &L->Kd, sizeof(LbmConst<double>), cudaMemcpyHostToDevice, L->stream));
   default_config(L.get());
   PS_CUDA(cudaStreamSynchronize(L->stream));
   *handle = L.release();

@@ -719,78 +719,79 @@ constexpr int kObsN = 40;  // per-block partial sums
 template <int PREC>
 __global__ void __launch_bounds__(256) k_lbm_obs(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                  const __grid_constant__ GeomDev G, const BufDev src,
-                                                 const double* cc, const LbmConst<double>* Kd, double* partial)
+                                                 const double* cc, double* partial)
 {
   using R = typename Store<PREC>::R;
   __shared__ double red[kObsN][8];
   double acc[kObsN];
 #pragma unroll
   for (int i = 0; i < kObsN; i++) acc[i] = 0.0;
-  const LbmConst<double>& D = *Kd;
+  // per-node quantities in the lattice's arithmetic type (FP64 for the FP64
+  // lattice, whose observables follow the reference; FP32 for the others,
+  // whose populations carry no more), sums over the nodes in FP64
+  using A = R;
+  const LbmConst<A>& D = K;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.nl;
        i += (long long)gridDim.x * blockDim.x) {
     const uint32_t cw = G.coord[i], m = G.mask[i];
-    R fR[38];
-    read_node<PREC>(K, G, src, (int)i, fR);
+    A f[38];
+    read_node<PREC>(K, G, src, (int)i, f);
     int x, y, z;
     unpack(cw, x, y, z);
-    double f[38];
-#pragma unroll
-    for (int d = 0; d < 38; d++) f[d] = (double)fR[d];
-    double rr = f[0], rb = f[19];
+    A rr = f[0], rb = f[19];
     for (int d = 1; d < 19; d++) {
       rr = rr + f[d];
       rb = rb + f[19 + d];
     }
-    const double cf = (rr - rb) / (rr + rb);
-    acc[0] += rr;
-    acc[1] += rb;
-    acc[2] += rr + rb;
-    if (cf > 0.99) {
+    const A cf = (rr - rb) / (rr + rb);
+    acc[0] += (double)rr;
+    acc[1] += (double)rb;
+    acc[2] += (double)(rr + rb);
+    if (cf > A(0.99)) {
       acc[5] += 1.0;
-      acc[3] += rr;
-    } else if (cf < -0.99) {
+      acc[3] += (double)rr;
+    } else if (cf < A(-0.99)) {
       acc[6] += 1.0;
-      acc[4] += rb;
+      acc[4] += (double)rb;
     }
     bool neg = false;
-    for (int d = 0; d < 38; d++) neg |= f[d] < 0.0;
+    for (int d = 0; d < 38; d++) neg |= f[d] < A(0);
     if (neg) acc[36] = 1.0;
-    if (rr < 0.0) acc[37] += 1.0;
-    if (rb < 0.0) acc[38] += 1.0;
+    if (rr < A(0)) acc[37] += 1.0;
+    if (rb < A(0)) acc[38] += 1.0;
     // raw momenta with the reference's precedence (last term scaled by dti)
     for (int k = 0; k < 2; k++) {
-      const double* g = f + 19 * (1 - k);  // k = 0: blue (bmt), 1: red (rmt)
-      const double dti = D.dti;
-      double jx = g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14] * dti;
-      double jy = g[3] - g[4] + g[7] + g[8] - g[9] - g[10] + g[15] - g[16] + g[17] - g[18] * dti;
-      double jz = g[5] - g[6] + g[11] + g[12] - g[13] - g[14] + g[15] + g[16] - g[17] - g[18] * dti;
-      acc[30 + 3 * k] += jx;
-      acc[31 + 3 * k] += jy;
-      acc[32 + 3 * k] += jz;
+      const A* g = f + 19 * (1 - k);  // k = 0: blue (bmt), 1: red (rmt)
+      const A dti = D.dti;
+      const A jx = g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14] * dti;
+      const A jy = g[3] - g[4] + g[7] + g[8] - g[9] - g[10] + g[15] - g[16] + g[17] - g[18] * dti;
+      const A jz = g[5] - g[6] + g[11] + g[12] - g[13] - g[14] + g[15] + g[16] - g[17] - g[18] * dti;
+      acc[30 + 3 * k] += (double)jx;
+      acc[31 + 3 * k] += (double)jy;
+      acc[32 + 3 * k] += (double)jz;
     }
     const int nxy = G.nx * G.ny;
     const int v = x + G.nx * y + nxy * z;
     const NbOff o = nb_offsets(m, G.nx, nxy, nxy, G.nz);
-    auto ccf = [&](int a, int b, int c) -> double { return cc[v + o.x[a] + o.y[b] + o.z[c]]; };
-    double n[3], Fs[3];
+    auto ccf = [&](int a, int b, int c) -> A { return (A)cc[v + o.x[a] + o.y[b] + o.z[c]]; };
+    A n[3], Fs[3];
     csf_force(D, ccf, n, Fs);
-    double g[19];
+    A g[19];
     for (int d = 0; d < 19; d++) g[d] = f[d] + f[19 + d];
-    const double ri = 1.0 / (rr + rb);
+    const A ri = A(1) / (rr + rb);
     const int ph = rr >= rb ? 0 : 1;
-    double bfi[3];
-    for (int d = 0; d < 3; d++) bfi[d] = D.dt * (D.bf[ph][d] + Fs[d]) * 0.5;
-    const double jx = (g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14] + bfi[0]) * D.dti;
-    const double jy = (g[3] - g[4] + g[7] + g[8] - g[9] - g[10] + g[15] - g[16] + g[17] - g[18] + bfi[1]) * D.dti;
-    const double jz = (g[5] - g[6] + g[11] + g[12] - g[13] - g[14] + g[15] + g[16] - g[17] - g[18] + bfi[2]) * D.dti;
-    const double jm[3] = {jx, jy, jz};
+    A bfi[3];
+    for (int d = 0; d < 3; d++) bfi[d] = D.dt * (D.bf[ph][d] + Fs[d]) * A(0.5);
+    const A jx = (g[1] - g[2] + g[7] - g[8] + g[9] - g[10] + g[11] - g[12] + g[13] - g[14] + bfi[0]) * D.dti;
+    const A jy = (g[3] - g[4] + g[7] + g[8] - g[9] - g[10] + g[15] - g[16] + g[17] - g[18] + bfi[1]) * D.dti;
+    const A jz = (g[5] - g[6] + g[11] + g[12] - g[13] - g[14] + g[15] + g[16] - g[17] - g[18] + bfi[2]) * D.dti;
+    const A jm[3] = {jx, jy, jz};
     const int q = ph == 0 ? 9 : 12, uo = ph == 0 ? 18 : 21, to = ph == 0 ? 24 : 27;
     for (int d = 0; d < 3; d++) {
-      acc[q + d] += jm[d];
-      acc[15 + d] += jm[d] * ri;
-      acc[uo + d] += jm[d] * ri;
-      acc[to + d] += bfi[d];
+      acc[q + d] += (double)jm[d];
+      acc[15 + d] += (double)(jm[d] * ri);
+      acc[uo + d] += (double)(jm[d] * ri);
+      acc[to + d] += (double)bfi[d];
     }
     acc[ph == 0 ? 7 : 8] += 1.0;
   }

@@ -10,7 +10,6 @@ namespace ps {
 
 struct LbmLaunchArgs {
   const void* K;        // LbmConst<R> of the storage precision (host copy)
-  const LbmConst<double>* Kd_dev;  // FP64 constants in device memory
   GeomDev G;
   BufDev src, dst;
   void* cc;             // colour field (R per voxel) used by the step kernels

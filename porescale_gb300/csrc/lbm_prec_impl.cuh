@@ -176,8 +176,7 @@ template <int PREC>
 cudaError_t obs(const LbmLaunchArgs& a, const double* cc, double* partial, int nblocks, double* out)
 {
   using R = typename Store<PREC>::R;
-  k_lbm_obs<PREC><<<nblocks, 256, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K), a.G, a.src, cc, a.Kd_dev,
-                                                 partial);
+  k_lbm_obs<PREC><<<nblocks, 256, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K), a.G, a.src, cc, partial);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_obs_final<<<1, 64, 0, a.stream>>>(partial, nblocks, out);

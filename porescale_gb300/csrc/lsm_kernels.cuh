@@ -112,11 +112,15 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
             if (b == (e ^ 7)) continue;  // no spring couples opposite corners
             const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
             const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
-            const T u0 = p[nvb], u1 = p[nv + nvb], u2 = p[2 * nv + nvb];
+            const T u[3] = {p[nvb], p[nv + nvb], p[2 * nv + nvb]};
+            // FP64: the handle's K of material m; entries zero in both Ka
+            // and Kb (known at compile time) are skipped
 #pragma unroll
             for (int r = 0; r < 3; r++)
-              acc[r] += kval<T>(G, m - 1, 3 * e + r, 3 * b) * u0 + kval<T>(G, m - 1, 3 * e + r, 3 * b + 1) * u1 +
-                        kval<T>(G, m - 1, 3 * e + r, 3 * b + 2) * u2;
+#pragma unroll
+              for (int c = 0; c < 3; c++)
+                if (kKa[3 * e + r][3 * b + c] != 0.0 || kKb[3 * e + r][3 * b + c] != 0.0)
+                  acc[r] += kval<T>(G, m - 1, 3 * e + r, 3 * b + c) * u[c];
           }
         }
       }
