@@ -140,6 +140,23 @@ def load_traffic(prec: str, nl: int, kind: str = "two-pass"):
     return float(e["dram_bytes_per_fluid_node"]) * nl
 
 
+def max_over_ranks(t: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time (the whole job's time): all-reduce MAX over
+    the process group; the value itself with one rank."""
+    if world <= 1:
+        return t
+    import torch
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(units_per_rank: float, t_max: float, world: int) -> float:
+    """Whole-job throughput of a weak-scaled run: every rank processes the
+    same units (its own replica) and the job takes the slowest rank's time."""
+    return units_per_rank * world / t_max
+
+
 def time_steps(L, steps, warmup, torch):
     """Device time of `steps` step launches on the lattice's stream (CUDA events).
     Under the wavefront schedule the warm-up is whole 8-step graphs, so the
@@ -646,11 +663,8 @@ def main():
         t = time_steps(L, steps, args.warmup, torch)
         if sampler:
             clocks = sampler.stop()
-        if world > 1:
-            tt = torch.tensor([t], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t = float(tt.item())
-        mlups = nl * steps / t / 1e6 * world
+        t = max_over_ranks(t, world)
+        mlups = job_rate(nl * steps, t, world) / 1e6
         launch_s = t / steps
         achieved = nl * ALGO_BYTES[q] / launch_s / 1e9
         if q != "f64" and not args.no_autotune and not args.tile:
@@ -719,11 +733,8 @@ def main():
                 obs = L.observables()
                 L.get_state((ofr, ofb))
             te = time.perf_counter() - t0
-            if world > 1:
-                tt = torch.tensor([te], device="cuda")
-                torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-                te = float(tt.item())
-            res["e2e"] = {"value": nl * args.itw * args.e2e_steps / te / 1e6 * world, "unit": "MLUPS",
+            te = max_over_ranks(te, world)
+            res["e2e"] = {"value": job_rate(nl * args.itw * args.e2e_steps, te, world) / 1e6, "unit": "MLUPS",
                           "h2d_bytes_per_step": 2 * 19 * nl * 8, "d2h_bytes_per_step": 2 * 19 * nl * 8 + 8 * 40,
                           "steps_per_e2e_step": args.itw, "e2e_steps": args.e2e_steps,
                           "permr": obs.permr, "permb": obs.permb}
