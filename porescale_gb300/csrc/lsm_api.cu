@@ -13,10 +13,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "lsm_cube.h"
@@ -469,6 +472,45 @@ int finish(Springs* S, double bb, double rtol, ps_lsm_result* out)
   return PS_OK;
 }
 
+// Runs f(s) for every network s = 0..n-1 on up to 8 host threads (each
+// network has its own stream, so the per-network launches and waits of the
+// refinement overlap instead of queueing behind one another); returns the
+// first error code, its message moved to the calling thread.
+template <typename F>
+int each_network(int n, F f)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int> next{0};
+  std::mutex mu;
+  int err = PS_OK;
+  std::string msg;
+  auto work = [&]() {
+    cudaSetDevice(dev);
+    for (int s = next++; s < n; s = next++) {
+      {
+        std::lock_guard<std::mutex> g(mu);
+        if (err) return;
+      }
+      const int e = f(s);
+      if (e) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!err) {
+          err = e;
+          msg = last_error();
+        }
+        return;
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < std::min(n, 8); t++) th.emplace_back(work);
+  work();
+  for (std::thread& t : th) t.join();
+  if (err) last_error() = msg;
+  return err;
+}
+
 // ---- batched CG over several networks ---------------------------------------
 // CG on A x = r0 (x = 0, p = r0 set by the caller) for every network of the
 // list at once: the iteration of cg<T> with each kernel launched once for
@@ -887,20 +929,19 @@ int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t max
     memset(out + s, 0, sizeof(ps_lsm_result));
   }
   std::vector<double> bb((size_t)n, 0.0);
-  for (int s = 0; s < n; s++)
-    if (int e = prepare(sys[s], &bb[s])) return e;
+  if (int e = each_network(n, [&](int s) { return prepare(sys[s], &bb[s]); })) return e;
   cudaStream_t st = nullptr;
   PS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   int rc = PS_OK;
   if (sys[0]->p.precision == PS_LSM_F64) {
-    for (int s = 0; s < n && rc == PS_OK; s++) {
+    rc = each_network(n, [&](int s) {
       Springs* S = sys[s];
       const size_t b3 = sizeof(double) * 3 * (size_t)S->nvox;
       cudaError_t e = cudaMemcpyAsync(S->r, S->b, b3, cudaMemcpyDeviceToDevice, S->stream);
       if (e == cudaSuccess) e = cudaMemcpyAsync(S->p64, S->b, b3, cudaMemcpyDeviceToDevice, S->stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
-      if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
-    }
+      return e == cudaSuccess ? PS_OK : cuda_fail(e, "ps_lsm_batch_solve");
+    });
     if (rc == PS_OK) rc = batch_cg<double>(sys, rtol, maxit, st);
     for (int s = 0; s < n && rc == PS_OK; s++) {
       double h8[8];
@@ -912,45 +953,58 @@ int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t max
     // networks that have not reached rtol
     std::vector<int> rounds((size_t)n, 0);
     long long budget = maxit;
+    std::vector<double> rn((size_t)n, 0.0);
+    std::vector<long long> its((size_t)n, 0);
     for (int round = 0; round < 60 && rc == PS_OK && budget > 0; round++) {
-      std::vector<Springs*> act;
-      std::vector<double> rns;
-      for (int s = 0; s < n && rc == PS_OK; s++) {
+      // residual of every network (round 0: r = b); those above rtol start
+      // an FP32 inner solve on r / |r|
+      std::vector<char> on((size_t)n, 0);
+      rc = each_network(n, [&](int s) {
         Springs* S = sys[s];
         const int n3 = 3 * S->nvox;
         double rn2 = 0.0;
         if (round == 0) {
           cudaError_t e = cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream);
-          if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
+          if (e != cudaSuccess) return cuda_fail(e, "ps_lsm_batch_solve");
           rn2 = bb[s];
-        } else if ((rc = residual(S, &rn2))) {
-          break;
+        } else if (int e = residual(S, &rn2)) {
+          return e;
         }
-        if (!(bb[s] > 0.0) || rn2 <= rtol * rtol * bb[s]) continue;
-        const double rn = std::sqrt(rn2);
-        k_ir_start<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, 1.0 / rn, S->r, S->r32, S->p32, S->x32);
+        if (!(bb[s] > 0.0) || rn2 <= rtol * rtol * bb[s]) return PS_OK;
+        rn[s] = std::sqrt(rn2);
+        k_ir_start<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, 1.0 / rn[s], S->r, S->r32, S->p32, S->x32);
         cudaError_t e = cudaStreamSynchronize(S->stream);
-        if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
-        act.push_back(S);
-        rns.push_back(rn);
-        rounds[s]++;
-      }
+        if (e != cudaSuccess) return cuda_fail(e, "ps_lsm_batch_solve");
+        on[s] = 1;
+        return PS_OK;
+      });
+      std::vector<Springs*> act;
+      std::vector<int> idx;
+      for (int s = 0; s < n; s++)
+        if (on[s]) {
+          act.push_back(sys[s]);
+          idx.push_back(s);
+          rounds[s]++;
+        }
       if (rc != PS_OK || act.empty()) break;
       if ((rc = batch_cg<float>(act, 1e-4, budget, st))) break;
-      long long most = 0;
-      for (size_t a = 0; a < act.size() && rc == PS_OK; a++) {
+      // x64 += |r| x32 for every network of the round
+      rc = each_network((int)act.size(), [&](int a) {
         Springs* S = act[a];
+        const int s = idx[a];
         double h8[8];
-        if ((rc = read_scal(S, h8, 8))) break;
-        const long long it = (long long)h8[7];
-        most = std::max(most, it);
-        const int si = (int)(std::find(sys.begin(), sys.end(), S) - sys.begin());
-        out[si].inner_iterations += it;
-        out[si].iterations++;
+        if (int e = read_scal(S, h8, 8)) return e;
+        its[s] = (long long)h8[7];
         const int n3 = 3 * S->nvox;
-        k_ir_update<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, rns[a], S->x32, S->x);
+        k_ir_update<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, rn[s], S->x32, S->x);
         cudaError_t e = cudaStreamSynchronize(S->stream);
-        if (e != cudaSuccess) rc = cuda_fail(e, "ps_lsm_batch_solve");
+        return e == cudaSuccess ? PS_OK : cuda_fail(e, "ps_lsm_batch_solve");
+      });
+      long long most = 0;
+      for (int s : idx) {
+        out[s].inner_iterations += its[s];
+        out[s].iterations++;
+        most = std::max(most, its[s]);
       }
       budget -= most;
     }
@@ -958,11 +1012,10 @@ int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t max
   }
   cudaStreamDestroy(st);
   if (rc != PS_OK) return rc;
+  if (int e = each_network(n, [&](int s) { return finish(sys[s], bb[s], rtol, out + s); })) return e;
   int bad = -1;
-  for (int s = 0; s < n; s++) {
-    if (int e = finish(sys[s], bb[s], rtol, out + s)) return e;
-    if (!out[s].converged && bad < 0) bad = s;
-  }
+  for (int s = 0; s < n && bad < 0; s++)
+    if (!out[s].converged) bad = s;
   return bad < 0 ? PS_OK
                  : fail(PS_ERR_NOTCONV, "ps_lsm_batch_solve: network %d at relative residual %.3e above %.3e", bad,
                         out[bad].relres, rtol);

@@ -207,6 +207,17 @@ def test_wave_schedule_matches_two_pass(gpu, prec, planes, window, tile):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
 
+def test_wave_schedule_without_fluid(gpu):
+    """A lattice with no fluid node: every slab launch is an empty graph node."""
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    with Lattice(p, np.zeros((6, 5, 4), np.int32), PREC_F16) as L:
+        L.set_wave(1)
+        L.init_random(0.5)
+        L.step(16)
+        o = L.observables()
+        assert o.tmr == 0.0 and o.tmb == 0.0
+
+
 def test_wave_and_fused_exclusive(gpu):
     ind = geo.sphere_pack((12, 12, 12), 0.45, 3.0, seed=3)
     p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
