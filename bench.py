@@ -128,13 +128,16 @@ def load_peaks():
 def load_traffic(prec: str, nl: int, kind: str = "two-pass"):
     """DRAM bytes of one step from the committed ncu summary (scaled to this
     workload's fluid-node count; key "<prec>" for the two-pass step,
-    "<prec>_fused" / "<prec>_wave" for the other schedules), or None."""
+    "<prec>_fused" / "<prec>_wave" for the other schedules, the two-pass
+    figure standing for the wavefront where it has none), or None."""
     path = os.path.join(ROOT, "profiles", "lbm_step_dram.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
     e = d.get(prec + ("" if kind == "two-pass" else "_" + kind))
+    if not e and kind == "wave":  # measured to move the two-pass step's bytes
+        e = d.get(prec)
     if not e:
         return None
     return float(e["dram_bytes_per_fluid_node"]) * nl

@@ -73,6 +73,10 @@ struct Lattice {
   int wave_key[5] = {0, 0, 0, 0, 0};  // (tx, ty, occ, planes, window) of wave_exec
   int obs_blocks = 0;
   int cur = 0;           // buffer holding the current state
+  // per buffer: 16-bit slots stored against the reading node's densities (a
+  // state set from outside; the first step reads it so, every step writes
+  // against the writing node's)
+  int recv[2] = {0, 0};
   bool have_state = false;
   int tx = 128, ty = 256, zchunk = 0;  // collide / density block sizes
   long long dev_bytes = 0;
@@ -100,6 +104,7 @@ struct Lattice {
     BufDev r;
     r.pop = d_pop[b];
     r.rho = d_rho[b];
+    r.recv = recv[b];
     return r;
   }
   LbmLaunchArgs args(int src, int dst) const
@@ -114,6 +119,12 @@ struct Lattice {
     return a;
   }
   size_t elem() const { return prec == 0 ? 8 : (prec == 1 ? 4 : 2); }
+  // bytes of one buffer's densities: per compact node (FP32 deviations), per
+  // voxel of the box (16-bit, sender reference), none (FP64)
+  size_t rho_bytes() const
+  {
+    return prec == 0 ? 0 : sizeof(float2) * (size_t)std::max(64LL, prec >= 2 ? nvox : pitch);
+  }
   // plane stride of the step colour field: whole 128-byte lines per plane
   int cplane() const { return (nx * ny + 31) / 32 * 32; }
 };
@@ -453,9 +464,10 @@ int ensure_wave(Lattice* L)
   std::vector<int> first(S + 1);
   for (int k = 0; k <= S; k++) first[k] = L->rowstart_h[(size_t)std::min(L->nz, k * P) * L->ny];
   LbmLaunchArgs a[kWaveSteps];
-  for (int s = 0; s < kWaveSteps; s++) {
+  for (int s = 0; s < kWaveSteps; s++) {  // graphs start after a step (no recv buffer)
     const int b = L->cur ^ (s & 1);
     a[s] = L->args(b, 1 - b);
+    a[s].src.recv = a[s].dst.recv = 0;
   }
   cudaGraph_t g = nullptr;
   cudaError_t e = PREC_DISPATCH(lbm_wave_graph, L->prec, L->tx, L->ty, L->zchunk, a, kWaveSteps, first.data(), S,
@@ -475,12 +487,23 @@ int launch_steps(Lattice* L, int n)
   if (L->fused_planes > 0)
     if (int r = ensure_schedule(L)) return r;
   int done = 0;
-  if (L->wave_planes > 0 && n >= kWaveSteps) {
+  if (n > 0 && L->recv[L->cur]) {  // a state set from outside: one two-pass step reads it
+    LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
+    a.dst.recv = 0;
+    cudaError_t e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, L->zchunk, a);
+    if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
+    L->recv[1 - L->cur] = 0;
+    L->cur = 1 - L->cur;
+    done = 1;
+  }
+  if (L->wave_planes > 0 && n - done >= kWaveSteps) {
     if (int r = ensure_wave(L)) return r;
     for (; n - done >= kWaveSteps; done += kWaveSteps) PS_CUDA(cudaGraphLaunch(L->wave_exec[L->cur], L->stream));
+    L->recv[0] = L->recv[1] = 0;
   }
   for (int s = done; s < n; s++) {
     LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
+    a.dst.recv = 0;
     cudaError_t e;
     if (L->fused_planes > 0) {
       FusedArgs f;
@@ -495,6 +518,7 @@ int launch_steps(Lattice* L, int n)
       e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, L->zchunk, a);
     }
     if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
+    L->recv[1 - L->cur] = 0;
     L->cur = 1 - L->cur;
   }
   return PS_OK;
@@ -586,7 +610,9 @@ int batch_tiles(Batch* B)
 }
 
 // descriptor table of one step in which lattice v reads buffer cur_v ^ flip
-VolTable batch_table(const Batch* B, int flip)
+// (recv flags as the lattices hold them only when `first`: every later step
+// reads buffers that a step wrote)
+VolTable batch_table(const Batch* B, int flip, bool first = false)
 {
   VolTable T;
   memset(&T, 0, sizeof T);
@@ -596,6 +622,8 @@ VolTable batch_table(const Batch* B, int flip)
     T.v[v].G = L->geom();
     T.v[v].src = L->buf(c);
     T.v[v].dst = L->buf(c ^ 1);
+    T.v[v].dst.recv = 0;
+    if (!first) T.v[v].src.recv = 0;
     T.v[v].cc = L->d_col;
   }
   return T;
@@ -619,6 +647,17 @@ cudaError_t batch_launch(Batch* B, const VolTable& T)
 int batch_steps(Batch* B, int n)
 {
   if (int r = batch_tiles(B)) return r;
+  bool recv = false;
+  for (Lattice* L : B->L) recv = recv || L->recv[L->cur];
+  if (n > 0 && recv) {  // states set from outside: one direct step reads them
+    cudaError_t e = batch_launch(B, batch_table(B, 0, true));
+    if (e != cudaSuccess) return cuda_fail(e, "batch step");
+    for (Lattice* L : B->L) {
+      L->recv[L->cur ^ 1] = 0;
+      L->cur ^= 1;
+    }
+    n--;
+  }
   std::vector<int> cur;
   for (Lattice* L : B->L) cur.push_back(L->cur);
   const bool valid = B->exec && B->g_tx == B->tx && B->g_ty == B->ty && B->g_occ == B->occ && B->graph_cur == cur;
@@ -659,7 +698,10 @@ int batch_steps(Batch* B, int n)
     cudaError_t e = batch_launch(B, batch_table(B, done & 1));
     if (e != cudaSuccess) return cuda_fail(e, "batch step");
   }
-  for (Lattice* L : B->L) L->cur ^= (n & 1);
+  for (Lattice* L : B->L) {
+    if (n > 0) L->recv[0] = L->recv[1] = 0;
+    L->cur ^= (n & 1);
+  }
   return PS_OK;
 }
 
@@ -764,8 +806,8 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
     if (int r = dalloc(L.get(), &L->d_pop[b], popb)) return r;
     PS_CUDA(cudaMemsetAsync(L->d_pop[b], 0, popb, L->stream));
     if (precision >= 1) {  // deviation storage: the reference densities
-      if (int r = dalloc(L.get(), &L->d_rho[b], sizeof(float2) * pitch)) return r;
-      PS_CUDA(cudaMemsetAsync(L->d_rho[b], 0, sizeof(float2) * pitch, L->stream));
+      if (int r = dalloc(L.get(), &L->d_rho[b], L->rho_bytes())) return r;
+      PS_CUDA(cudaMemsetAsync(L->d_rho[b], 0, L->rho_bytes(), L->stream));
     }
   }
   default_config(L.get());
@@ -899,6 +941,7 @@ int ps_lbm_set_state(void* h, const double* fr, const double* fb)
   LbmLaunchArgs a = L->args(L->cur, L->cur);
   cudaError_t e = PREC_DISPATCH(lbm_set_state_launch, L->prec, a, L->d_fr, L->d_fb);
   if (e != cudaSuccess) return cuda_fail(e, "set_state kernel");
+  L->recv[L->cur] = L->prec >= 2 ? 1 : 0;  // 16-bit storage is read against the writer's densities
   L->have_state = true;
   PS_CUDA(cudaStreamSynchronize(L->stream));
   return PS_OK;
@@ -1110,13 +1153,14 @@ int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, 
   // save every lattice's current buffer (populations and reference densities)
   std::vector<void*> sp(nv, nullptr);
   std::vector<float2*> sr(nv, nullptr);
-  std::vector<int> cur(nv);
+  std::vector<int> cur(nv), rcv(nv);
   auto popb = [&](const Lattice* L) { return 2 * L->elem() * 19 * (size_t)std::max(64LL, L->pitch); };
-  auto rhob = [&](const Lattice* L) { return sizeof(float2) * (size_t)std::max(64LL, L->pitch); };
+  auto rhob = [&](const Lattice* L) { return L->rho_bytes(); };
   int rc = PS_OK;
   for (size_t v = 0; v < nv && rc == PS_OK; v++) {
     Lattice* L = B->L[v];
     cur[v] = L->cur;
+    rcv[v] = L->recv[L->cur];
     cudaError_t e = cudaMalloc(&sp[v], popb(L));
     if (e == cudaSuccess) e = cudaMemcpyAsync(sp[v], L->d_pop[L->cur], popb(L), cudaMemcpyDeviceToDevice, B->stream);
     if (e == cudaSuccess && L->prec >= 1) e = cudaMalloc((void**)&sr[v], rhob(L));
@@ -1157,6 +1201,7 @@ int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, 
   for (size_t v = 0; v < nv; v++) {  // restore
     Lattice* L = B->L[v];
     L->cur = cur[v];
+    L->recv[L->cur] = rcv[v];
     if (sp[v]) cudaMemcpyAsync(L->d_pop[L->cur], sp[v], popb(L), cudaMemcpyDeviceToDevice, B->stream);
     if (sr[v]) cudaMemcpyAsync(L->d_rho[L->cur], sr[v], rhob(L), cudaMemcpyDeviceToDevice, B->stream);
   }
@@ -1234,7 +1279,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   // configurations; the state is restored afterwards from a saved copy of
   // the current buffer
   const size_t popb = 2 * L->elem() * 19 * (size_t)std::max(64LL, L->pitch);
-  const size_t rhob = sizeof(float2) * (size_t)std::max(64LL, L->pitch);
+  const size_t rhob = L->rho_bytes();
   void* save = nullptr;
   float2* saver = nullptr;
   PS_CUDA(cudaMalloc(&save, popb));
@@ -1261,7 +1306,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   cudaEventCreate(&e1);
   float best = 1e30f;
   Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead, L->wave_planes, L->wave_window};
-  const int saved_cur = L->cur;
+  const int saved_cur = L->cur, saved_recv[2] = {L->recv[0], L->recv[1]};
   int rc = PS_OK;
   for (const Cfg& c : cand) {
     L->tx = c.tx;
@@ -1293,6 +1338,8 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   cudaEventDestroy(e1);
   // restore the state
   L->cur = saved_cur;
+  L->recv[0] = saved_recv[0];
+  L->recv[1] = saved_recv[1];
   cudaMemcpyAsync(L->d_pop[L->cur], save, popb, cudaMemcpyDeviceToDevice, L->stream);
   if (saver) cudaMemcpyAsync(L->d_rho[L->cur], saver, rhob, cudaMemcpyDeviceToDevice, L->stream);
   cudaStreamSynchronize(L->stream);

@@ -99,10 +99,14 @@ struct GeomDev {
 };
 
 // one population buffer: pop -> 19*pitch (red, blue) pairs, rho -> pitch
-// (red, blue) FP32 reference densities (16-bit storage only)
+// (red, blue) FP32 densities of the nodes (deviation storage).  recv: the
+// 16-bit slots hold deviations from the READING node's densities (a state
+// given from outside, whose populations are consistent with each node's own
+// densities); steps always write deviations from the writing node's.
 struct BufDev {
   void* pop;
-  float2* rho;  // (red, blue) reference densities (deviation storage)
+  float2* rho;
+  int recv;
 };
 
 // ---- storage policies ----------------------------------------------------
@@ -113,28 +117,28 @@ struct Store<0> {  // FP64
   using T = double;
   using T2 = double2;
   using R = double;
-  static constexpr bool kDev = false;
+  static constexpr bool kDev = false, kSendRef = false;
 };
 template <>
-struct Store<1> {  // FP32 deviation
+struct Store<1> {  // FP32 deviation (receiver reference)
   using T = float;
   using T2 = float2;
   using R = float;
-  static constexpr bool kDev = true;
+  static constexpr bool kDev = true, kSendRef = false;
 };
 template <>
-struct Store<2> {  // FP16 deviation
+struct Store<2> {  // FP16 deviation (sender reference)
   using T = __half;
   using T2 = __half2;
   using R = float;
-  static constexpr bool kDev = true;
+  static constexpr bool kDev = true, kSendRef = true;
 };
 template <>
-struct Store<3> {  // BF16 deviation
+struct Store<3> {  // BF16 deviation (sender reference)
   using T = __nv_bfloat16;
   using T2 = __nv_bfloat162;
   using R = float;
-  static constexpr bool kDev = true;
+  static constexpr bool kDev = true, kSendRef = true;
 };
 
 // FP16 deviations are stored scaled by 2^10 to keep them in the normal range
@@ -293,18 +297,6 @@ __device__ __forceinline__ void pull_sources(const GeomDev& G, int i, uint32_t c
   }
 }
 
-// The 19 post-streaming populations of both components of node i from its
-// own slots: f[0..18] red, f[19..37] blue.
-template <int PREC>
-__device__ __forceinline__ void read_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& src, int i, typename Store<PREC>::R* f)
-{
-  float2 rho = make_float2(0.f, 0.f);
-  if constexpr (Store<PREC>::kDev) rho = __ldg(src.rho + i);
-#pragma unroll
-  for (int d = 0; d < 19; d++) Pop<PREC>::load(K, src, d, i, G.pitch, rho, f[d], f[19 + d]);
-}
-
 // Writes the 19 post-collision (red, blue) populations of node i to their
 // receivers (push streaming with half-way bounce-back).  s[] are the pull
 // sources of node i (pull_sources): the receiver of an outgoing population
@@ -319,19 +311,23 @@ __device__ __forceinline__ T ld_step(const T* p, bool coherent)
 
 template <int PREC, bool kCoh = false>
 __device__ __forceinline__ void push_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& dst, int i, uint32_t m, const int* s,
+                                          const BufDev& dst, int i, long long ri, uint32_t m, const int* s,
                                           const typename Store<PREC>::R* outr, const typename Store<PREC>::R* outb)
 {
-  constexpr bool kDev = Store<PREC>::kDev;
+  constexpr bool kDev = Store<PREC>::kDev, kSend = Store<PREC>::kSendRef;
   const float2 zero = make_float2(0.f, 0.f);
-  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], kDev ? ld_step(dst.rho + i, kCoh) : zero);
+  // ri: node i's entry in rho.  Sender reference: every population against
+  // node i's own densities; otherwise against each receiver's.
+  const float2 own = kDev ? ld_step(dst.rho + ri, kCoh) : zero;
+  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], own);
 #pragma unroll
   for (int e = 1; e < 19; e++) {
     const int oe = opp(e);
     const bool stream = m & (1u << (oe - 1));
     const int node = stream ? s[oe] : i;
     const int slot = stream ? e : oe;
-    Pop<PREC>::put(K, dst, slot, node, G.pitch, outr[e], outb[e], kDev ? ld_step(dst.rho + node, kCoh) : zero);
+    Pop<PREC>::put(K, dst, slot, node, G.pitch, outr[e], outb[e],
+                   kDev && !kSend ? ld_step(dst.rho + node, kCoh) : own);
   }
 }
 
@@ -413,6 +409,87 @@ __device__ __forceinline__ NbOff nb_offsets(uint32_t m, int nx, int nxy, int zs,
   return o;
 }
 
+// Sender-reference storage (16-bit): slot (d, i) was written by the node at
+// x - c_d when the incoming link d is open, else (rest population,
+// half-way bounce-back) by node i itself; its deviation is taken from the
+// writer's densities at that step, which the writer stored in the same
+// buffer's rho.  Those densities live on the dense voxel box (v = voxel of
+// node i, o its neighbour offsets), so each writer is a fixed offset away.
+// src.recv: every slot against node i's own densities.  f[0..18] red,
+// f[19..37] blue.
+template <int PREC>
+__device__ __forceinline__ void read_node_s(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                            const BufDev& src, int i, uint32_t m, long long v, const NbOff& o,
+                                            typename Store<PREC>::R* f)
+{
+  const float2* rv = src.rho + v;
+  const float2 own = __ldg(rv);
+  const uint32_t wm = src.recv ? 0u : m;  // links whose slot another node wrote
+  Pop<PREC>::load(K, src, 0, i, G.pitch, own, f[0], f[19]);
+#pragma unroll
+  for (int d = 1; d < 19; d++) {
+    const int off = (wm & (1u << (d - 1))) ? o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : 0;
+    Pop<PREC>::load(K, src, d, i, G.pitch, __ldg(rv + off), f[d], f[19 + d]);
+  }
+}
+
+// The (red, blue) densities of node i under sender-reference storage,
+// summed on the fly (sum of the stored deviations plus sum of t_d times the
+// writers' densities) without holding the 38 populations
+template <int PREC>
+__device__ __forceinline__ float2 densities_s(const LbmConst<float>& K, const GeomDev& G, const BufDev& src, int i,
+                                              uint32_t m, long long v, const NbOff& o)
+{
+  using T = typename Store<PREC>::T;
+  using T2 = typename Store<PREC>::T2;
+  const float2* rv = src.rho + v;
+  const float2 own = __ldg(rv);
+  const uint32_t wm = src.recv ? 0u : m;  // links whose slot another node wrote
+  const T2* p = static_cast<const T2*>(src.pop) + i;
+  // the stored values summed unscaled, then scaled once (a power of two:
+  // the same result as scaling each term)
+  float2 g = to_f2(p[0]);
+  float sr = g.x, sb = g.y, wr = K.t[0][0] * own.x, wb = K.t[1][0] * own.y;
+#pragma unroll
+  for (int d = 1; d < 19; d++) {
+    const int off = (wm & (1u << (d - 1))) ? o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : 0;
+    const float2 rw = __ldg(rv + off);
+    g = to_f2(p[(long long)d * G.pitch]);
+    sr = sr + g.x;
+    sb = sb + g.y;
+    wr = wr + K.t[0][wcls(d)] * rw.x;
+    wb = wb + K.t[1][wcls(d)] * rw.y;
+  }
+  return make_float2(wr + sr * DevScale<T>::down, wb + sb * DevScale<T>::down);
+}
+__device__ __forceinline__ long long voxel_of(const GeomDev& G, uint32_t c)
+{
+  int x, y, z;
+  unpack(c, x, y, z);
+  return x + (long long)G.nx * (y + (long long)G.ny * z);
+}
+__device__ __forceinline__ NbOff box_offsets(const GeomDev& G, uint32_t m)
+{
+  return nb_offsets(m, G.nx, G.nx * G.ny, G.nx * G.ny, G.nz);
+}
+
+// The 19 post-streaming populations of both components of node i from its
+// own slots: f[0..18] red, f[19..37] blue.
+template <int PREC>
+__device__ __forceinline__ void read_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, int i, typename Store<PREC>::R* f)
+{
+  if constexpr (Store<PREC>::kSendRef) {
+    const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+    read_node_s<PREC>(K, G, src, i, m, voxel_of(G, c), box_offsets(G, m), f);
+  } else {
+    float2 rho = make_float2(0.f, 0.f);
+    if constexpr (Store<PREC>::kDev) rho = __ldg(src.rho + i);
+#pragma unroll
+    for (int d = 0; d < 19; d++) Pop<PREC>::load(K, src, d, i, G.pitch, rho, f[d], f[19 + d]);
+  }
+}
+
 // ---- step kernels ---------------------------------------------------------
 // per-node bodies, shared by the single-lattice and the batched kernels
 
@@ -424,7 +501,15 @@ __device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R
 {
   using R = typename Store<PREC>::R;
   R rr, rb;
-  if constexpr (Store<PREC>::kDev) {
+  const uint32_t c = __ldg(G.coord + i);
+  if constexpr (Store<PREC>::kSendRef) {
+    const uint32_t m = __ldg(G.mask + i);
+    const long long v = voxel_of(G, c);
+    const float2 r2 = densities_s<PREC>(K, G, src, i, m, v, box_offsets(G, m));
+    rr = r2.x;
+    rb = r2.y;
+    dst.rho[v] = r2;
+  } else if constexpr (Store<PREC>::kDev) {
     float gr[19], gb[19];
     const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
     R sr = gr[0], sb = gb[0];
@@ -442,7 +527,7 @@ __device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R
     densities(f, rr, rb);
   }
   int x, y, z;
-  unpack(__ldg(G.coord + i), x, y, z);
+  unpack(c, x, y, z);
   cc[x + G.nx * y + G.cplane * z] = stencil_colour(rr, rb, K.wet);
 }
 
@@ -480,14 +565,20 @@ __device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R
     push_node_dev<PREC, kCoh>(K, G, dst, i, m, s, Sr, Sb, Zr, Zb, rn);
   } else {
     R f[38];
-    read_node<PREC>(K, G, src, i, f);
+    long long ri = i;  // node i's entry in rho
+    if constexpr (Store<PREC>::kSendRef) {
+      ri = x + (long long)G.nx * (y + (long long)G.ny * z);
+      read_node_s<PREC>(K, G, src, i, m, ri, box_offsets(G, m), f);
+    } else {
+      read_node<PREC>(K, G, src, i, f);
+    }
     R rr, rb;
     densities(f, rr, rb);
     R outr[19], outb[19];
     node_update(K, f, f + 19, rr, rb, col, outr, outb);
     int s[19];
     pull_sources(G, i, c, m, s);
-    push_node<PREC, kCoh>(K, G, dst, i, m, s, outr, outb);
+    push_node<PREC, kCoh>(K, G, dst, i, ri, m, s, outr, outb);
   }
 }
 
@@ -662,7 +753,20 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nl) return;
   const long long r = G.ref[i];
-  if constexpr (Store<PREC>::kDev) {  // decode t_d rho + g in FP64
+  if constexpr (Store<PREC>::kSendRef) {  // decode t_d rho_writer + g in FP64
+    const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+    const long long v = voxel_of(G, c);
+    const NbOff o = box_offsets(G, m);
+#pragma unroll
+    for (int d = 0; d < 19; d++) {
+      const bool wr = !src.recv && d > 0 && (m & (1u << (d - 1)));  // written by another node
+      const float2 rw = __ldg(src.rho + (wr ? v + o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : v));
+      R gr, gb;
+      Pop<PREC>::load_dev(src, d, i, G.pitch, gr, gb);
+      fr[19 * r + d] = (double)K.t[0][wcls(d)] * (double)rw.x + (double)gr;
+      fb[19 * r + d] = (double)K.t[1][wcls(d)] * (double)rw.y + (double)gb;
+    }
+  } else if constexpr (Store<PREC>::kDev) {  // decode t_d rho + g in FP64
     float gr[19], gb[19];
     const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
 #pragma unroll
@@ -682,7 +786,8 @@ __global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<
 }
 
 // post-streaming populations fr, fb (reference layout) into the node's own
-// slots; 16-bit storage takes the node's own densities as the reference
+// slots; deviation storage takes the node's own densities as the reference
+// (for sender-reference storage the buffer is then marked recv)
 template <int PREC>
 __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                 const __grid_constant__ GeomDev G, const BufDev dst, const double* fr,
@@ -701,7 +806,7 @@ __global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<
       sb += fb[19 * me + d];
     }
     const float2 rho = make_float2((float)sr, (float)sb);
-    dst.rho[i] = rho;
+    dst.rho[S::kSendRef ? voxel_of(G, G.coord[i]) : (long long)i] = rho;
     for (int d = 0; d < 19; d++)
       Pop<PREC>::put_dev(dst, d, i, G.pitch, (R)(fr[19 * me + d] - (double)K.t[0][wcls(d)] * (double)rho.x),
                          (R)(fb[19 * me + d] - (double)K.t[1][wcls(d)] * (double)rho.y));
@@ -892,8 +997,8 @@ __global__ void __launch_bounds__(128) k_lbm_wall_load(const __grid_constant__ L
         for (int b = a; b > 0 && ds[b - 1] > ds[b]; b--) {
           const int t = ds[b]; ds[b] = ds[b - 1]; ds[b - 1] = t;
         }
-      float2 rho = make_float2(0.f, 0.f);
-      if constexpr (Store<PREC>::kDev) rho = __ldg(src.rho + i);
+      float2 rho = make_float2(0.f, 0.f);  // the bounced populations were written by node i
+      if constexpr (Store<PREC>::kDev) rho = __ldg(src.rho + (Store<PREC>::kSendRef ? voxel_of(G, G.coord[i]) : (long long)i));
       for (int j = 0; j < 3; j++) {
         const int d = opp(ds[j]);  // incoming link of the bounced population
         if (m & (1u << (d - 1))) continue;
