@@ -558,7 +558,7 @@ def main():
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--prec", default="f16", choices=list(PREC_ID))
     ap.add_argument("--itw", type=int, default=100, help="steps per e2e step (check_state cadence)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the FP64/FP32 comparison legs")
