@@ -207,6 +207,24 @@ def test_wave_schedule_matches_two_pass(gpu, prec, planes, window, tile):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
 
+@pytest.mark.parametrize("prec,tol", [(PREC_F16, 1e-4), (PREC_BF16, 1e-3)])
+def test_restart_16bit(gpu, prec, tol):
+    """A 16-bit lattice continued directly and one restarted from its
+    get_state (stored against each node's own densities, then read so by
+    the first step) stay within the storage rounding of each other."""
+    ind, p = _case()
+    with Lattice(p, ind, prec) as A, Lattice(p, ind, prec) as B:
+        A.init_random(0.5)
+        A.step(10)
+        fr, fb = A.get_state()
+        B.set_state(fr, fb)
+        A.step(10)
+        B.step(10)
+        ar, ab = A.get_state()
+        br, bb = B.get_state()
+    assert max(np.abs(ar - br).max(), np.abs(ab - bb).max()) <= tol
+
+
 def test_wave_schedule_without_fluid(gpu):
     """A lattice with no fluid node: every slab launch is an empty graph node."""
     p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
