@@ -41,8 +41,9 @@ extern "C" {
 /* ---- LBM population storage precisions ---- */
 #define PS_PREC_F64 0   /* FP64 storage, FP64 arithmetic (plain path)            */
 #define PS_PREC_F32 1   /* FP32 storage, FP32 arithmetic                         */
-#define PS_PREC_F16 2   /* FP16 deviations from rest equilibrium, FP32 arithmetic */
-#define PS_PREC_BF16 3  /* BF16 deviations from rest equilibrium, FP32 arithmetic */
+#define PS_PREC_F16 2   /* FP16 deviations from the rest equilibrium of the node that
+                           wrote each population, FP32 arithmetic            */
+#define PS_PREC_BF16 3  /* BF16 deviations, as PS_PREC_F16                           */
 
 /* Physical parameters of the two-phase LBM, as read from INPUT_PARAMETERS
  * (S1:435-469).  `sig` is the value in the file (the library applies the
