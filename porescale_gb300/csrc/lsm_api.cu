@@ -956,7 +956,7 @@ int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t max
     std::vector<double> rn((size_t)n, 0.0);
     std::vector<long long> its((size_t)n, 0);
     for (int round = 0; round < 60 && rc == PS_OK && budget > 0; round++) {
-      // residual of every network (round 0: r = b); those above rtol start
+      // residual of every network (first refinement pass: r = b); those above rtol start
       // an FP32 inner solve on r / |r|
       std::vector<char> on((size_t)n, 0);
       rc = each_network(n, [&](int s) {
