@@ -586,7 +586,7 @@ __device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R
 // or one z-slab of the wavefront schedule (slabs are contiguous ranges of
 // the compact numbering, z being the slowest coordinate).
 template <int PREC, int BLK>
-__global__ void __launch_bounds__(BLK) k_lbm_dens(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+__global__ void __launch_bounds__(BLK, (PREC == 0 ? 1024 : 2048) / BLK) k_lbm_dens(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                   const __grid_constant__ GeomDev G, const BufDev src,
                                                   const BufDev dst, typename Store<PREC>::R* __restrict__ cc,
                                                   int i0, int i1)
