@@ -124,7 +124,9 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
           }
         }
       }
-      pq = (double)p[v] * (double)acc[0] + (double)p[nv + v] * (double)acc[1] + (double)p[2 * nv + v] * (double)acc[2];
+      // the node's p.(Ap) in T (FP32: one conversion instead of three FP64
+      // products on GB300's small FP64 pipe); sums across nodes stay FP64
+      pq = (double)(p[v] * acc[0] + p[nv + v] * acc[1] + p[2 * nv + v] * acc[2]);
     }
     q[v] = acc[0];
     q[nv + v] = acc[1];
@@ -421,16 +423,18 @@ template <typename T, int BLK>
 __device__ __forceinline__ double cg_xr_tile(int n3, T al, T* __restrict__ x, T* __restrict__ r,
                                              const T* __restrict__ p, const T* __restrict__ q, int i0)
 {
-  double rr = 0.0;
+  // the thread's kVecPer squares summed in T (FP32: one conversion to FP64
+  // per thread), the sums across threads in FP64
+  T rr = T(0);
   const int i1 = min(i0 + kVecPer * BLK, n3);
   for (int i = i0 + (int)threadIdx.x; i < i1; i += BLK) {
     const T xi = x[i] + al * p[i];
     const T ri = r[i] - al * q[i];
     x[i] = xi;
     r[i] = ri;
-    rr += (double)ri * (double)ri;
+    rr += ri * ri;
   }
-  return rr;
+  return (double)rr;
 }
 template <typename T, int BLK>
 __device__ __forceinline__ void cg_p_tile(int n3, T beta, const T* __restrict__ r, T* __restrict__ p, int i0)
