@@ -45,6 +45,8 @@ struct Lattice {
   LbmConst<float> Kf{};
   // device
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // second copy stream: fr and fb move side by side
+  cudaEvent_t ev_copy = nullptr;
   uint32_t* d_coord = nullptr;  // compact node -> packed coordinates
   uint32_t* d_mask = nullptr;   // compact node -> link and face bits
   int32_t* d_ref = nullptr;     // compact node -> reference fluid index
@@ -141,6 +143,8 @@ int dalloc(Lattice* L, T** p, size_t bytes)
 void free_lattice(Lattice* L)
 {
   if (!L) return;
+  if (L->stream2) cudaStreamDestroy(L->stream2);
+  if (L->ev_copy) cudaEventDestroy(L->ev_copy);
   cudaFree(L->d_coord);
   cudaFree(L->d_wall);
   for (cudaGraphExec_t x : L->wave_exec)
@@ -770,6 +774,8 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   lsm_node_numbers(L.get(), &L->ns);
   make_constants(L.get());
   PS_CUDA(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+  PS_CUDA(cudaStreamCreateWithFlags(&L->stream2, cudaStreamNonBlocking));
+  PS_CUDA(cudaEventCreateWithFlags(&L->ev_copy, cudaEventDisableTiming));
   const size_t nv = (size_t)L->nvox, nlc = (size_t)std::max(1LL, L->nl);
   if (int r = dalloc(L.get(), &L->d_coord, sizeof(uint32_t) * nlc)) return r;
   if (int r = dalloc(L.get(), &L->d_mask, sizeof(uint32_t) * nlc)) return r;
@@ -934,9 +940,13 @@ int ps_lbm_set_state(void* h, const double* fr, const double* fb)
   Lattice* L = as_lattice(h);
   if (int r = ensure_staging(L)) return r;
   const size_t b = sizeof(double) * 19 * (size_t)L->nl;
-  if (b) {
+  if (b) {  // the two arrays on two streams (two copy engines), joined before the kernel
+    PS_CUDA(cudaEventRecord(L->ev_copy, L->stream));
+    PS_CUDA(cudaStreamWaitEvent(L->stream2, L->ev_copy, 0));
     PS_CUDA(cudaMemcpyAsync(L->d_fr, fr, b, cudaMemcpyHostToDevice, L->stream));
-    PS_CUDA(cudaMemcpyAsync(L->d_fb, fb, b, cudaMemcpyHostToDevice, L->stream));
+    PS_CUDA(cudaMemcpyAsync(L->d_fb, fb, b, cudaMemcpyHostToDevice, L->stream2));
+    PS_CUDA(cudaEventRecord(L->ev_copy, L->stream2));
+    PS_CUDA(cudaStreamWaitEvent(L->stream, L->ev_copy, 0));
   }
   LbmLaunchArgs a = L->args(L->cur, L->cur);
   cudaError_t e = PREC_DISPATCH(lbm_set_state_launch, L->prec, a, L->d_fr, L->d_fb);
@@ -957,9 +967,12 @@ int ps_lbm_get_state(void* h, double* fr, double* fb)
   cudaError_t e = PREC_DISPATCH(lbm_get_state_launch, L->prec, a, L->d_fr, L->d_fb);
   if (e != cudaSuccess) return cuda_fail(e, "get_state kernel");
   const size_t b = sizeof(double) * 19 * (size_t)L->nl;
-  if (b) {
+  if (b) {  // the two arrays on two streams (two copy engines)
+    PS_CUDA(cudaEventRecord(L->ev_copy, L->stream));
+    PS_CUDA(cudaStreamWaitEvent(L->stream2, L->ev_copy, 0));
     PS_CUDA(cudaMemcpyAsync(fr, L->d_fr, b, cudaMemcpyDeviceToHost, L->stream));
-    PS_CUDA(cudaMemcpyAsync(fb, L->d_fb, b, cudaMemcpyDeviceToHost, L->stream));
+    PS_CUDA(cudaMemcpyAsync(fb, L->d_fb, b, cudaMemcpyDeviceToHost, L->stream2));
+    PS_CUDA(cudaStreamSynchronize(L->stream2));
   }
   PS_CUDA(cudaStreamSynchronize(L->stream));
   return check_fused(L);
