@@ -120,7 +120,7 @@ int ps_lbm_sync(void *handle);
 /* Step-kernel configuration: tx threads per CTA of the collide kernel, ty
  * of the density kernel, occ the minimum resident collide CTAs per SM asked
  * of the register allocator (0 = its choice).  Compiled: (128,256,0),
- * (256,256,0), (128,128,0), (256,512,0), (128,256,6), (128,256,7), (128,256,8),
+ * (256,256,0), (128,128,0), (128,256,6), (128,256,7), (128,256,8),
  * (256,256,3).  Used by the autotuner; values are validated. */
 int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
 /* Fused step schedule: planes > 0 runs each step as ONE persistent launch

@@ -1184,7 +1184,7 @@ int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, 
   struct Cfg {
     int tx, ty, occ;
   };
-  const std::vector<Cfg> cand = {{128, 256, 0}, {256, 256, 0}, {128, 128, 0}, {256, 512, 0},
+  const std::vector<Cfg> cand = {{128, 256, 0}, {256, 256, 0}, {128, 128, 0},
                                  {128, 256, 6}, {128, 256, 8}, {256, 256, 3}};
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
@@ -1308,7 +1308,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   // two-pass configurations, fused ones (slab planes, look-ahead), then
   // wavefront graphs (slab planes, window)
   const std::vector<Cfg> cand = {
-      {128, 256, 0, 0, 1, 0, 0}, {256, 256, 0, 0, 1, 0, 0},  {128, 128, 0, 0, 1, 0, 0}, {256, 512, 0, 0, 1, 0, 0},
+      {128, 256, 0, 0, 1, 0, 0}, {256, 256, 0, 0, 1, 0, 0},  {128, 128, 0, 0, 1, 0, 0},
       {128, 256, 6, 0, 1, 0, 0}, {128, 256, 8, 0, 1, 0, 0},  {256, 256, 3, 0, 1, 0, 0}, {128, 256, 0, 2, 1, 0, 0},
       {128, 256, 0, 4, 1, 0, 0}, {128, 256, 0, 8, 1, 0, 0},  {128, 256, 0, 4, 2, 0, 0}, {256, 256, 0, 4, 1, 0, 0},
       {128, 256, 6, 4, 1, 0, 0}, {128, 256, 8, 4, 1, 0, 0},  {128, 256, 6, 0, 1, 16, 0}, {128, 256, 6, 0, 1, 32, 0},

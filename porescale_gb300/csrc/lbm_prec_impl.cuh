@@ -210,7 +210,6 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
       if (tx == 128 && ty == 256) return detail::step_blk<P, 128, 256>(a);                                 \
       if (tx == 256 && ty == 256) return detail::step_blk<P, 256, 256>(a);                                 \
       if (tx == 128 && ty == 128) return detail::step_blk<P, 128, 128>(a);                                 \
-      if (tx == 256 && ty == 512) return detail::step_blk<P, 256, 512>(a);                                 \
     }                                                                                                      \
     if (tx == 128 && ty == 256 && occ == 6) return detail::step_blk<P, 128, 256, 6>(a);                    \
     if (tx == 128 && ty == 256 && occ == 7) return detail::step_blk<P, 128, 256, 7>(a);                    \
@@ -225,7 +224,6 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
       if (tx == 128 && ty == 256) return detail::wave_graph<P, 128, 256>(a, steps, first, S, window, g);   \
       if (tx == 256 && ty == 256) return detail::wave_graph<P, 256, 256>(a, steps, first, S, window, g);   \
       if (tx == 128 && ty == 128) return detail::wave_graph<P, 128, 128>(a, steps, first, S, window, g);   \
-      if (tx == 256 && ty == 512) return detail::wave_graph<P, 256, 512>(a, steps, first, S, window, g);   \
     }                                                                                                      \
     if (tx == 128 && ty == 256 && occ == 6) return detail::wave_graph<P, 128, 256, 6>(a, steps, first, S, window, g); \
     if (tx == 128 && ty == 256 && occ == 7) return detail::wave_graph<P, 128, 256, 7>(a, steps, first, S, window, g); \
@@ -247,7 +245,6 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
       if (tx == 128 && ty == 256) return detail::step_batch_blk<P, 128, 256>(b);                           \
       if (tx == 256 && ty == 256) return detail::step_batch_blk<P, 256, 256>(b);                           \
       if (tx == 128 && ty == 128) return detail::step_batch_blk<P, 128, 128>(b);                           \
-      if (tx == 256 && ty == 512) return detail::step_batch_blk<P, 256, 512>(b);                           \
     }                                                                                                      \
     if (tx == 128 && ty == 256 && occ == 6) return detail::step_batch_blk<P, 128, 256, 6>(b);              \
     if (tx == 128 && ty == 256 && occ == 8) return detail::step_batch_blk<P, 128, 256, 8>(b);              \
@@ -278,7 +275,7 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
   }                                                                                                        \
   size_t lbm_step_smem_##P(int tx, int ty, int occ)                                                        \
   {                                                                                                        \
-    const bool base = (tx == 128 && (ty == 256 || ty == 128)) || (tx == 256 && (ty == 256 || ty == 512)); \
+    const bool base = (tx == 128 && (ty == 256 || ty == 128)) || (tx == 256 && ty == 256);                \
     const bool hi = (tx == 128 && ty == 256 && (occ == 6 || occ == 7 || occ == 8)) || (tx == 256 && ty == 256 && occ == 3); \
     return (occ == 0 && base) || hi ? 1 : 0;                                                               \
   }                                                                                                        \
