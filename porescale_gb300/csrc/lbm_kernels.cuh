@@ -28,15 +28,18 @@
 //   * cc[v]: the stencil colour of the current step on the dense box
 //     (wetting colour on non-fluid voxels, written once at creation), read
 //     27 times per interface node from L1/L2;
-//   * 16-bit storage keeps each population as a deviation from the rest
-//     equilibrium t_d * rho_ref of its own component, rho_ref being the
+//   * deviation storage keeps each population as a deviation from the rest
+//     equilibrium t_d * rho_ref of its own component.  FP32: rho_ref is the
 //     component density of the RECEIVING node at the step that wrote it
-//     (FP32 pair rho[i] next to the populations): a reader needs only its
-//     own two densities.
+//     (FP32 pair rho[i] per compact node), so a reader needs only its own
+//     two densities.  16-bit: rho_ref is that of the WRITING node (pairs on
+//     the dense voxel box, rho[v]), so a population crossing an interface
+//     carries its own non-equilibrium part, not the density jump; the
+//     writer of slot d of the node at voxel v is voxel v - c_d (or v).
 //
 // One step = two launches over the fluid nodes:
 //   k_lbm_dens  reads each node's populations, writes the colour (and for
-//               16-bit storage the component densities that become the
+//               deviation storage the component densities that become the
 //               deviation reference of the populations written this step);
 //   k_lbm_coll  reads them again, collides with the 27-point colour stencil
 //               and writes the post-collision populations to their
