@@ -10,7 +10,10 @@ derivations of them without the reference present:
 * `nta` -- the 48 angle arm-direction pairs of the same file;
 * the cube-local tables cube_bon / cube_sbond / cube_ang / cube_abond of
   LSM2S/Cxxxx (as canonical sorted sets: their row order is irrelevant);
-* the table sizes the oracle builds for the two shipped `ind` geometries.
+* the table sizes the oracle builds for the two shipped `ind` geometries;
+* 40^3 crops of those two geometries (shipped_crops.npz: the corner
+  [0:40, 0:40, 0:40] of each, values as shipped) with the oracle's table
+  sizes for them, so GPU parity runs on the reference's own inputs.
 """
 import json
 import math
@@ -77,6 +80,15 @@ def main():
         sizes[name] = {"nl": o.nl, "nps": o.nps, "npb2": o.npb2, "npb4": o.npb4, "ns": o.ns,
                        "n_overflow": o.n_overflow, "solid": int((ind == 0).sum()), "phase2": int((ind == 3).sum())}
     out["shipped_geometry_tables"] = sizes
+    crops, crop_sizes = {}, {}
+    for key, name, dims in (("lbm_lsm_40", "LBM-LSM", (120, 120, 120)), ("lbm_lsm2s_40", "LBM-LSM2S", (150, 150, 54))):
+        c = read_ind(os.path.join(REF, name, "ind"), *dims)[:40, :40, :40].astype(np.uint8)
+        crops[key] = c
+        o = oracle.OracleLattice(make_params(), c.astype(np.int32))
+        crop_sizes[key] = {"nl": o.nl, "nps": o.nps, "npb2": o.npb2, "npb4": o.npb4, "ns": o.ns,
+                           "values": sorted(int(v) for v in np.unique(c))}
+    np.savez_compressed(os.path.join(HERE, "shipped_crops.npz"), **crops)
+    out["shipped_crop_tables"] = crop_sizes
     with open(os.path.join(HERE, "reference_tables.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_tables.json"))
