@@ -747,75 +747,112 @@ __global__ void k_lbm_fields(const __grid_constant__ LbmConst<typename Store<PRE
   cc[x + G.nx * (y + G.ny * z)] = (double)((q - K.wet) + K.wet);
 }
 
-// post-streaming populations in the reference layout fr(19,nl), fb(19,nl)
-template <int PREC>
-__global__ void k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
-                                const __grid_constant__ GeomDev G, const BufDev src, double* fr, double* fb)
+// The state kernels move between the reference layout (19 consecutive
+// doubles per node, nodes in reference order, so consecutive compact nodes
+// are far apart) and per-node values through shared memory: each warp
+// copies its 32 nodes' 152-byte blocks one block at a time with 19 lanes,
+// so every global access is one contiguous block rather than 32 scattered
+// 8-byte words per direction.
+constexpr int kStateBlk = 128;
+__device__ __forceinline__ void state_block_io(double (*sh)[kStateBlk][19], const GeomDev& G, double* fr, double* fb,
+                                               bool to_global)
 {
-  using R = typename Store<PREC>::R;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= G.nl) return;
-  const long long r = G.ref[i];
-  if constexpr (Store<PREC>::kSendRef) {  // decode t_d rho_writer + g in FP64
-    const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
-    const long long v = voxel_of(G, c);
-    const NbOff o = box_offsets(G, m);
-#pragma unroll
-    for (int d = 0; d < 19; d++) {
-      const bool wr = !src.recv && d > 0 && (m & (1u << (d - 1)));  // written by another node
-      const float2 rw = __ldg(src.rho + (wr ? v + o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : v));
-      R gr, gb;
-      Pop<PREC>::load_dev(src, d, i, G.pitch, gr, gb);
-      fr[19 * r + d] = (double)K.t[0][wcls(d)] * (double)rw.x + (double)gr;
-      fb[19 * r + d] = (double)K.t[1][wcls(d)] * (double)rw.y + (double)gb;
-    }
-  } else if constexpr (Store<PREC>::kDev) {  // decode t_d rho + g in FP64
-    float gr[19], gb[19];
-    const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
-#pragma unroll
-    for (int d = 0; d < 19; d++) {
-      fr[19 * r + d] = (double)K.t[0][wcls(d)] * (double)ro.x + (double)gr[d];
-      fb[19 * r + d] = (double)K.t[1][wcls(d)] * (double)ro.y + (double)gb[d];
-    }
-  } else {
-    R f[38];
-    read_node<PREC>(K, G, src, i, f);
-#pragma unroll
-    for (int d = 0; d < 19; d++) {
-      fr[19 * r + d] = (double)f[d];
-      fb[19 * r + d] = (double)f[19 + d];
+  const int lane = threadIdx.x & 31, w0 = threadIdx.x & ~31;
+  for (int k = 0; k < 32; k++) {
+    const int node = blockIdx.x * kStateBlk + w0 + k;
+    if (node >= G.nl) break;  // warp-uniform
+    const long long r = G.ref[node];
+    if (lane < 19) {
+      if (to_global) {
+        fr[19 * r + lane] = sh[0][w0 + k][lane];
+        fb[19 * r + lane] = sh[1][w0 + k][lane];
+      } else {
+        sh[0][w0 + k][lane] = fr[19 * r + lane];
+        sh[1][w0 + k][lane] = fb[19 * r + lane];
+      }
     }
   }
+  __syncwarp();
+}
+
+// post-streaming populations in the reference layout fr(19,nl), fb(19,nl)
+template <int PREC>
+__global__ void __launch_bounds__(kStateBlk) k_lbm_get_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+                                                             const __grid_constant__ GeomDev G, const BufDev src,
+                                                             double* fr_out, double* fb_out)
+{
+  using R = typename Store<PREC>::R;
+  __shared__ double sh[2][kStateBlk][19];
+  double* fr = sh[0][threadIdx.x];  // this node's values, written below
+  double* fb = sh[1][threadIdx.x];
+  const int i = blockIdx.x * kStateBlk + threadIdx.x;
+  if (i < G.nl) {
+    if constexpr (Store<PREC>::kSendRef) {  // decode t_d rho_writer + g in FP64
+      const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+      const long long v = voxel_of(G, c);
+      const NbOff o = box_offsets(G, m);
+#pragma unroll
+      for (int d = 0; d < 19; d++) {
+        const bool wr = !src.recv && d > 0 && (m & (1u << (d - 1)));  // written by another node
+        const float2 rw = __ldg(src.rho + (wr ? v + o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)] : v));
+        R gr, gb;
+        Pop<PREC>::load_dev(src, d, i, G.pitch, gr, gb);
+        fr[d] = (double)K.t[0][wcls(d)] * (double)rw.x + (double)gr;
+        fb[d] = (double)K.t[1][wcls(d)] * (double)rw.y + (double)gb;
+      }
+    } else if constexpr (Store<PREC>::kDev) {  // decode t_d rho + g in FP64
+      float gr[19], gb[19];
+      const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
+#pragma unroll
+      for (int d = 0; d < 19; d++) {
+        fr[d] = (double)K.t[0][wcls(d)] * (double)ro.x + (double)gr[d];
+        fb[d] = (double)K.t[1][wcls(d)] * (double)ro.y + (double)gb[d];
+      }
+    } else {
+      R f[38];
+      read_node<PREC>(K, G, src, i, f);
+#pragma unroll
+      for (int d = 0; d < 19; d++) {
+        fr[d] = (double)f[d];
+        fb[d] = (double)f[19 + d];
+      }
+    }
+  }
+  __syncwarp();
+  state_block_io(sh, G, fr_out, fb_out, true);
 }
 
 // post-streaming populations fr, fb (reference layout) into the node's own
 // slots; deviation storage takes the node's own densities as the reference
 // (for sender-reference storage the buffer is then marked recv)
 template <int PREC>
-__global__ void k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
-                                const __grid_constant__ GeomDev G, const BufDev dst, const double* fr,
-                                const double* fb)
+__global__ void __launch_bounds__(kStateBlk) k_lbm_set_state(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
+                                                             const __grid_constant__ GeomDev G, const BufDev dst,
+                                                             const double* fr_in, const double* fb_in)
 {
   using S = Store<PREC>;
   using R = typename S::R;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double sh[2][kStateBlk][19];
+  state_block_io(sh, G, const_cast<double*>(fr_in), const_cast<double*>(fb_in), false);
+  const int i = blockIdx.x * kStateBlk + threadIdx.x;
   if (i >= G.nl) return;
-  const long long me = G.ref[i];
+  const double* fr = sh[0][threadIdx.x];  // this node's values
+  const double* fb = sh[1][threadIdx.x];
   if constexpr (S::kDev) {
     // the node's own densities are the reference; deviations formed in FP64
-    double sr = fr[19 * me], sb = fb[19 * me];
+    double sr = fr[0], sb = fb[0];
     for (int d = 1; d < 19; d++) {
-      sr += fr[19 * me + d];
-      sb += fb[19 * me + d];
+      sr += fr[d];
+      sb += fb[d];
     }
     const float2 rho = make_float2((float)sr, (float)sb);
     dst.rho[S::kSendRef ? voxel_of(G, G.coord[i]) : (long long)i] = rho;
     for (int d = 0; d < 19; d++)
-      Pop<PREC>::put_dev(dst, d, i, G.pitch, (R)(fr[19 * me + d] - (double)K.t[0][wcls(d)] * (double)rho.x),
-                         (R)(fb[19 * me + d] - (double)K.t[1][wcls(d)] * (double)rho.y));
+      Pop<PREC>::put_dev(dst, d, i, G.pitch, (R)(fr[d] - (double)K.t[0][wcls(d)] * (double)rho.x),
+                         (R)(fb[d] - (double)K.t[1][wcls(d)] * (double)rho.y));
   } else {
     for (int d = 0; d < 19; d++)
-      Pop<PREC>::put(K, dst, d, i, G.pitch, (R)fr[19 * me + d], (R)fb[19 * me + d], make_float2(0.f, 0.f));
+      Pop<PREC>::put(K, dst, d, i, G.pitch, (R)fr[d], (R)fb[d], make_float2(0.f, 0.f));
   }
 }
 

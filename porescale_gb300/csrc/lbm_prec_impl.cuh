@@ -156,7 +156,7 @@ cudaError_t get_state(const LbmLaunchArgs& a, double* fr, double* fb)
   using R = typename Store<PREC>::R;
   const long long n = a.G.nl;
   if (n == 0) return cudaSuccess;
-  k_lbm_get_state<PREC><<<(unsigned)((n + 255) / 256), 256, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K),
+  k_lbm_get_state<PREC><<<(unsigned)((n + kStateBlk - 1) / kStateBlk), kStateBlk, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K),
                                                                              a.G, a.src, fr, fb);
   return cudaGetLastError();
 }
@@ -167,7 +167,7 @@ cudaError_t set_state(const LbmLaunchArgs& a, const double* fr, const double* fb
   using R = typename Store<PREC>::R;
   const long long n = a.G.nl;
   if (n == 0) return cudaSuccess;
-  k_lbm_set_state<PREC><<<(unsigned)((n + 255) / 256), 256, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K),
+  k_lbm_set_state<PREC><<<(unsigned)((n + kStateBlk - 1) / kStateBlk), kStateBlk, 0, a.stream>>>(*static_cast<const LbmConst<R>*>(a.K),
                                                                              a.G, a.dst, fr, fb);
   return cudaGetLastError();
 }
