@@ -689,7 +689,7 @@ def main():
             # wavefront graphs (slab planes / window) on the collide tile 128 x 6
             L.set_fused(0, 1)
             L.set_tile(128, 256, 6)
-            for planes, window in ((2, 0), (4, 0), (8, 0), (16, 0), (32, 0), (64, 0), (4, 3), (8, 3)):
+            for planes, window in ((2, 0), (4, 0), (8, 0), (16, 0), (32, 0), (64, 0), (128, 0), (4, 3), (8, 3)):
                 L.set_wave(planes, window)
                 L.set_state(fr, fb)
                 study[f"w{planes}/{window}"] = nl * 48 / time_steps(L, 48, 8, torch) / 1e6

@@ -1312,7 +1312,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
       {128, 256, 6, 0, 1, 0, 0}, {128, 256, 8, 0, 1, 0, 0},  {256, 256, 3, 0, 1, 0, 0}, {128, 256, 0, 2, 1, 0, 0},
       {128, 256, 0, 4, 1, 0, 0}, {128, 256, 0, 8, 1, 0, 0},  {128, 256, 0, 4, 2, 0, 0}, {256, 256, 0, 4, 1, 0, 0},
       {128, 256, 6, 4, 1, 0, 0}, {128, 256, 8, 4, 1, 0, 0},  {128, 256, 6, 0, 1, 16, 0}, {128, 256, 6, 0, 1, 32, 0},
-      {128, 256, 8, 0, 1, 32, 0}, {128, 256, 0, 0, 1, 32, 0}, {128, 256, 6, 0, 1, 64, 0}, {128, 256, 7, 0, 1, 0, 0},
+      {128, 256, 8, 0, 1, 32, 0}, {128, 256, 0, 0, 1, 32, 0}, {128, 256, 6, 0, 1, 64, 0}, {128, 256, 6, 0, 1, 128, 0}, {128, 256, 7, 0, 1, 0, 0},
       {128, 256, 7, 0, 1, 64, 0}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
