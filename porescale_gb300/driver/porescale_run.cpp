@@ -505,7 +505,6 @@ int main(int argc, char** argv)
   }
   check(ps_lbm_step(h, 2), "ps_lbm_step (initialisation)");  // S1:3454-3621
   ps_lbm_obs ob{};
-  const double t0 = (double)in.ncx * in.ncy * in.ncz;
   for (int it1 = itms; it1 <= in.itm; it1++) {
     check(ps_lbm_step(h, in.itw), "ps_lbm_step");
     check(ps_lbm_get_state(h, fr.data(), fb.data()), "ps_lbm_get_state");
