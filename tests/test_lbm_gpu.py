@@ -277,3 +277,32 @@ def test_edge_geometries(gpu, oracle_lib, prec):
             assert np.array_equal(gr, want_r) and np.array_equal(gb, want_b)
         else:
             assert max(np.abs(gr - want_r).max(), np.abs(gb - want_b).max()) < 5e-4
+
+
+def _pinned(shape):
+    torch = pytest.importorskip("torch")
+    return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+
+@pytest.mark.parametrize("prec", [PREC_F64, PREC_F32, PREC_F16, PREC_BF16])
+def test_state_io_through_pinned_buffers(gpu, prec):
+    """Page-locked caller buffers (direct DMA by the copy engines) give the
+    same state as pageable ones bit for bit, in both directions."""
+    ind, p = _case()
+    with Lattice(p, ind, PREC_F64) as S:
+        S.init_random(0.5)
+        S.step(5)
+        fr, fb = S.get_state()
+    nl = fr.shape[0]
+    hr, hb = _pinned((nl, 19)), _pinned((nl, 19))
+    hr[:], hb[:] = fr, fb
+    with Lattice(p, ind, prec) as A, Lattice(p, ind, prec) as B:
+        A.set_state(fr, fb)    # pageable
+        B.set_state(hr, hb)    # page-locked
+        A.step(7)
+        B.step(7)
+        ar, ab = A.get_state()
+        br, bb = B.get_state((_pinned((nl, 19)), _pinned((nl, 19))))
+        cr, cb = B.get_state()
+    assert np.array_equal(ar, br) and np.array_equal(ab, bb)
+    assert np.array_equal(br, cr) and np.array_equal(bb, cb)
