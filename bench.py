@@ -594,8 +594,8 @@ def main():
     metric = "D3Q19 two-phase MLUPS"
 
     if args.impl == "reference":
-        # the reference is Fortran and no Fortran compiler exists here or on
-        # the GPU machine: its CPU path is timed through the C restatement
+        # the reference is Fortran and no Fortran compiler exists on either
+        # build host: its CPU path is timed through the C restatement
         if rank != 0:
             return
         from porescale_gb300 import _build

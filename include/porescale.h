@@ -266,9 +266,10 @@ int ps_lsm_alpha_beta(void *handle, const int32_t *lab, int32_t npores, int32_t 
 /* Largest box (voxel cubes) ps_lsm_stress_noalloc accepts: 128^3. */
 #define PS_LSM_NOALLOC_MAX_CUBES (2 * 1024 * 1024)
 /* Allocation-free stress evaluation -- no counterpart in the reference.
- * For callers that cannot allocate device memory when they need the moduli
- * (a time loop being captured into a CUDA graph, or a driver confined to a
- * fixed device memory budget).  d_u is a DEVICE array of the displacements
+ * For callers that cannot allocate device memory when they need the moduli:
+ * an application whose own pool has already reserved the device's memory,
+ * or a driver stepping several streams, where freeing device memory would
+ * wait for all work on the device.  d_u is a DEVICE array of the displacements
  * of the unique nodes of the handle's box, three planes (x, y, z component)
  * of nx*ny*nz values, node (x,y,z) at x + nx*(y + ny*z), without the jump;
  * out (host) receives the 9 summed cube stresses (as ps_lsm_result.sigma)

@@ -1,8 +1,8 @@
 /*
  * ps_oracle.h -- CPU FP64 restatement of porescale's two hot paths.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
- * implementation in porescale_gb300/.  Only tests/, __graft_entry__.smoke()
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity reference for
+ * the GPU implementation in porescale_gb300/.  Only tests/, __graft_entry__.smoke()
  * and bench.py's CPU-baseline leg may load it; the product never does.
  *
  * Every routine restates the Fortran reference (Eng-RSMY/porescale) in

@@ -1,8 +1,8 @@
 /*
  * ps_oracle_lbm.c -- TEST INFRASTRUCTURE: FP64 CPU restatement of the
  * colour-gradient two-phase D3Q19 step of porescale (S1 =
- * LBM-LSM/lsm_lbm_static_alpha_beta_multipore.f).  Used only as the checker
- * for the GPU kernels and as the timed CPU baseline ("port").
+ * LBM-LSM/lsm_lbm_static_alpha_beta_multipore.f).  Used only as the parity
+ * reference for the GPU kernels and as the timed CPU baseline ("port").
  *
  * Compiled with -ffp-contract=off so that every multiply and add rounds
  * separately, as the reference's source expressions do; expressions keep

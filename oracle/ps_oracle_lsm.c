@@ -2,7 +2,7 @@
  * ps_oracle_lsm.c -- TEST INFRASTRUCTURE: FP64 CPU restatement of the
  * two-solid alpha-beta / bond-bending lattice-spring model of porescale
  * (XX = LSM2S/Cxxxx/XX_P.f, x-stretch; YZ = LSM2S/Cyzyz/YZ_P.f, yz-shear).
- * Used only as the checker of the GPU solver and as the CPU baseline.
+ * Used only as the reference for parity tests of the GPU solver and as the CPU baseline.
  *
  * The reference pads the loaded axis with a pore column and ties the node
  * planes 1 and N+1 (their forces are summed and shared) with a displacement

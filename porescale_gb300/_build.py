@@ -2,8 +2,8 @@
 
 * ``porescale_gb300/libporescale_gpu.so`` -- the CUDA library behind the C ABI
   declared in ``include/porescale.h`` (sm_103a only);
-* ``oracle/libps_oracle.so`` -- the CPU FP64 restatement used as the checker
-  by the tests and as the CPU baseline of ``bench.py`` (built, never called,
+* ``oracle/libps_oracle.so`` -- the CPU FP64 restatement used as the parity
+  reference by the tests and as the CPU baseline of ``bench.py`` (built, never called,
   by the library itself).
 
 Translation units are compiled in parallel; an output is rebuilt only when a

@@ -1068,10 +1068,12 @@ void* ps_lsm_stream(void* h) { return h ? (void*)static_cast<Springs*>(h)->strea
 // Stress and modulus of a caller-supplied displacement field, computed
 // without any device allocation: the per-CTA partial sums go to the
 // library's static scratch array instead of memory from cudaMalloc.  Meant
-// for callers that may not allocate at that point -- a time loop being
-// captured into a CUDA graph, or a driver running inside a fixed device
-// memory budget that re-evaluates the moduli every few steps.  The handle
-// must already exist (ps_lsm_create allocates; this call does not).
+// for callers that cannot allocate device memory when they re-evaluate the
+// moduli: a host application whose own pool has already reserved the
+// device's memory (a cudaMalloc there fails or competes with the pool), and
+// a driver stepping several streams, where freeing device memory waits for
+// all work on the device and would stall the other streams.  The handle must
+// already exist (ps_lsm_create allocates; this call does not).
 //
 // The scratch array is shared by every call in the process and keeps the
 // last call's partial sums; each call rewrites the slots it reads before

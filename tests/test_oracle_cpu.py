@@ -1,4 +1,4 @@
-"""CPU tests of the FP64 oracle (the checker of the GPU kernels).
+"""CPU tests of the FP64 oracle (the parity reference of the GPU kernels).
 
 The reference ships no golden outputs, so the oracle is pinned by the
 reference's own known answers and by physics: the homogeneous-solid moduli

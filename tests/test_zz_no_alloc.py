@@ -2,9 +2,10 @@
 ps_lsm_solve's own stress result.
 
 ps_lsm_stress_noalloc serves callers that cannot allocate device memory
-when they need the moduli (a time loop being captured into a CUDA graph, a
-driver confined to a fixed device memory budget); its partial sums live in
-a static device array of the library.  This file runs last (pytest collects
+when they need the moduli (an application whose own pool has already
+reserved the device's memory, a driver stepping several streams where
+freeing device memory would stall the others); its partial sums live in a
+static device array of the library.  This file runs last (pytest collects
 it after the others) and also passes on its own in a fresh process.
 """
 import ctypes as C
