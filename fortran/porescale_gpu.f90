@@ -49,6 +49,12 @@ module porescale_gpu
     integer(c_int32_t) :: load, precision
   end type
 
+  type, bind(c) :: ps_lsm_info
+    integer(c_int64_t) :: nnode, ncube, nvox
+    integer(c_int32_t) :: nx, ny, nz, load, precision, reserved
+    integer(c_int64_t) :: device_bytes
+  end type
+
   type, bind(c) :: ps_lsm_result
     real(c_double) :: modulus, sigma(9), strain, relres
     integer(c_int64_t) :: iterations, inner_iterations, nnode, ncube
@@ -118,6 +124,20 @@ module porescale_gpu
       integer(c_int32_t), value :: steps
       integer(c_int32_t), intent(out) :: tx, ty, occ
     end function
+    ! the lattice's CUDA stream (cudaStream_t) and a wait for its work
+    type(c_ptr) function ps_lbm_stream(handle) bind(c, name='ps_lbm_stream')
+      import :: c_ptr
+      type(c_ptr), value :: handle
+    end function
+    integer(c_int) function ps_lbm_sync(handle) bind(c, name='ps_lbm_sync')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: handle
+    end function
+    integer(c_int) function ps_lbm_set_tile(handle, tx, ty, occ) bind(c, name='ps_lbm_set_tile')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: tx, ty, occ
+    end function
     ! several subvolumes advanced together (handles(n) from ps_lbm_create)
     integer(c_int) function ps_batch_create(handles, n, batch) bind(c, name='ps_batch_create')
       import :: c_int, c_int32_t, c_ptr
@@ -129,6 +149,21 @@ module porescale_gpu
       import :: c_int, c_int32_t, c_ptr
       type(c_ptr), value :: batch
       integer(c_int32_t), value :: nsteps
+    end function
+    integer(c_int) function ps_batch_set_tile(batch, tx, ty, occ) bind(c, name='ps_batch_set_tile')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: batch
+      integer(c_int32_t), value :: tx, ty, occ
+    end function
+    integer(c_int) function ps_batch_autotune(batch, steps, tx, ty, occ) bind(c, name='ps_batch_autotune')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: batch
+      integer(c_int32_t), value :: steps
+      integer(c_int32_t), intent(out) :: tx, ty, occ
+    end function
+    type(c_ptr) function ps_batch_stream(batch) bind(c, name='ps_batch_stream')
+      import :: c_ptr
+      type(c_ptr), value :: batch
     end function
     integer(c_int) function ps_batch_destroy(batch) bind(c, name='ps_batch_destroy')
       import :: c_int, c_ptr
@@ -150,6 +185,17 @@ module porescale_gpu
       type(c_ptr), value :: handle
       real(c_double), intent(out) :: k, dk_ds(*)
     end function
+    integer(c_int) function ps_gray_permeability(handle, k) bind(c, name='ps_gray_permeability')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: k
+    end function
+    ! f(19, nx*ny*nz) of the last forward run
+    integer(c_int) function ps_gray_get_state(handle, f) bind(c, name='ps_gray_get_state')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: f(*)
+    end function
     integer(c_int) function ps_gray_destroy(handle) bind(c, name='ps_gray_destroy')
       import :: c_int, c_ptr
       type(c_ptr), value :: handle
@@ -165,6 +211,11 @@ module porescale_gpu
       integer(c_int32_t), intent(in) :: ind(*)
       integer(c_int32_t), value :: nx, ny, nz
       type(c_ptr), intent(out) :: handle
+    end function
+    integer(c_int) function ps_lsm_get_info(handle, info) bind(c, name='ps_lsm_get_info')
+      import :: c_int, c_ptr, ps_lsm_info
+      type(c_ptr), value :: handle
+      type(ps_lsm_info), intent(out) :: info
     end function
     integer(c_int) function ps_lsm_solve(handle, rtol, maxit, res) bind(c, name='ps_lsm_solve')
       import :: c_int, c_int32_t, c_double, c_ptr, ps_lsm_result
@@ -185,6 +236,10 @@ module porescale_gpu
       import :: c_int, c_double, c_ptr
       type(c_ptr), value :: handle
       real(c_double), intent(out) :: u(*)
+    end function
+    type(c_ptr) function ps_lsm_stream(handle) bind(c, name='ps_lsm_stream')
+      import :: c_ptr
+      type(c_ptr), value :: handle
     end function
     integer(c_int) function ps_lsm_gradients(handle, grad) bind(c, name='ps_lsm_gradients')
       import :: c_int, c_double, c_ptr
@@ -213,6 +268,14 @@ module porescale_gpu
       real(c_double), value :: pres
       real(c_double), intent(out) :: alphai(9), betai(*)
     end function
+    ! stress of a device displacement field (d_u: a device address, three
+    ! planes of nx*ny*nz) without any device allocation; out(1:9) the summed
+    ! cube stresses, out(10) the modulus
+    integer(c_int) function ps_lsm_stress_noalloc(handle, d_u, out) bind(c, name='ps_lsm_stress_noalloc')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle, d_u
+      real(c_double), intent(out) :: out(10)
+    end function
     integer(c_int) function ps_lsm_destroy(handle) bind(c, name='ps_lsm_destroy')
       import :: c_int, c_ptr
       type(c_ptr), value :: handle
@@ -221,6 +284,10 @@ module porescale_gpu
       import :: c_int, c_int32_t, c_char
       character(kind=c_char), intent(out) :: buf(*)
       integer(c_int32_t), value :: len
+    end function
+    ! NUL-terminated version string (convert with c_f_pointer)
+    type(c_ptr) function ps_version() bind(c, name='ps_version')
+      import :: c_ptr
     end function
   end interface
 end module porescale_gpu

@@ -272,7 +272,10 @@ int ps_lsm_alpha_beta(void *handle, const int32_t *lab, int32_t npores, int32_t 
  * wait for all work on the device.  d_u is a DEVICE array of the displacements
  * of the unique nodes of the handle's box, three planes (x, y, z component)
  * of nx*ny*nz values, node (x,y,z) at x + nx*(y + ny*z), without the jump;
- * out (host) receives the 9 summed cube stresses (as ps_lsm_result.sigma)
+ * its kernels run on the handle's stream (ps_lsm_stream), so work that
+ * writes d_u on another stream must be complete or ordered before the
+ * call, which returns after that stream is synchronised; out (host)
+ * receives the 9 summed cube stresses (as ps_lsm_result.sigma)
  * and then the modulus.  Uses a static device scratch array instead of
  * cudaMalloc; boxes above PS_LSM_NOALLOC_MAX_CUBES are rejected
  * (PS_ERR_ARG).  Calls that overlap on the GPU share that array and race;

@@ -35,6 +35,55 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
 
 
+def test_fortran_module_binds_every_entry_point():
+    """The ISO_C_BINDING module (no Fortran compiler on this machine, so read
+    as text) binds exactly the entry points the header declares, each under
+    its own name, in lines within the free-form limit of 132 characters."""
+    src = open(os.path.join(ROOT, "fortran", "porescale_gpu.f90")).read()
+    bound = re.findall(r"function\s+(ps_\w+)\s*\([^)]*\)\s*&?\s*bind\(c,\s*name='(ps_\w+)'\)", src)
+    assert all(f == c for f, c in bound), [b for b in bound if b[0] != b[1]]
+    assert sorted(c for _, c in bound) == _declared()
+    assert max(len(line) for line in src.splitlines()) <= 132
+
+
+def _c_structs():
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "porescale.h")).read(), flags=re.S)
+    out = {}
+    for body, name in re.findall(r"typedef struct\s*\{(.*?)\}\s*(ps_\w+)\s*;", src, flags=re.S):
+        fields = []
+        for decl in filter(None, (d.strip() for d in body.split(";"))):
+            ctype, rest = decl.split(None, 1)
+            for v in rest.split(","):
+                m = re.fullmatch(r"\s*(\w+)\s*(?:\[(\d+)\])?\s*", v)
+                fields.append((ctype, m.group(1).lower(), int(m.group(2) or 1)))
+        out[name] = fields
+    return out
+
+
+def _fortran_types():
+    src = open(os.path.join(ROOT, "fortran", "porescale_gpu.f90")).read()
+    kinds = {"c_double": "double", "c_int32_t": "int32_t", "c_int64_t": "int64_t"}
+    out = {}
+    for name, body in re.findall(r"type, bind\(c\) :: (ps_\w+)\n(.*?)\n\s*end type", src, flags=re.S):
+        fields = []
+        for line in body.splitlines():
+            m = re.fullmatch(r"\s*(?:real|integer)\((\w+)\) :: (.*)", line)
+            for v in re.findall(r"(\w+)(?:\((\d+)\))?", m.group(2)):
+                fields.append((kinds[m.group(1)], v[0].lower(), int(v[1] or 1)))
+        out[name] = fields
+    return out
+
+
+def test_fortran_types_match_c_structs():
+    """Every bind(c) derived type of the Fortran module lists the fields of
+    the header's struct of the same name: same order, types and extents, so
+    the two layouts agree byte for byte."""
+    c, f = _c_structs(), _fortran_types()
+    assert sorted(f) == sorted(c)
+    for name in c:
+        assert f[name] == c[name], name
+
+
 def test_version_and_error_without_gpu(lib):
     lib.ps_version.restype = ctypes.c_char_p
     assert b"sm_103a" in lib.ps_version()
