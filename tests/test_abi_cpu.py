@@ -95,6 +95,11 @@ def test_python_bindings_cover_header():
     from porescale_gb300 import _lib, gray, springs  # noqa: F401  (these register their signatures)
     missing = [n for n in _declared() if n not in _lib.SIGNATURES]
     assert not missing, missing
+    # and with the header's parameter count
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "porescale.h")).read(), flags=re.S)
+    for name, params in re.findall(r"\b(ps_\w+)\s*\(([^)]*)\)\s*;", src):
+        count = 0 if params.strip() in ("", "void") else params.count(",") + 1
+        assert len(_lib.SIGNATURES[name][1]) == count, name
 
 
 def test_argument_errors_and_missing_device(lib):
