@@ -113,6 +113,11 @@ module porescale_gpu
       type(c_ptr), value :: handle
       integer(c_int32_t), value :: planes, ahead
     end function
+    integer(c_int) function ps_lbm_set_wait_limit(handle, polls) bind(c, name='ps_lbm_set_wait_limit')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: polls
+    end function
     integer(c_int) function ps_lbm_set_wave(handle, planes, window) bind(c, name='ps_lbm_set_wave')
       import :: c_int, c_int32_t, c_ptr
       type(c_ptr), value :: handle

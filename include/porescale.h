@@ -134,6 +134,16 @@ int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
  * whose wait gives up (bounded) makes the next synchronising call return
  * PS_ERR_TIMEOUT. */
 int ps_lbm_set_fused(void *handle, int32_t planes, int32_t ahead);
+/* Bound of the fused schedule's device waits, in polls of a density-tile
+ * counter (about 32 ns apart); 0 restores the default 2^22.  A wait that
+ * reaches it gives up, the tile collides with whatever colour field it
+ * finds, and the next synchronising call (ps_lbm_sync, ps_lbm_observables,
+ * ps_lbm_get_state, ...) returns PS_ERR_TIMEOUT: the state is then invalid
+ * until ps_lbm_set_state.  Every index the collide uses comes from the
+ * geometry, never from the data, so giving up reads and writes only the
+ * lattice's own arrays.  No counterpart in the reference: it exists so
+ * that the give-up path can be exercised. */
+int ps_lbm_set_wait_limit(void *handle, int32_t polls);
 /* Wavefront schedule: planes > 0 runs the steps in graphs of 8 steps whose
  * density and collide launches each cover one z-slab of `planes` planes,
  * ordered only by their data dependencies (density of slab k after the
@@ -278,9 +288,11 @@ int ps_lsm_alpha_beta(void *handle, const int32_t *lab, int32_t npores, int32_t 
  * receives the 9 summed cube stresses (as ps_lsm_result.sigma)
  * and then the modulus.  Uses a static device scratch array instead of
  * cudaMalloc; boxes above PS_LSM_NOALLOC_MAX_CUBES are rejected
- * (PS_ERR_ARG).  Calls that overlap on the GPU share that array and race;
- * the first call on a device sets it up and should precede any stream
- * capture. */
+ * (PS_ERR_ARG).  Calls that overlap on the GPU share that array and race.
+ * Every call looks up the array's device address on the current device
+ * (cudaGetSymbolAddress, no allocation), so it stays valid across a device
+ * reset; a handle with no imposed strain (gstrain 0) gets modulus 0, as
+ * from ps_lsm_solve. */
 int ps_lsm_stress_noalloc(void *handle, const double *d_u, double *out);
 
 /* ---- gray partial-bounce-back lattice and its adjoint (extension) ---- */

@@ -67,6 +67,7 @@ struct Lattice {
   int* d_ntd = nullptr;
   unsigned* d_ctr = nullptr;
   int* d_err = nullptr;
+  unsigned spin_limit = kFusedSpinLimit;  // polls before a fused-step wait gives up
   int nitems = 0, nslab = 0, sched_tx = 0, sched_planes = 0, sched_ahead = 0;
   // wavefront schedule (0 planes: off): z-slab launches in a graph of
   // kWaveSteps steps, one executable per starting buffer
@@ -517,6 +518,7 @@ int launch_steps(Lattice* L, int n)
       f.ntd = L->d_ntd;
       f.ctr = L->d_ctr;
       f.err = L->d_err;
+      f.spin_limit = L->spin_limit;
       e = PREC_DISPATCH(lbm_fused_launch, L->prec, L->tx, L->zchunk, a, f);
     } else {
       e = PREC_DISPATCH(lbm_step_launch, L->prec, L->tx, L->ty, L->zchunk, a);
@@ -1253,6 +1255,14 @@ int ps_lbm_set_fused(void* h, int32_t planes, int32_t ahead)
   L->fused_planes = planes;
   L->fused_ahead = ahead;
   if (planes > 0) L->wave_planes = 0;
+  return PS_OK;
+}
+
+int ps_lbm_set_wait_limit(void* h, int32_t polls)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_wait_limit: null handle");
+  if (polls < 0) return fail(PS_ERR_ARG, "ps_lbm_set_wait_limit: polls < 0");
+  as_lattice(h)->spin_limit = polls == 0 ? kFusedSpinLimit : (unsigned)polls;
   return PS_OK;
 }
 

@@ -675,8 +675,9 @@ struct FusedArgs {
   const int* ntd;        // density tiles per slab
   unsigned int* ctr;     // [1 + s] completed density tiles of slab s (zeroed before the launch)
   int* err;              // set to 1 when a wait gave up
+  unsigned spin_limit;   // polls before a wait gives up
 };
-constexpr unsigned kFusedSpinLimit = 1u << 22;
+constexpr unsigned kFusedSpinLimit = 1u << 22;  // default spin_limit
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
 {
@@ -707,7 +708,7 @@ __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
           const unsigned target = (unsigned)__ldg(F.ntd + sl);
           unsigned n = 0;
           while (ld_acquire_u32(F.ctr + 1 + sl) < target) {
-            if (++n > kFusedSpinLimit) {
+            if (++n > F.spin_limit) {
               atomicExch(F.err, 1);
               ok = false;
               break;

@@ -340,24 +340,17 @@ __global__ void k_stress_final(const double* part, int n, double* out)
   out[threadIdx.x] = s;
 }
 
-// device address of g_stress_scratch on each device, looked up once per
-// device with that device current (the host-side symbol is only a stand-in)
-std::mutex g_scratch_mu;
-double* g_scratch_ptr[64] = {nullptr};
-
+// device address of g_stress_scratch on the current device.  Looked up on
+// every call, with the caller's device current: the host-side symbol is
+// only a stand-in, and an address kept from an earlier call would be stale
+// after the application resets the device or recreates its primary
+// context.  The lookup allocates nothing.
 int noalloc_scratch(double** out)
 {
-  int dev = 0;
-  PS_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(PS_ERR_ARG, "ps_lsm_stress_noalloc: device %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
-    double* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress((void**)&p, g_stress_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_stress_scratch)");
-    g_scratch_ptr[dev] = p;
-  }
-  *out = g_scratch_ptr[dev];
+  double* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void**)&p, g_stress_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_stress_scratch)");
+  *out = p;
   return PS_OK;
 }
 
@@ -1078,8 +1071,10 @@ void* ps_lsm_stream(void* h) { return h ? (void*)static_cast<Springs*>(h)->strea
 // The scratch array is shared by every call in the process and keeps the
 // last call's partial sums; each call rewrites the slots it reads before
 // reading them.  Calls that overlap on the GPU (from several host threads or
-// streams) race on it and must be serialised by the caller.  The first call
-// on a device looks up the array's device address with that device current.
+// streams) race on it and must be serialised by the caller.  Every call
+// looks up the array's device address on the current device
+// (cudaGetSymbolAddress, which allocates nothing), so a device reset between
+// calls leaves no stale address behind.
 int ps_lsm_stress_noalloc(void* h, const double* d_u, double* out)
 {
   if (!h || !d_u || !out) return fail(PS_ERR_ARG, "ps_lsm_stress_noalloc: null argument");
@@ -1101,7 +1096,9 @@ int ps_lsm_stress_noalloc(void* h, const double* d_u, double* out)
   const double vcell = (double)S->nx * S->ny * S->nz;
   const double nax = S->pa == 0 ? S->nx : S->ny;
   for (int i = 0; i < 9; i++) out[i] = sig[i];
-  out[9] = (S->pa == 0 ? sig[0] : sig[5]) / (vcell * jump / nax);
+  // no imposed strain (a handle that only carries a wall load): modulus 0,
+  // as ps_lsm_solve reports it
+  out[9] = jump != 0.0 ? (S->pa == 0 ? sig[0] : sig[5]) / (vcell * jump / nax) : 0.0;
   return PS_OK;
 }
 

@@ -129,6 +129,10 @@ class Lattice:
         """Fused one-launch step over z-slabs of `planes` planes (0: two-pass)."""
         check(self._lib.ps_lbm_set_fused(self._h, planes, ahead))
 
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls before a fused-step wait gives up (0: the default 2^22)."""
+        check(self._lib.ps_lbm_set_wait_limit(self._h, polls))
+
     def set_wave(self, planes: int, window: int = 0) -> None:
         """Wavefront schedule: 8-step graphs of z-slab launches of `planes`
         planes ordered by their data dependencies (0: off)."""

@@ -1,7 +1,7 @@
 """Writes tests/golden/reference_tables.json from the reference sources.
 
-Run in a checkout that has the porescale reference at $PORESCALE_REF
-(default /root/reference).  It extracts the lattice-spring constant tables
+Usage: python tests/golden/make_golden.py <porescale checkout>, or with the
+checkout's path in $PORESCALE_REF.  It extracts the lattice-spring constant tables
 the reference ships or spells out literally, so the tests can check our own
 derivations of them without the reference present:
 
@@ -25,7 +25,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PORESCALE_REF", "/root/reference")
+REF = None  # the porescale checkout, set by main()
 
 
 def parse_anf(src):
@@ -95,4 +95,7 @@ def main():
 
 
 if __name__ == "__main__":
+    REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PORESCALE_REF")
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py <porescale checkout>  (or set PORESCALE_REF)")
     main()

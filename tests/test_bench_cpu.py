@@ -77,3 +77,6 @@ def test_reference_arm_line():
     for k in ("metric", "n_gpus", "steps", "warmup", "higher_is_better", "config", "cpu_baseline", "e2e"):
         assert k in line, k
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    # the same config object as our arm prints for this workload
+    assert set(line["config"]) == {"workload", "size", "seed", "fluid_nodes", "l2"}
+    assert line["config"]["size"] == 32 and line["config"]["fluid_nodes"] > 0

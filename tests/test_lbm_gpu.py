@@ -306,3 +306,42 @@ def test_state_io_through_pinned_buffers(gpu, prec):
         cr, cb = B.get_state()
     assert np.array_equal(ar, br) and np.array_equal(ab, bb)
     assert np.array_equal(br, cr) and np.array_equal(bb, cb)
+
+
+def test_fused_wait_gives_up_and_recovers(gpu):
+    """The fused schedule's bounded device wait, run out on purpose: with a
+    limit of one poll the first collide tiles find their density tiles
+    unfinished, give up, and the next synchronising call returns
+    PS_ERR_TIMEOUT (the wait returns rather than spins, and every index the
+    collide uses comes from the geometry, so nothing leaves the lattice's
+    arrays).  After ps_lbm_set_state the same lattice, back on the default
+    limit, steps exactly as a fresh one."""
+    ind = geo.sphere_pack((48, 40, 40), 0.45, 3.0, seed=19)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    with Lattice(p, ind, PREC_F32) as L:
+        L.init_random(0.5)
+        fr0, fb0 = L.get_state()
+        L.set_tile(128, 256, 0)
+        L.set_fused(2, 1)
+        L.set_wait_limit(1)
+        timed_out = False
+        for _ in range(20):
+            L.step(1)
+            try:
+                L.sync()
+            except PorescaleError as exc:
+                assert exc.code == 4  # PS_ERR_TIMEOUT
+                timed_out = True
+                break
+        assert timed_out
+        L.sync()  # the flag is cleared once reported
+        L.set_wait_limit(0)
+        L.set_state(fr0, fb0)
+        L.step(6)
+        L.sync()
+        got = L.get_state()
+    with Lattice(p, ind, PREC_F32) as R:
+        R.set_state(fr0, fb0)
+        R.step(6)
+        want = R.get_state()
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
