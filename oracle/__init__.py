@@ -195,6 +195,11 @@ def _lsm_sigs(L):
         "or_lsm_forces": (None, [C.c_void_p, _DP, _DP]),
         "or_lsm_relax": (C.c_int64, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double]),
         "or_lsm_cg": (C.c_int64, [C.c_void_p, C.c_double, C.c_int64, _DP]),
+        "or_lsm_cg_par": (C.c_int64, [C.c_void_p, C.c_double, C.c_int64, _DP, C.c_int]),
+        "or_lsm_relax_par": (C.c_int64, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64, C.c_double,
+                                         C.c_int]),
+        "or_lsm_dyn_step": (None, [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_int]),
+        "or_lsm_get_dyn": (None, [C.c_void_p, _DP, _DP, _DP]),
         "or_lsm_set_load": (None, [C.c_void_p, _DP]),
         "or_lsm_get_disp": (None, [C.c_void_p, _DP]),
         "or_lsm_set_disp": (None, [C.c_void_p, _DP]),
@@ -251,13 +256,31 @@ class OracleSprings:
         lib().or_lsm_forces(self._h, _d(u), _d(a))
         return a
 
-    def relax(self, dt, rs, damp, maxsteps, ftol):
+    def relax(self, dt, rs, damp, maxsteps, ftol, nthreads=1):
+        """XX:1377-1545's damped Verlet relaxation until the largest nodal
+        force is below ftol or maxsteps; returns the steps done."""
+        if nthreads > 1:
+            return int(lib().or_lsm_relax_par(self._h, dt, rs, damp, int(maxsteps), ftol, int(nthreads)))
         return int(lib().or_lsm_relax(self._h, dt, rs, damp, int(maxsteps), ftol))
 
-    def cg(self, rtol=1e-10, maxit=100000):
+    def cg(self, rtol=1e-10, maxit=100000, nthreads=1):
         rel = C.c_double()
-        it = int(lib().or_lsm_cg(self._h, rtol, int(maxit), C.byref(rel)))
+        if nthreads > 1:
+            it = int(lib().or_lsm_cg_par(self._h, rtol, int(maxit), C.byref(rel), int(nthreads)))
+        else:
+            it = int(lib().or_lsm_cg(self._h, rtol, int(maxit), C.byref(rel)))
         return it, rel.value
+
+    def dyn_step(self, nsteps, dt, rsi, damp, nthreads=1):
+        """The coupled driver's spring dynamics (lsm_step, S1:1721-1903)
+        with the external load (set_load) as afdat."""
+        lib().or_lsm_dyn_step(self._h, int(nsteps), dt, rsi, damp, int(nthreads))
+
+    def dyn_state(self):
+        """(r, v, a), each (ns, 3) in node order."""
+        out = [np.zeros((self.ns, 3)) for _ in range(3)]
+        lib().or_lsm_get_dyn(self._h, *[_d(x) for x in out])
+        return tuple(out)
 
     def set_load(self, f):
         """external nodal load (ns, 3) in node order for the next cg(); None removes it"""

@@ -95,8 +95,17 @@ void or_lsm_tables(const or_lsm *o, int32_t *icors, int32_t *bon, double *sbond,
 void or_lsm_forces(const or_lsm *o, const double *u, double *a);
 /* damped Verlet dynamic relaxation as XX:1377-1545; returns steps done */
 int64_t or_lsm_relax(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol);
-/* FP64 CG on the same operator over unique nodes; returns iterations */
+/* FP64 CG on the same operator over unique nodes; returns iterations.
+ * or_lsm_cg_par evaluates the forces on nthreads OpenMP threads. */
 int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres);
+int64_t or_lsm_cg_par(or_lsm *o, double rtol, int64_t maxit, double *relres, int nthreads);
+/* the relaxation XX:1377-1545 with the forces on nthreads OpenMP threads */
+int64_t or_lsm_relax_par(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol, int nthreads);
+/* the coupled driver's spring dynamics lsm_step (S1:1721-1903): nsteps of
+ * velocity Verlet with the external load (or_lsm_set_load) as afdat,
+ * accelerations F rsi and damping a -= damp v */
+void or_lsm_dyn_step(or_lsm *o, int64_t nsteps, double dt, double rsi, double damp, int nthreads);
+void or_lsm_get_dyn(const or_lsm *o, double *r, double *v, double *a);
 /* external nodal load (3, ns) added to the CG right-hand side; NULL = none */
 void or_lsm_set_load(or_lsm *o, const double *f);
 void or_lsm_get_disp(const or_lsm *o, double *u);

@@ -387,7 +387,136 @@ static void forces(const or_lsm *o, const double *u, double *a, int linear)
 
 void or_lsm_forces(const or_lsm *o, const double *u, double *a) { forces(o, u, a, 0); }
 
-int64_t or_lsm_relax(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol)
+/* The same forces on `nthreads` OpenMP threads, scheduled as the reference
+ * schedules its force loops (XX:1406-1500, S1:1785-1879): the bond and the
+ * angle lists are cut into 2*nthreads chunks and the odd chunks run before
+ * the even ones, so that no two chunks that run together touch the same
+ * node.  Chunks are whole node slabs of the slowest axis (z; the tables are
+ * in node order), at least two slabs wide; with fewer slabs than that the
+ * serial loop runs.  Sums at chunk borders add in another order than the
+ * serial loop. */
+static void forces_par(const or_lsm *o, const double *u, double *a, int linear, int nthreads)
+{
+  const int nzn = o->M[2];
+  int nch = 2 * nthreads;
+  while (nch > 1 && nzn / nch < 2) nch -= 2;
+  if (nthreads <= 1 || nch < 2) {
+    forces(o, u, a, linear);
+    return;
+  }
+  memset(a, 0, sizeof(double) * 3 * o->ns);
+  /* chunk c: elements whose first node (bonds) or centre node (angles) lies
+   * in z slabs [c*nzn/nch, (c+1)*nzn/nch) */
+  int64_t *bcut = (int64_t *)calloc(nch + 1, sizeof(int64_t)), *acut = (int64_t *)calloc(nch + 1, sizeof(int64_t));
+  for (int c = 0; c <= nch; c++) {
+    const int zc = (int)((int64_t)c * nzn / nch) + 1; /* 1-based slab */
+    int64_t lo = 0, hi = o->nbo;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (o->icors[3 * (o->bon[3 * mid] - 1) + 2] < zc) lo = mid + 1; else hi = mid;
+    }
+    bcut[c] = c == nch ? o->nbo : lo;
+    lo = 0, hi = o->nna;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (o->icors[3 * (o->ang[6 * mid] - 1) + 2] < zc) lo = mid + 1; else hi = mid;
+    }
+    acut[c] = c == nch ? o->nna : lo;
+  }
+  for (int parity = 0; parity < 2; parity++) {
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1)
+    for (int c = parity; c < nch; c += 2) {
+      for (int64_t i = bcut[c]; i < bcut[c + 1]; i++) {
+        const int32_t *b = o->bon + 3 * i;
+        const double *xn = o->bn[b[2] - 1], *rn = o->vb[b[2] - 1];
+        const double *u1 = u + 3 * (b[0] - 1), *u2 = u + 3 * (b[1] - 1);
+        double rt[3], f[3];
+        for (int d = 0; d < 3; d++) rt[d] = linear ? u2[d] - u1[d] : u2[d] - u1[d] + rn[d];
+        const double sd = rt[0] * xn[0] + rt[1] * xn[1] + rt[2] * xn[2];
+        for (int d = 0; d < 3; d++) f[d] = o->sbond[i] * (linear ? sd * xn[d] : sd * xn[d] - rn[d]);
+        for (int d = 0; d < 3; d++) {
+          a[3 * (b[0] - 1) + d] += f[d];
+          a[3 * (b[1] - 1) + d] -= f[d];
+        }
+      }
+      for (int64_t i = acut[c]; i < acut[c + 1]; i++) {
+        const int32_t *g = o->ang + 6 * i;
+        const double *xrj = o->vx[g[3] - 1], *xrk = o->vx[g[4] - 1];
+        double rtj[3], rtk[3];
+        const double *ui = u + 3 * (g[0] - 1), *uj = u + 3 * (g[1] - 1), *uk = u + 3 * (g[2] - 1);
+        for (int d = 0; d < 3; d++) {
+          rtj[d] = linear ? uj[d] - ui[d] : uj[d] - ui[d] + CV[g[3] - 1][d];
+          rtk[d] = linear ? uk[d] - ui[d] : uk[d] - ui[d] + CV[g[4] - 1][d];
+        }
+        const double *an = o->anf[g[5] - 1];
+        const double dfi = ((xrk[1] * rtk[2] - xrk[2] * rtk[1] - xrj[1] * rtj[2] + xrj[2] * rtj[1]) * an[0] -
+                            (xrk[0] * rtk[2] - xrk[2] * rtk[0] - xrj[0] * rtj[2] + xrj[2] * rtj[0]) * an[1] +
+                            (xrk[0] * rtk[1] - xrk[1] * rtk[0] - xrj[0] * rtj[1] + xrj[1] * rtj[0]) * an[2]) *
+                           o->abond[i];
+        for (int d = 0; d < 3; d++) {
+          a[3 * (g[1] - 1) + d] += dfi * an[3 + d];
+          a[3 * (g[2] - 1) + d] += dfi * an[6 + d];
+          a[3 * (g[0] - 1) + d] -= dfi * an[3 + d] + dfi * an[6 + d];
+        }
+      }
+    }
+  }
+  free(bcut);
+  free(acut);
+  for (int64_t t = 0; t < o->ntie; t++) {
+    double *a1 = a + 3 * (o->tie[2 * t] - 1), *a2 = a + 3 * (o->tie[2 * t + 1] - 1);
+    for (int d = 0; d < 3; d++) {
+      a1[d] = a1[d] + a2[d];
+      a2[d] = a1[d];
+    }
+  }
+}
+
+/* nsteps of the coupled driver's spring dynamics, lsm_step S1:1721-1903:
+ * velocity Verlet with the fluid's wall load afdat (the external load of
+ * or_lsm_set_load, already an acceleration: S1 forms it with rsdti2 = rsi
+ * dti^2, S1:3413) added to both half kicks, spring accelerations F rsi and
+ * viscous damping a -= damp v (damp = 0.25 at S1:1888; the standalone
+ * relaxation XX:1533 uses 0.5 and no load).  The load of a tied duplicate
+ * plane acts on both nodes of the pair, as the tied forces do.  State: the
+ * handle's r, v, a (r starts with the jump).  nthreads > 1 evaluates the
+ * forces on that many threads (forces_par). */
+void or_lsm_dyn_step(or_lsm *o, int64_t nsteps, double dt, double rsi, double damp, int nthreads)
+{
+  const int64_t n3 = 3 * o->ns;
+  double *f = (double *)calloc(n3 + 3, sizeof(double));
+  if (o->load) {
+    memcpy(f, o->load, sizeof(double) * n3);
+    for (int64_t t = 0; t < o->ntie; t++) {
+      double *f1 = f + 3 * (o->tie[2 * t] - 1), *f2 = f + 3 * (o->tie[2 * t + 1] - 1);
+      for (int d = 0; d < 3; d++) {
+        f1[d] = f1[d] + f2[d];
+        f2[d] = f1[d];
+      }
+    }
+  }
+  for (int64_t it = 0; it < nsteps; it++) {
+    for (int64_t i = 0; i < n3; i++) o->v[i] = o->v[i] + o->a[i] * dt * 0.5 + f[i] * dt * 0.5;
+    for (int64_t i = 0; i < n3; i++) o->r[i] = o->r[i] + o->v[i] * dt;
+    forces_par(o, o->r, o->a, 0, nthreads);
+    for (int64_t i = 0; i < n3; i++) o->a[i] = o->a[i] * rsi;
+    for (int64_t i = 0; i < n3; i++) o->a[i] = o->a[i] - damp * o->v[i];
+    for (int64_t i = 0; i < n3; i++) o->v[i] = o->v[i] + o->a[i] * dt * 0.5 + f[i] * dt * 0.5;
+  }
+  free(f);
+}
+
+/* r, v, a of the dynamics (3, ns each, node order); NULL skips one */
+void or_lsm_get_dyn(const or_lsm *o, double *r, double *v, double *a)
+{
+  if (r) memcpy(r, o->r, sizeof(double) * 3 * o->ns);
+  if (v) memcpy(v, o->v, sizeof(double) * 3 * o->ns);
+  if (a) memcpy(a, o->a, sizeof(double) * 3 * o->ns);
+}
+
+static void forces_par(const or_lsm *o, const double *u, double *a, int linear, int nthreads);
+
+static int64_t relax_impl(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol, int nthreads)
 {
   const int64_t n3 = 3 * o->ns;
   const double rsi = 1.0 / rs;
@@ -395,7 +524,7 @@ int64_t or_lsm_relax(or_lsm *o, double dt, double rs, double damp, int64_t maxst
   for (; it < maxsteps; it++) {
     for (int64_t i = 0; i < n3; i++) o->v[i] = o->v[i] + o->a[i] * dt * 0.5;
     for (int64_t i = 0; i < n3; i++) o->r[i] = o->r[i] + o->v[i] * dt;
-    forces(o, o->r, o->a, 0);
+    forces_par(o, o->r, o->a, 0, nthreads);
     double fmax = 0.0;
     for (int64_t i = 0; i < n3; i++) {
       double f = fabs(o->a[i]);
@@ -412,10 +541,20 @@ int64_t or_lsm_relax(or_lsm *o, double dt, double rs, double damp, int64_t maxst
   return it;
 }
 
+int64_t or_lsm_relax(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol)
+{
+  return relax_impl(o, dt, rs, damp, maxsteps, ftol, 1);
+}
+
+int64_t or_lsm_relax_par(or_lsm *o, double dt, double rs, double damp, int64_t maxsteps, double ftol, int nthreads)
+{
+  return relax_impl(o, dt, rs, damp, maxsteps, ftol, nthreads);
+}
+
 /* FP64 CG on the tied system: unknowns are the displacements of all nodes
  * except the second plane of each tied pair, which follows its partner plus
  * the jump.  A = E^T K E, b = E^T F(J) with F the linear spring forces. */
-int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres)
+static int64_t cg_impl(or_lsm *o, double rtol, int64_t maxit, double *relres, int nthreads)
 {
   const int64_t ns = o->ns, n3 = 3 * ns;
   char *dup = (char *)calloc(ns + 1, 1);
@@ -457,7 +596,7 @@ int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres)
   while (it < maxit && rr > rtol * rtol * bb) {
     for (int64_t i = 0; i < ns; i++)
       for (int d = 0; d < 3; d++) full[3 * i + d] = dup[i] ? p[3 * partner[i] + d] : p[3 * i + d];
-    forces(o, full, f, 1);
+    forces_par(o, full, f, 1, nthreads);
     for (int64_t i = 0; i < ns; i++)
       for (int d = 0; d < 3; d++) q[3 * i + d] = dup[i] ? 0.0 : -f[3 * i + d];
     double pq = 0.0;
@@ -486,6 +625,16 @@ int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres)
     }
   free(dup); free(partner); free(x); free(r); free(p); free(q); free(full); free(f);
   return it;
+}
+
+int64_t or_lsm_cg(or_lsm *o, double rtol, int64_t maxit, double *relres)
+{
+  return cg_impl(o, rtol, maxit, relres, 1);
+}
+
+int64_t or_lsm_cg_par(or_lsm *o, double rtol, int64_t maxit, double *relres, int nthreads)
+{
+  return cg_impl(o, rtol, maxit, relres, nthreads);
 }
 
 /* the derived angle table (48 x 9) and the cube-local tables as generated

@@ -250,3 +250,34 @@ def test_generated_cube_constants_are_current(tmp_path):
     subprocess.run([cxx, "-O2", "-I" + csrc, os.path.join(csrc, "gen_cube_const.cpp"), "-o", exe], check=True)
     out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     assert out == open(os.path.join(csrc, "lsm_cube_const.h")).read()
+
+
+def test_threaded_spring_forces_match_serial(oracle_lib):
+    """The OpenMP force evaluation (odd/even slab chunks, as the reference
+    schedules its force loops) gives the serial CG's iterations and modulus
+    up to summation order, and the same dynamics trajectory."""
+    ind = geo.inclusions(12, 0.25, 2.5, seed=5)
+    g = 0.006
+    a = oracle_lib.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    b = oracle_lib.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    ia, ra = a.cg(1e-10, 10000)
+    ib, rb = b.cg(1e-10, 10000, nthreads=4)
+    assert ia == ib
+    assert b.stress()["modulus"] == pytest.approx(a.stress()["modulus"], rel=1e-12)
+    c = oracle_lib.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    d = oracle_lib.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    c.dyn_step(30, 0.1, 1.0, 0.5)
+    d.dyn_step(30, 0.1, 1.0, 0.5, nthreads=4)
+    rc, rd = c.dyn_state()[0], d.dyn_state()[0]
+    assert np.abs(rc - rd).max() <= 1e-12 * np.abs(rc).max()
+
+
+def test_dynamics_without_load_is_the_relaxation(oracle_lib):
+    """lsm_step's Verlet scheme (S1:1721-1903) with no fluid load and the
+    standalone damping 0.5 is the relaxation of XX:1377-1545, step for step."""
+    ind = geo.inclusions(8, 0.25, 2.0, seed=3)
+    a = oracle_lib.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, 0.004, 0)
+    b = oracle_lib.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, 0.004, 0)
+    assert a.relax(0.1, 1.0, 0.5, 40, 0.0) == 40
+    b.dyn_step(40, 0.1, 1.0, 0.5)
+    assert np.array_equal(a.disp(), b.dyn_state()[0])
