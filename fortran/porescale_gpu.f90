@@ -13,7 +13,7 @@ module porescale_gpu
 
   integer(c_int), parameter :: PS_OK = 0
   integer(c_int), parameter :: PS_PREC_F64 = 0, PS_PREC_F32 = 1, PS_PREC_F16 = 2, PS_PREC_BF16 = 3
-  integer(c_int), parameter :: PS_LOAD_XSTRETCH = 0, PS_LOAD_YZSHEAR = 1
+  integer(c_int), parameter :: PS_LOAD_XSTRETCH = 0, PS_LOAD_YZSHEAR = 1, PS_LOAD_NONE = 2
   integer(c_int), parameter :: PS_LSM_F64 = 0, PS_LSM_MIXED = 1
 
   ! ps_lbm_params: the LBM block of INPUT_PARAMETERS (S1:435-469)
@@ -280,6 +280,26 @@ module porescale_gpu
       import :: c_int, c_double, c_ptr
       type(c_ptr), value :: handle, d_u
       real(c_double), intent(out) :: out(10)
+    end function
+    ! the coupled driver's lsm_step (S1:1721-1903): nsteps of damped velocity
+    ! Verlet under the wall load of ps_lsm_set_wall_load
+    integer(c_int) function ps_lsm_dyn_step(handle, nsteps, dt, rsi, damp) bind(c, name='ps_lsm_dyn_step')
+      import :: c_int, c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: nsteps
+      real(c_double), value :: dt, rsi, damp
+    end function
+    ! rdat, vdat, adat (3, ns) in and out of the dynamic state (the
+    ! iteration checkpoint of the coupled driver)
+    integer(c_int) function ps_lsm_set_dyn_state(handle, rdat, vdat, adat) bind(c, name='ps_lsm_set_dyn_state')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(in) :: rdat(3, *), vdat(3, *), adat(3, *)
+    end function
+    integer(c_int) function ps_lsm_get_dyn_state(handle, rdat, vdat, adat) bind(c, name='ps_lsm_get_dyn_state')
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: handle
+      real(c_double), intent(out) :: rdat(3, *), vdat(3, *), adat(3, *)
     end function
     integer(c_int) function ps_lsm_destroy(handle) bind(c, name='ps_lsm_destroy')
       import :: c_int, c_ptr

@@ -185,6 +185,9 @@ void *ps_batch_stream(void *handle);
 /* ---- lattice-spring static solve (hot path b) ---- */
 #define PS_LOAD_XSTRETCH 0 /* x stretch with tied x faces: Cxxxx (XX_P.f) */
 #define PS_LOAD_YZSHEAR 1  /* yz shear with tied y faces: Cyzyz (YZ_P.f)  */
+#define PS_LOAD_NONE 2     /* no tie, no imposed strain (gstrain must be 0),
+                              every axis periodic: the coupled driver's network
+                              (S1:541-660), nodes in its k-j-i order            */
 #define PS_LSM_F64 0       /* FP64 conjugate gradient                                */
 #define PS_LSM_MIXED 1     /* FP32 CG inside FP64 iterative refinement              */
 
@@ -272,6 +275,30 @@ int ps_lsm_set_wall_load(void *handle, void *lattice, double rsi);
  * solid.  The reference evaluates them with pres = 0.01 rr0 cr2 (S1:3987). */
 int ps_lsm_alpha_beta(void *handle, const int32_t *lab, int32_t npores, int32_t iipore, double pres, double *alpha,
                       double *beta);
+
+/* Damped spring dynamics of the coupled driver: nsteps of lsm_step
+ * (S1:1721-1903, called once per fluid step at S1:1884), velocity Verlet
+ *   v += a dt/2 + afdat dt/2;  r += v dt;  a = F(r) rsi;  a -= damp v;
+ *   v += a dt/2 + afdat dt/2
+ * with F the spring forces (the imposed jump included), afdat the wall load
+ * set by ps_lsm_set_wall_load (used as given, an acceleration: the lattice
+ * forms it with rsi / dt^2, S1:3413; none when unset) and damp = 0.25 in S1
+ * (0.5 with dt = 0.01 and no load is the standalone relaxation of
+ * XX:1377-1545).  The state (r, v, a) starts at zero displacement (the
+ * jump on the tied plane) and rest unless ps_lsm_set_dyn_state set it; r is
+ * the handle's displacement, so ps_lsm_get_disp and ps_lsm_alpha_beta see
+ * it (a later ps_lsm_solve replaces it by the static solution).  FP64 on
+ * the GPU in either solve precision.  The spring forces are the linear
+ * operator of the static solve (the reference's bond term -rn cancels up to
+ * rounding). */
+int ps_lsm_dyn_step(void *handle, int32_t nsteps, double dt, double rsi, double damp);
+/* r, v, a (3 x ns each, the reference's node order as ps_lsm_get_disp; a
+ * tied duplicate node follows its partner, r plus the jump) into the
+ * dynamic state; NULL sets that vector to zero.  The `iteration` checkpoint
+ * of the coupled driver (S1:3951-3960) restarts through this call. */
+int ps_lsm_set_dyn_state(void *handle, const double *r, const double *v, const double *a);
+/* the dynamic state in the same layout; NULL skips a vector */
+int ps_lsm_get_dyn_state(void *handle, double *r, double *v, double *a);
 
 /* Largest box (voxel cubes) ps_lsm_stress_noalloc accepts: 128^3. */
 #define PS_LSM_NOALLOC_MAX_CUBES (2 * 1024 * 1024)

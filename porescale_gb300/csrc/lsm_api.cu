@@ -59,6 +59,10 @@ struct Springs {
   // FP32 inner vectors
   float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
   double *part = nullptr, *scal = nullptr;
+  // damped dynamics (ps_lsm_dyn_step): velocity and acceleration [3][nvox]
+  // (the displacement is x) and the spring forces of the jump alone
+  double *dv = nullptr, *da = nullptr, *bj = nullptr;
+  bool periodic = false;  // PS_LOAD_NONE: no tied plane, every axis periodic
   unsigned* ctr = nullptr;  // last-CTA counter of the CG reductions
   int nblk = 0;
   bool solved = false;
@@ -92,6 +96,9 @@ void free_springs(Springs* S)
   cudaFree(S->p32);
   cudaFree(S->q32);
   cudaFree(S->ctr);
+  cudaFree(S->dv);
+  cudaFree(S->da);
+  cudaFree(S->bj);
   cudaFree(S->part);
   cudaFree(S->scal);
   if (S->g64.exec) cudaGraphExecDestroy(S->g64.exec);
@@ -620,6 +627,61 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
   return r;
 }
 
+// Calls f(k, v, dup) for the reference's nodes k = 0, 1, ... in their order:
+// k-j-i over the node grid, which for a tied load has the loaded axis padded
+// to planes 0..N (plane N duplicates plane 0 plus the jump, XX:446-523) and
+// for PS_LOAD_NONE is the periodic box (S1:541-602).  v is the node's box
+// index, dup marks a node on the duplicate plane.  A node exists when one of
+// its cubes is solid; along the loaded axis there are no cubes beyond the
+// ends (no wrap there).
+template <typename F>
+void for_ref_nodes(const Springs* S, F f)
+{
+  const int n3[3] = {S->nx, S->ny, S->nz};
+  const int pad = S->periodic ? -1 : S->pa;
+  const int M[3] = {S->nx + (pad == 0 ? 1 : 0), S->ny + (pad == 1 ? 1 : 0), S->nz};
+  long long k = 0;
+  for (int z = 0; z < M[2]; z++)
+    for (int y = 0; y < M[1]; y++)
+      for (int xx = 0; xx < M[0]; xx++) {
+        const int c[3] = {xx, y, z};
+        int w[3];
+        for (int d = 0; d < 3; d++) w[d] = c[d] % n3[d];
+        const int v = w[0] + S->nx * (w[1] + S->ny * w[2]);
+        bool exists = false;
+        for (int e = 0; e < 8 && !exists; e++) {
+          int cc[3];
+          bool ok = true;
+          for (int d = 0; d < 3; d++) {
+            cc[d] = c[d] - ((e >> d) & 1);
+            if (d == pad) ok = ok && cc[d] >= 0 && cc[d] < n3[d];
+            else cc[d] = (cc[d] + n3[d]) % n3[d];
+          }
+          exists = ok && S->mat[cc[0] + S->nx * (cc[1] + S->ny * cc[2])] != 0;
+        }
+        if (!exists) continue;
+        f(k, v, pad >= 0 && c[pad] == n3[pad]);
+        k++;
+      }
+}
+
+// velocity, acceleration and jump-force vectors of the dynamics, allocated
+// (velocity and acceleration zero) on first use
+int ensure_dyn(Springs* S)
+{
+  if (S->dv) return PS_OK;
+  const size_t b64 = sizeof(double) * 3 * (size_t)S->nvox;
+  if (int r = dalloc(S, &S->dv, b64)) return r;
+  if (int r = dalloc(S, &S->da, b64)) return r;
+  if (int r = dalloc(S, &S->bj, b64)) return r;
+  PS_CUDA(cudaMemsetAsync(S->dv, 0, b64, S->stream));
+  PS_CUDA(cudaMemsetAsync(S->da, 0, b64, S->stream));
+  lsm::k_lsm_rhs<<<blocks_for(S->nvox), kBlk, 0, S->stream>>>(S->geom(), S->pa, S->jc, 2.0 * S->p.gstrain, S->bj);
+  PS_CUDA(cudaGetLastError());
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  return PS_OK;
+}
+
 }  // namespace
 }  // namespace ps
 
@@ -633,7 +695,10 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   *handle = nullptr;
   if (nx < 2 || ny < 2 || nz < 2) return fail(PS_ERR_ARG, "ps_lsm_create: box %d x %d x %d too small", nx, ny, nz);
   if ((long long)nx * ny * nz * 3 > (1LL << 31) - 1) return fail(PS_ERR_ARG, "ps_lsm_create: box too large");
-  if (p->load != PS_LOAD_XSTRETCH && p->load != PS_LOAD_YZSHEAR) return fail(PS_ERR_ARG, "ps_lsm_create: bad load %d", p->load);
+  if (p->load != PS_LOAD_XSTRETCH && p->load != PS_LOAD_YZSHEAR && p->load != PS_LOAD_NONE)
+    return fail(PS_ERR_ARG, "ps_lsm_create: bad load %d", p->load);
+  if (p->load == PS_LOAD_NONE && p->gstrain != 0.0)
+    return fail(PS_ERR_ARG, "ps_lsm_create: PS_LOAD_NONE imposes no strain (gstrain must be 0)");
   if (p->precision != PS_LSM_F64 && p->precision != PS_LSM_MIXED)
     return fail(PS_ERR_ARG, "ps_lsm_create: bad precision %d", p->precision);
   int ndev = 0;
@@ -644,8 +709,11 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   S->ny = ny;
   S->nz = nz;
   S->nvox = nx * ny * nz;
-  S->pa = p->load == PS_LOAD_XSTRETCH ? 0 : 1;
-  S->jc = p->load == PS_LOAD_XSTRETCH ? 0 : 2;
+  // PS_LOAD_NONE: the x-stretch layout with a zero jump; only the node
+  // order of the state calls differs (no duplicate plane)
+  S->pa = p->load == PS_LOAD_YZSHEAR ? 1 : 0;
+  S->jc = p->load == PS_LOAD_YZSHEAR ? 2 : 0;
+  S->periodic = p->load == PS_LOAD_NONE;
   const int nv = S->nvox;
   S->mat.assign(nv, 0);
   S->node.assign(nv, 0);
@@ -714,6 +782,7 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   PS_CUDA(cudaMemcpyAsync(S->d_K32, K32.data(), sizeof(float) * K32.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_S64, S64.data(), sizeof(double) * S64.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_Kab, Kab.data(), sizeof(double) * Kab.size(), cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaMemsetAsync(S->x, 0, b64, S->stream));  // the dynamic state starts at zero displacement
   PS_CUDA(cudaStreamSynchronize(S->stream));
   *handle = S.release();
   return PS_OK;
@@ -1023,36 +1092,77 @@ int ps_lsm_get_disp(void* h, double* u)
   std::vector<double> x((size_t)3 * nv);
   PS_CUDA(cudaMemcpyAsync(x.data(), S->x, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, S->stream));
   PS_CUDA(cudaStreamSynchronize(S->stream));
-  // reference node order: k-j-i over the padded node grid, the loaded axis
-  // having node planes 1..N+1 (plane N+1 = plane 1 + jump)
-  const int M[3] = {S->nx + (S->pa == 0 ? 1 : 0), S->ny + (S->pa == 1 ? 1 : 0), S->nz};
-  const int n3[3] = {S->nx, S->ny, S->nz};
-  long long k = 0;
-  for (int z = 0; z < M[2]; z++)
-    for (int y = 0; y < M[1]; y++)
-      for (int xx = 0; xx < M[0]; xx++) {
-        const int c[3] = {xx, y, z};
-        int w[3];
-        for (int d = 0; d < 3; d++) w[d] = c[d] % n3[d];
-        const int v = w[0] + S->nx * (w[1] + S->ny * w[2]);
-        // the reference's node exists when one of its cubes is solid, cubes
-        // beyond the ends of the loaded axis being pore (no wrap there)
-        bool exists = false;
-        for (int e = 0; e < 8 && !exists; e++) {
-          int cc[3];
-          bool ok = true;
-          for (int d = 0; d < 3; d++) {
-            cc[d] = c[d] - ((e >> d) & 1);
-            if (d == S->pa) ok = ok && cc[d] >= 0 && cc[d] < n3[d];
-            else cc[d] = (cc[d] + n3[d]) % n3[d];
-          }
-          exists = ok && S->mat[cc[0] + S->nx * (cc[1] + S->ny * cc[2])] != 0;
-        }
-        if (!exists) continue;
-        const bool dup = c[S->pa] == n3[S->pa];
-        for (int d = 0; d < 3; d++) u[3 * k + d] = x[(size_t)d * nv + v] + (dup && d == S->jc ? 2.0 * S->p.gstrain : 0.0);
-        k++;
-      }
+  const double jump = 2.0 * S->p.gstrain;
+  for_ref_nodes(S, [&](long long k, int v, bool dup) {
+    for (int d = 0; d < 3; d++) u[3 * k + d] = x[(size_t)d * nv + v] + (dup && d == S->jc ? jump : 0.0);
+  });
+  return PS_OK;
+}
+
+int ps_lsm_set_dyn_state(void* h, const double* r, const double* v, const double* a)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lsm_set_dyn_state: null handle");
+  Springs* S = static_cast<Springs*>(h);
+  if (int e = ensure_dyn(S)) return e;
+  const int nv = S->nvox;
+  double* dst[3] = {S->x, S->dv, S->da};
+  const double* src[3] = {r, v, a};
+  std::vector<double> box((size_t)3 * nv);
+  for (int q = 0; q < 3; q++) {
+    std::fill(box.begin(), box.end(), 0.0);
+    if (src[q])
+      for_ref_nodes(S, [&](long long k, int vv, bool dup) {
+        if (dup) return;  // follows its partner
+        for (int d = 0; d < 3; d++) box[(size_t)d * nv + vv] = src[q][3 * k + d];
+      });
+    PS_CUDA(cudaMemcpyAsync(dst[q], box.data(), sizeof(double) * box.size(), cudaMemcpyHostToDevice, S->stream));
+    PS_CUDA(cudaStreamSynchronize(S->stream));
+  }
+  S->solved = true;
+  return PS_OK;
+}
+
+int ps_lsm_get_dyn_state(void* h, double* r, double* v, double* a)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lsm_get_dyn_state: null handle");
+  Springs* S = static_cast<Springs*>(h);
+  if (int e = ensure_dyn(S)) return e;
+  const int nv = S->nvox;
+  const double jump = 2.0 * S->p.gstrain;
+  const double* src[3] = {S->x, S->dv, S->da};
+  double* dst[3] = {r, v, a};
+  std::vector<double> box((size_t)3 * nv);
+  for (int q = 0; q < 3; q++) {
+    if (!dst[q]) continue;
+    PS_CUDA(cudaMemcpyAsync(box.data(), src[q], sizeof(double) * box.size(), cudaMemcpyDeviceToHost, S->stream));
+    PS_CUDA(cudaStreamSynchronize(S->stream));
+    for_ref_nodes(S, [&](long long k, int vv, bool dup) {
+      for (int d = 0; d < 3; d++)
+        dst[q][3 * k + d] = box[(size_t)d * nv + vv] + (q == 0 && dup && d == S->jc ? jump : 0.0);
+    });
+  }
+  return PS_OK;
+}
+
+int ps_lsm_dyn_step(void* h, int32_t nsteps, double dt, double rsi, double damp)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lsm_dyn_step: null handle");
+  if (nsteps < 0 || !(dt > 0.0) || !std::isfinite(dt) || !std::isfinite(rsi) || !std::isfinite(damp))
+    return fail(PS_ERR_ARG, "ps_lsm_dyn_step: need nsteps >= 0, dt > 0 and finite rsi, damp");
+  Springs* S = static_cast<Springs*>(h);
+  if (int e = ensure_dyn(S)) return e;
+  const int nv = S->nvox, n3 = 3 * nv;
+  const int nb = blocks_for(nv), nb3 = blocks_for(n3);
+  const double* f = S->has_load ? S->fext : nullptr;
+  const double* bj = S->p.gstrain != 0.0 ? S->bj : nullptr;
+  for (int s = 0; s < nsteps; s++) {
+    lsm::k_dyn_kick_drift<<<nb3, kBlk, 0, S->stream>>>(n3, dt, f, S->x, S->dv, S->da);
+    lsm::k_lsm_matvec<double, kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
+    lsm::k_dyn_force_kick<<<nb3, kBlk, 0, S->stream>>>(n3, dt, rsi, damp, bj, S->q64, f, S->dv, S->da);
+  }
+  PS_CUDA(cudaGetLastError());
+  PS_CUDA(cudaStreamSynchronize(S->stream));
+  S->solved = true;
   return PS_OK;
 }
 

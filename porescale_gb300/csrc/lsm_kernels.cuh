@@ -298,6 +298,38 @@ __global__ void __launch_bounds__(BLK) k_lsm_energy(const LsmGeom G, int pa, int
   }
 }
 
+// ---- damped spring dynamics (lsm_step, S1:1721-1903) ------------------------
+// One velocity-Verlet step is three launches: k_dyn_kick_drift, the FP64
+// matvec q = K u (k_lsm_matvec), k_dyn_force_kick.  u, v, a: displacement,
+// velocity, acceleration [3][nvox]; f: the fluid wall load afdat (already
+// an acceleration) or null; bj: the spring forces of the imposed jump alone
+// (k_lsm_rhs) or null, so that the spring force at u is bj - K u.
+// Expressions keep the reference's order: v + a dt/2 + f dt/2.
+__global__ void k_dyn_kick_drift(int n3, double dt, const double* __restrict__ f, double* __restrict__ u,
+                                 double* __restrict__ v, const double* __restrict__ a)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  double vi = v[i] + a[i] * dt * 0.5;
+  if (f) vi = vi + f[i] * dt * 0.5;
+  v[i] = vi;
+  u[i] = u[i] + vi * dt;
+}
+__global__ void k_dyn_force_kick(int n3, double dt, double rsi, double damp, const double* __restrict__ bj,
+                                 const double* __restrict__ q, const double* __restrict__ f,
+                                 double* __restrict__ v, double* __restrict__ a)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  const double F = bj ? bj[i] - q[i] : -q[i];  // spring force at u
+  const double vi = v[i];
+  const double ai = F * rsi - damp * vi;       // acceleration, then the viscous term (S1:1888)
+  a[i] = ai;
+  double vn = vi + ai * dt * 0.5;
+  if (f) vn = vn + f[i] * dt * 0.5;
+  v[i] = vn;
+}
+
 // ---- CG vector kernels (device-resident scalars, no host round trips) ----
 // scal[]: 0 rr, 1 pq, 2 alpha, 3 beta, 4 rr_new, 5 bb (|b|^2), 6 done flag
 __global__ void k_sum(const double* __restrict__ part, int n, double* __restrict__ out)

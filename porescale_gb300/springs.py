@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib
 from ._lib import check, dptr, iptr
 
-LOAD_XSTRETCH, LOAD_YZSHEAR = 0, 1
+LOAD_XSTRETCH, LOAD_YZSHEAR, LOAD_NONE = 0, 1, 2
 LSM_F64, LSM_MIXED = 0, 1
 
 
@@ -46,6 +46,11 @@ _SIGS = {
     "ps_lsm_get_disp": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ps_lsm_stream": (C.c_void_p, [C.c_void_p]),
     "ps_lsm_stress_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "ps_lsm_dyn_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double]),
+    "ps_lsm_set_dyn_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
+    "ps_lsm_get_dyn_state": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
     "ps_lsm_gradients": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "ps_lsm_batch_solve": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_double, C.c_int32, C.POINTER(LsmResult)]),
     "ps_lsm_set_wall_load": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
@@ -108,6 +113,22 @@ class SpringNetwork:
         u = np.zeros((ns, 3))
         check(self._lib.ps_lsm_get_disp(self._h, dptr(u)))
         return u
+
+    def dyn_step(self, nsteps: int, dt: float = 1.0, rsi: float = 1.0, damp: float = 0.25) -> None:
+        """nsteps of the coupled driver's damped spring dynamics (lsm_step,
+        S1:1721-1903) under the wall load set by set_wall_load."""
+        check(self._lib.ps_lsm_dyn_step(self._h, int(nsteps), float(dt), float(rsi), float(damp)))
+
+    def set_dyn_state(self, r=None, v=None, a=None) -> None:
+        """(ns, 3) arrays in the reference node order; None = zero."""
+        arrs = [None if x is None else np.ascontiguousarray(x, np.float64) for x in (r, v, a)]
+        check(self._lib.ps_lsm_set_dyn_state(self._h, *[None if x is None else dptr(x) for x in arrs]))
+
+    def dyn_state(self, ns: int):
+        """(r, v, a), each (ns, 3) in the reference node order."""
+        out = [np.zeros((ns, 3)) for _ in range(3)]
+        check(self._lib.ps_lsm_get_dyn_state(self._h, *[dptr(x) for x in out]))
+        return tuple(out)
 
     def gradients(self) -> np.ndarray:
         """d modulus / d(alf1, bet1, alf2, bet2) at the last converged
