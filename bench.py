@@ -207,14 +207,14 @@ def cpu_oracle_mlups(ind, p, fr, fb, threads: int, budget_s: float):
     return nl * n / dt / 1e6, n, dt
 
 
-def lsm_leg(size=64, seed=20240601, cpu_iters=0):
+def lsm_leg(size=64, seed=20240601, cpu_budget=0.0):
     """Lattice-spring static solve on the two-solid cube (matrix alpha 1.0,
     beta 0.4; radius-5 inclusions at volume fraction 0.25, alpha 0.3, beta
     0.1; strain 1e-3): Cxxxx and Cyzyz by FP64 CG and by FP32 CG in FP64
     refinement, CG iterations per second and the inner iteration's
     bandwidth (133 algorithmic bytes per node per FP32 iteration, 265 for
-    FP64).  cpu_iters > 0 also times that many iterations of the oracle's
-    FP64 CG (one host thread) on the Cxxxx system as the CPU baseline."""
+    FP64).  cpu_budget > 0 also times the oracle on all host cores, about
+    cpu_budget seconds for each of the two CPU algorithms (lsm_cpu_baseline)."""
     from porescale_gb300 import geometry
     from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, LSM_MIXED, SpringNetwork
     ind = geometry.inclusions(size, 0.25, 5.0, seed)
@@ -237,18 +237,107 @@ def lsm_leg(size=64, seed=20240601, cpu_iters=0):
                                           "frac": its * r.nnode * bpn / dt / 1e9 / peak}
         out[f"{name}_rel_diff_mixed_vs_f64"] = abs(out[f"{name}_mixed"]["modulus"] - out[f"{name}_f64"]["modulus"]) / \
             abs(out[f"{name}_f64"]["modulus"])
-    if cpu_iters > 0:
-        import oracle
-        o = oracle.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
-        t = time.perf_counter()
-        its, _ = o.cg(1e-10, cpu_iters)
-        dt = time.perf_counter() - t
-        o.close()
-        out["cpu_baseline"] = {"value": its / dt, "unit": "CG iterations/s", "cores": 1, "kind": "port",
-                               "sample": f"first {its} FP64 CG iterations of the Cxxxx system ({dt:.1f} s, "
-                                         "C restatement of the spring forces)"}
-        out["f64_vs_cpu"] = out["Cxxxx_f64"]["cg_iters_per_s"] / out["cpu_baseline"]["value"]
+    if cpu_budget > 0:
+        out["cpu_baseline"] = lsm_cpu_baseline(ind, g, cpu_budget, out["Cxxxx_f64"])
     return out
+
+
+# the standalone relaxation's parameters in the reference's shipped input
+# (LSM2S/Cxxxx/INPUT_PARAMETERS: dt 0.01, rs 1; damping 0.5 at XX:1533)
+DR_DT, DR_RS, DR_DAMP = 0.01, 1.0, 0.5
+
+
+def lsm_cpu_baseline(ind, g, budget, gpu_f64):
+    """The spring solve's CPU baselines on all host cores (OpenMP, the
+    reference's odd/even slab scheduling of its force loops): the oracle's
+    FP64 CG (iterations/s; the solve needs the GPU FP64 CG's iteration
+    count) and the reference's own algorithm, the damped Verlet relaxation
+    XX:1377-1545 at its shipped dt 0.01 (steps/s; the steps it needs to
+    reach the CG's residual come from the committed GPU run of the same
+    dynamics, profiles/lsm_dr_64.json).  Each is a bounded sample of about
+    `budget` seconds on the Cxxxx system."""
+    import oracle
+    threads = os.cpu_count() or 1
+    out = {}
+    o = oracle.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    t = time.perf_counter()
+    o.cg(1e-10, 3, nthreads=threads)
+    per = max((time.perf_counter() - t) / 3, 1e-6)
+    o.close()
+    o = oracle.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    t = time.perf_counter()
+    its, _ = o.cg(1e-10, max(3, int(budget / per)), nthreads=threads)
+    dt = time.perf_counter() - t
+    o.close()
+    rate = its / dt
+    out["cg"] = {"value": rate, "unit": "CG iterations/s", "cores": threads, "kind": "port", "algorithm": "CG",
+                 "sample": f"first {its} FP64 CG iterations of the Cxxxx system ({dt:.1f} s, C restatement of the "
+                           f"spring forces, {threads} threads)",
+                 "seconds_to_solution": gpu_f64["iterations"] / rate,
+                 "gpu_f64_speedup": (gpu_f64["iterations"] / rate) / gpu_f64["seconds"]}
+    o = oracle.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, 0)
+    t = time.perf_counter()
+    o.relax(DR_DT, DR_RS, DR_DAMP, 5, 0.0, nthreads=threads)
+    per = max((time.perf_counter() - t) / 5, 1e-6)
+    t = time.perf_counter()
+    steps = o.relax(DR_DT, DR_RS, DR_DAMP, max(5, int(budget / per)), 0.0, nthreads=threads)
+    dt = time.perf_counter() - t
+    o.close()
+    rate = steps / dt
+    dr = {"value": rate, "unit": "DR steps/s", "cores": threads, "kind": "port",
+          "algorithm": "damped Verlet relaxation (XX:1377-1545)",
+          "sample": f"{steps} relaxation steps of the Cxxxx system (dt {DR_DT}, damping {DR_DAMP}; {dt:.1f} s, "
+                    f"{threads} threads)"}
+    rec = os.path.join(ROOT, "profiles", "lsm_dr_64.json")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            need = json.load(f)["Cxxxx"]["steps"]
+        dr["steps_to_cg_residual"] = need
+        dr["seconds_to_solution"] = need / rate
+        dr["gpu_f64_cg_speedup"] = (need / rate) / gpu_f64["seconds"]
+    out["dr"] = dr
+    return out
+
+
+def lsm_dr_mode(args):
+    """The reference's relaxation (XX:1377-1545, YZ likewise) run on the GPU
+    to the static solve's residual: ps_lsm_dyn_step with dt 0.01, rs 1,
+    damping 0.5 and no fluid load, from the reference's starting field (tied
+    planes at -g / +g), until |F| <= 1e-10 |F_1| (F the spring forces, F_1
+    those after the first step), checked every `check` steps.  Gives the
+    step count the CPU relaxation baseline is scaled by."""
+    import oracle
+    from porescale_gb300 import geometry
+    from porescale_gb300.springs import LOAD_XSTRETCH, LOAD_YZSHEAR, LSM_F64, SpringNetwork
+    size = args.lsm_size
+    ind = geometry.inclusions(size, 0.25, 5.0, 20240601)
+    g = 1e-3 * size / 2
+    out = {"mode": "lsm_dr", "size": size, "dt": DR_DT, "rs": DR_RS, "damping": DR_DAMP, "rtol": 1e-10}
+    for load, name in ((LOAD_XSTRETCH, "Cxxxx"), (LOAD_YZSHEAR, "Cyzyz")):
+        osp = oracle.OracleSprings(ind, 1.0, 0.4, 0.3, 0.1, g, load)
+        r0 = osp.dyn_state()[0]
+        ns = osp.ns
+        osp.close()
+        with SpringNetwork(ind, 1.0, 0.4, 0.3, 0.1, g, load, LSM_F64) as S:
+            cg = S.solve(1e-10, 200000)
+            S.set_dyn_state(r0)
+
+            def fnorm():
+                _, v, a = S.dyn_state(ns)
+                return float(np.linalg.norm((a + DR_DAMP * v) * DR_RS))
+
+            S.dyn_step(1, DR_DT, 1.0 / DR_RS, DR_DAMP)
+            f0 = fnorm()
+            steps, rel = 1, 1.0
+            t = time.perf_counter()
+            while rel > 1e-10 and steps < args.lsm_dr_max:
+                S.dyn_step(args.lsm_dr_check, DR_DT, 1.0 / DR_RS, DR_DAMP)
+                steps += args.lsm_dr_check
+                rel = fnorm() / f0
+            dt = time.perf_counter() - t
+        out[name] = {"steps": steps, "rel_force": rel, "gpu_seconds": dt, "cg_iterations": int(cg.iterations),
+                     "cg_modulus": cg.modulus}
+    print(json.dumps(out))
 
 
 def accuracy(args, cfg):
@@ -619,6 +708,13 @@ def main():
     ap.add_argument("--tile", default="", help="tx,ty,occ: pin the step configuration instead of autotuning")
     ap.add_argument("--wave", default="", help="planes,window: with --tile, pin the wavefront schedule")
     ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
+    ap.add_argument("--lsm-cpu-budget", type=float, default=10.0,
+                    help="seconds of each CPU spring-solve baseline (CG, relaxation)")
+    ap.add_argument("--lsm-dr", action="store_true",
+                    help="instead of timing the step: the reference's relaxation on the GPU to the CG residual")
+    ap.add_argument("--lsm-size", type=int, default=64)
+    ap.add_argument("--lsm-dr-check", type=int, default=2000)
+    ap.add_argument("--lsm-dr-max", type=int, default=1000000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -667,6 +763,9 @@ def main():
         return
     if args.batch:
         batch_mode(args)
+        return
+    if args.lsm_dr:
+        lsm_dr_mode(args)
         return
     if world > 1:
         import torch.distributed as dist
@@ -787,7 +886,7 @@ def main():
 
     lsm = None
     if rank == 0 and not args.no_lsm:
-        lsm = lsm_leg(cpu_iters=0 if args.no_cpu_baseline else 40)
+        lsm = lsm_leg(cpu_budget=0.0 if args.no_cpu_baseline else args.lsm_cpu_budget)
     h = res[args.prec]
     traffic = load_traffic(args.prec, nl, h["schedule"]["kind"])
     line = {
