@@ -76,6 +76,10 @@ struct Lattice {
   int wave_key[5] = {0, 0, 0, 0, 0};  // (tx, ty, occ, planes, window) of wave_exec
   int obs_blocks = 0;
   int cur = 0;           // buffer holding the current state
+  // steps since the state was last set: the step number of the stochastic
+  // rounding of 16-bit stores (graph replays read it from d_stepbase)
+  uint32_t nsteps = 0;
+  uint32_t* d_stepbase = nullptr;
   // per buffer: 16-bit slots stored against the reading node's densities (a
   // state set from outside; the first step reads it so, every step writes
   // against the writing node's)
@@ -108,6 +112,8 @@ struct Lattice {
     r.pop = d_pop[b];
     r.rho = d_rho[b];
     r.recv = recv[b];
+    r.step = nsteps;
+    r.stepbase = nullptr;
     return r;
   }
   LbmLaunchArgs args(int src, int dst) const
@@ -147,6 +153,7 @@ void free_lattice(Lattice* L)
   if (L->stream2) cudaStreamDestroy(L->stream2);
   if (L->ev_copy) cudaEventDestroy(L->ev_copy);
   cudaFree(L->d_coord);
+  cudaFree(L->d_stepbase);
   cudaFree(L->d_wall);
   for (cudaGraphExec_t x : L->wave_exec)
     if (x) cudaGraphExecDestroy(x);
@@ -473,6 +480,8 @@ int ensure_wave(Lattice* L)
     const int b = L->cur ^ (s & 1);
     a[s] = L->args(b, 1 - b);
     a[s].src.recv = a[s].dst.recv = 0;
+    a[s].dst.step = (uint32_t)s;  // plus the step base set before each replay
+    a[s].dst.stepbase = L->d_stepbase;
   }
   cudaGraph_t g = nullptr;
   cudaError_t e = PREC_DISPATCH(lbm_wave_graph, L->prec, L->tx, L->ty, L->zchunk, a, kWaveSteps, first.data(), S,
@@ -499,11 +508,16 @@ int launch_steps(Lattice* L, int n)
     if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
     L->recv[1 - L->cur] = 0;
     L->cur = 1 - L->cur;
+    L->nsteps++;
     done = 1;
   }
   if (L->wave_planes > 0 && n - done >= kWaveSteps) {
     if (int r = ensure_wave(L)) return r;
-    for (; n - done >= kWaveSteps; done += kWaveSteps) PS_CUDA(cudaGraphLaunch(L->wave_exec[L->cur], L->stream));
+    for (; n - done >= kWaveSteps; done += kWaveSteps) {
+      k_set_u32<<<1, 1, 0, L->stream>>>(L->d_stepbase, L->nsteps);  // the graph's steps count from here
+      PS_CUDA(cudaGraphLaunch(L->wave_exec[L->cur], L->stream));
+      L->nsteps += kWaveSteps;
+    }
     L->recv[0] = L->recv[1] = 0;
   }
   for (int s = done; s < n; s++) {
@@ -526,6 +540,7 @@ int launch_steps(Lattice* L, int n)
     if (e != cudaSuccess) return cuda_fail(e, "lbm step kernel launch");
     L->recv[1 - L->cur] = 0;
     L->cur = 1 - L->cur;
+    L->nsteps++;
   }
   return PS_OK;
 }
@@ -618,7 +633,7 @@ int batch_tiles(Batch* B)
 // descriptor table of one step in which lattice v reads buffer cur_v ^ flip
 // (recv flags as the lattices hold them only when `first`: every later step
 // reads buffers that a step wrote)
-VolTable batch_table(const Batch* B, int flip, bool first = false)
+VolTable batch_table(const Batch* B, int flip, bool first = false, int graph_step = -1)
 {
   VolTable T;
   memset(&T, 0, sizeof T);
@@ -629,6 +644,10 @@ VolTable batch_table(const Batch* B, int flip, bool first = false)
     T.v[v].src = L->buf(c);
     T.v[v].dst = L->buf(c ^ 1);
     T.v[v].dst.recv = 0;
+    if (graph_step >= 0) {  // captured: the step counts from the lattice's step base
+      T.v[v].dst.step = (uint32_t)graph_step;
+      T.v[v].dst.stepbase = L->d_stepbase;
+    }
     if (!first) T.v[v].src.recv = 0;
     T.v[v].cc = L->d_col;
   }
@@ -661,6 +680,7 @@ int batch_steps(Batch* B, int n)
     for (Lattice* L : B->L) {
       L->recv[L->cur ^ 1] = 0;
       L->cur ^= 1;
+      L->nsteps++;
     }
     n--;
   }
@@ -682,7 +702,7 @@ int batch_steps(Batch* B, int n)
     }
     PS_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < kGraphSteps && e == cudaSuccess; k++) e = batch_launch(B, batch_table(B, k & 1));
+    for (int k = 0; k < kGraphSteps && e == cudaSuccess; k++) e = batch_launch(B, batch_table(B, k & 1, false, k));
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(B->stream, &g);
     if (e != cudaSuccess) {
@@ -699,10 +719,17 @@ int batch_steps(Batch* B, int n)
     B->graph_cur = cur;
   }
   int done = 0;
-  for (; B->exec && n - done >= kGraphSteps; done += kGraphSteps) PS_CUDA(cudaGraphLaunch(B->exec, B->stream));
+  for (; B->exec && n - done >= kGraphSteps; done += kGraphSteps) {
+    for (Lattice* L : B->L) k_set_u32<<<1, 1, 0, B->stream>>>(L->d_stepbase, L->nsteps);
+    PS_CUDA(cudaGraphLaunch(B->exec, B->stream));
+    for (Lattice* L : B->L) L->nsteps += kGraphSteps;
+  }
   for (; done < n; done++) {
-    cudaError_t e = batch_launch(B, batch_table(B, done & 1));
+    VolTable T = batch_table(B, done & 1);
+    for (size_t v = 0; v < B->L.size(); v++) T.v[v].dst.step = B->L[v]->nsteps;  // buffers flipped, counts not yet
+    cudaError_t e = batch_launch(B, T);
     if (e != cudaSuccess) return cuda_fail(e, "batch step");
+    for (Lattice* L : B->L) L->nsteps++;
   }
   for (Lattice* L : B->L) {
     if (n > 0) L->recv[0] = L->recv[1] = 0;
@@ -780,6 +807,7 @@ int ps_lbm_create(const ps_lbm_params* p, const int32_t* ind, int32_t nx, int32_
   PS_CUDA(cudaEventCreateWithFlags(&L->ev_copy, cudaEventDisableTiming));
   const size_t nv = (size_t)L->nvox, nlc = (size_t)std::max(1LL, L->nl);
   if (int r = dalloc(L.get(), &L->d_coord, sizeof(uint32_t) * nlc)) return r;
+  if (int r = dalloc(L.get(), &L->d_stepbase, sizeof(uint32_t))) return r;
   if (int r = dalloc(L.get(), &L->d_mask, sizeof(uint32_t) * nlc)) return r;
   if (int r = dalloc(L.get(), &L->d_ref, sizeof(int32_t) * nlc)) return r;
   if (int r = dalloc(L.get(), &L->d_rowstart, sizeof(int32_t) * H.rowstart.size())) return r;
@@ -955,6 +983,7 @@ int ps_lbm_set_state(void* h, const double* fr, const double* fb)
   if (e != cudaSuccess) return cuda_fail(e, "set_state kernel");
   L->recv[L->cur] = L->prec >= 2 ? 1 : 0;  // 16-bit storage is read against the writer's densities
   L->have_state = true;
+  L->nsteps = 0;
   PS_CUDA(cudaStreamSynchronize(L->stream));
   return PS_OK;
 }
@@ -1169,6 +1198,7 @@ int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, 
   std::vector<void*> sp(nv, nullptr);
   std::vector<float2*> sr(nv, nullptr);
   std::vector<int> cur(nv), rcv(nv);
+  std::vector<uint32_t> stp(nv);
   auto popb = [&](const Lattice* L) { return 2 * L->elem() * 19 * (size_t)std::max(64LL, L->pitch); };
   auto rhob = [&](const Lattice* L) { return L->rho_bytes(); };
   int rc = PS_OK;
@@ -1176,6 +1206,7 @@ int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, 
     Lattice* L = B->L[v];
     cur[v] = L->cur;
     rcv[v] = L->recv[L->cur];
+    stp[v] = L->nsteps;
     cudaError_t e = cudaMalloc(&sp[v], popb(L));
     if (e == cudaSuccess) e = cudaMemcpyAsync(sp[v], L->d_pop[L->cur], popb(L), cudaMemcpyDeviceToDevice, B->stream);
     if (e == cudaSuccess && L->prec >= 1) e = cudaMalloc((void**)&sr[v], rhob(L));
@@ -1215,6 +1246,7 @@ int ps_batch_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, 
   cudaEventDestroy(e1);
   for (size_t v = 0; v < nv; v++) {  // restore
     Lattice* L = B->L[v];
+    L->nsteps = stp[v];
     L->cur = cur[v];
     L->recv[L->cur] = rcv[v];
     if (sp[v]) cudaMemcpyAsync(L->d_pop[L->cur], sp[v], popb(L), cudaMemcpyDeviceToDevice, B->stream);
@@ -1330,6 +1362,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   float best = 1e30f;
   Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead, L->wave_planes, L->wave_window};
   const int saved_cur = L->cur, saved_recv[2] = {L->recv[0], L->recv[1]};
+  const uint32_t saved_steps = L->nsteps;
   int rc = PS_OK;
   for (const Cfg& c : cand) {
     L->tx = c.tx;
@@ -1363,6 +1396,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   L->cur = saved_cur;
   L->recv[0] = saved_recv[0];
   L->recv[1] = saved_recv[1];
+  L->nsteps = saved_steps;
   cudaMemcpyAsync(L->d_pop[L->cur], save, popb, cudaMemcpyDeviceToDevice, L->stream);
   if (saver) cudaMemcpyAsync(L->d_rho[L->cur], saver, rhob, cudaMemcpyDeviceToDevice, L->stream);
   cudaStreamSynchronize(L->stream);

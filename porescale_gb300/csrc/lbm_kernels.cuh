@@ -110,6 +110,11 @@ struct BufDev {
   void* pop;
   float2* rho;
   int recv;
+  // step number of the stochastically rounded 16-bit stores written into
+  // this buffer: step, plus *stepbase when set (graph replays, whose kernel
+  // arguments are fixed at capture)
+  uint32_t step;
+  const uint32_t* stepbase;
 };
 
 // ---- storage policies ----------------------------------------------------
@@ -169,6 +174,65 @@ __device__ __forceinline__ __nv_bfloat162 from_f2<__nv_bfloat162>(float a, float
   return __floats2bfloat162_rn(a, b);
 }
 
+// ---- stochastic rounding of the 16-bit stores ------------------------------
+// A population of a flow that is steady, or nearly so, takes the same value
+// step after step, and round-to-nearest then stores it with the same error
+// every step: a bias that never averages out (in a steady two-layer flow,
+// round-to-nearest FP16 deviations biased the blue flux by 2e-3).  The
+// collide's 16-bit stores therefore round stochastically: a uniform random
+// integer below the bits the conversion drops is added to the FP32 bit
+// pattern, and the sum is rounded toward zero, so a value rounds up with
+// probability equal to its distance from the lower neighbour and the
+// rounding error has mean zero.  Values the 16-bit format holds exactly
+// (zeros included) are stored unchanged.  The random bits are a hash of
+// (node, direction, step), so a state is reproducible and is the same in
+// every schedule.
+__device__ __forceinline__ uint32_t dither_seed(uint32_t i, uint32_t step)
+{
+  uint32_t h = (i * 0x9E3779B1u) ^ (step * 0x85EBCA77u + 0x165667B1u);
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  h *= 0x297A2D39u;
+  h ^= h >> 15;
+  return h;
+}
+__device__ __forceinline__ uint32_t dither_bits(uint32_t seed, int e)
+{
+  uint32_t h = seed ^ ((uint32_t)e * 0x27D4EB2Fu);
+  h *= 0x165667B1u;
+  h ^= h >> 16;
+  h *= 0x85EBCA77u;
+  return h ^ (h >> 13);
+}
+__device__ __forceinline__ uint32_t step_of(const BufDev& b)
+{
+  return b.step + (b.stepbase ? __ldg(b.stepbase) : 0u);
+}
+// (a, b) to a 16-bit pair, stochastically rounded with the random bits r
+template <typename T2>
+__device__ __forceinline__ T2 from_f2_sr(float a, float b, uint32_t r);
+template <>
+__device__ __forceinline__ __half2 from_f2_sr<__half2>(float a, float b, uint32_t r)
+{
+  // FP16 keeps 10 of FP32's 23 mantissa bits: 13 random bits each
+  const float ad = __uint_as_float(__float_as_uint(a) + (r & 0x1FFFu));
+  const float bd = __uint_as_float(__float_as_uint(b) + ((r >> 16) & 0x1FFFu));
+  uint32_t h;
+  asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(bd), "f"(ad));
+  return *reinterpret_cast<__half2*>(&h);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat162 from_f2_sr<__nv_bfloat162>(float a, float b, uint32_t r)
+{
+  // BF16 keeps 7 mantissa bits: 16 random bits each
+  const float ad = __uint_as_float(__float_as_uint(a) + (r & 0xFFFFu));
+  const float bd = __uint_as_float(__float_as_uint(b) + (r >> 16));
+  uint32_t h;
+  asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(bd), "f"(ad));
+  return *reinterpret_cast<__nv_bfloat162*>(&h);
+}
+
 template <int PREC>
 struct Pop {
   using S = Store<PREC>;
@@ -203,12 +267,16 @@ struct Pop {
     *(static_cast<T2*>(b.pop) + (long long)d * pitch + i) = from_f2<T2>(gr * DevScale<T>::up, gb * DevScale<T>::up);
   }
   // writes the (red, blue) pair (vr, vb) into slot (d, i) whose node has
-  // deviation references rho
+  // deviation references rho; 16-bit storage rounds stochastically with the
+  // random bits rnd
   __device__ __forceinline__ static void put(const LbmConst<R>& K, const BufDev& b, int d, int i, long long pitch,
-                                             R vr, R vb, float2 rho)
+                                             R vr, R vb, float2 rho, uint32_t rnd = 0u)
   {
     T2* p = static_cast<T2*>(b.pop) + (long long)d * pitch + i;
-    if constexpr (S::kDev) {
+    if constexpr (S::kSendRef) {
+      *p = from_f2_sr<T2>((vr - K.t[0][wcls(d)] * rho.x) * DevScale<T>::up,
+                          (vb - K.t[1][wcls(d)] * rho.y) * DevScale<T>::up, rnd);
+    } else if constexpr (S::kDev) {
       *p = from_f2<T2>((vr - K.t[0][wcls(d)] * rho.x) * DevScale<T>::up,
                        (vb - K.t[1][wcls(d)] * rho.y) * DevScale<T>::up);
     } else {
@@ -322,7 +390,8 @@ __device__ __forceinline__ void push_node(const LbmConst<typename Store<PREC>::R
   // ri: node i's entry in rho.  Sender reference: every population against
   // node i's own densities; otherwise against each receiver's.
   const float2 own = kDev ? ld_step(dst.rho + ri, kCoh) : zero;
-  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], own);
+  const uint32_t seed = kSend ? dither_seed((uint32_t)i, step_of(dst)) : 0u;
+  Pop<PREC>::put(K, dst, 0, i, G.pitch, outr[0], outb[0], own, kSend ? dither_bits(seed, 0) : 0u);
 #pragma unroll
   for (int e = 1; e < 19; e++) {
     const int oe = opp(e);
@@ -330,7 +399,7 @@ __device__ __forceinline__ void push_node(const LbmConst<typename Store<PREC>::R
     const int node = stream ? s[oe] : i;
     const int slot = stream ? e : oe;
     Pop<PREC>::put(K, dst, slot, node, G.pitch, outr[e], outb[e],
-                   kDev && !kSend ? ld_step(dst.rho + node, kCoh) : own);
+                   kDev && !kSend ? ld_step(dst.rho + node, kCoh) : own, kSend ? dither_bits(seed, e) : 0u);
   }
 }
 
@@ -1056,6 +1125,9 @@ __global__ void __launch_bounds__(128) k_lbm_wall_load(const __grid_constant__ L
   out[G.nvox + v] = acc[1];
   out[2 * G.nvox + v] = acc[2];
 }
+
+// *p = v (the step base of a graph replay)
+static __global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
 
 static __global__ void k_obs_final(const double* partial, int nblocks, double* out)
 {
