@@ -51,6 +51,11 @@ def workload_config(size: int):
     }
 
 
+def march_fields(m: int):
+    """(rows, planes, producer warps, sorted) of ps_lbm_info.march."""
+    return m & 4095, (m >> 12) & 0x1FFF, ((m >> 25) & 3) * 4, not (m >> 30) & 1
+
+
 def bench_config(cfg, nl):
     """The `config` object of both bench arms (identical for the same
     workload): the workload, its size, seed and fluid-node count.  The state
@@ -707,6 +712,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default step configuration")
     ap.add_argument("--tile", default="", help="tx,ty,occ: pin the step configuration instead of autotuning")
     ap.add_argument("--wave", default="", help="planes,window: with --tile, pin the wavefront schedule")
+    ap.add_argument("--march", default="", help="rows,planes,producers,sort: with --tile, pin the marching step")
     ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
     ap.add_argument("--lsm-cpu-budget", type=float, default=10.0,
                     help="seconds of each CPU spring-solve baseline (CG, relaxation)")
@@ -786,6 +792,8 @@ def main():
             L.set_tile(*[int(v) for v in args.tile.split(",")])
             if args.wave:
                 L.set_wave(*[int(v) for v in args.wave.split(",")])
+            if args.march:
+                L.set_march(*[int(v) for v in args.march.split(",")])
             L.info = L.get_info()
         elif not args.no_autotune:
             L.autotune(4 if q != "f64" else 2)
@@ -808,10 +816,12 @@ def main():
             # the step schedules side by side on this workload (fused: slab
             # planes x look-ahead), each from the same state
             study = {}
-            tile = (L.info.tile_x, L.info.tile_y, L.info.occupancy, int(L.info.schedule), int(L.info.wave))
+            tile = (L.info.tile_x, L.info.tile_y, L.info.occupancy, int(L.info.schedule), int(L.info.wave),
+                    int(L.info.march))
             for planes, ahead in ((0, 1), (1, 1), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2)):
                 try:
                     L.set_wave(0)
+                    L.set_march(0)
                     L.set_fused(0, 1)
                     L.set_tile(128, 256, 0)
                     L.set_fused(planes, ahead)
@@ -827,8 +837,18 @@ def main():
                 L.set_wave(planes, window)
                 L.set_state(fr, fb)
                 study[f"w{planes}/{window}"] = nl * 48 / time_steps(L, 48, 8, torch) / 1e6
+            # marching one-launch steps (band rows, producer warps, sorted order)
+            for rows, pw, srt in ((4, 4, True), (8, 4, True), (16, 4, True), (8, 8, True), (16, 8, True),
+                                  (8, 4, False)):
+                L.set_wave(0)
+                L.set_march(rows, 0, pw, srt)
+                L.set_state(fr, fb)
+                study[f"m{rows}p{pw}{'' if srt else 'u'}"] = nl * 20 / time_steps(L, 20, 3, torch) / 1e6
+                L.set_march(0)
             L.set_wave(0)
             L.set_tile(*tile[:3])
+            if tile[5]:
+                L.set_march(*march_fields(tile[5]))
             if tile[3]:
                 L.set_fused(tile[3] % 256, tile[3] // 256)
             if tile[4]:
@@ -836,8 +856,13 @@ def main():
             L.set_state(fr, fb)
             L.info = L.get_info()
             res[q + "_schedules_mlups"] = study
-        sched, wave = int(L.info.schedule), int(L.info.wave)
-        if sched:
+        sched, wave, march = int(L.info.schedule), int(L.info.wave), int(L.info.march)
+        if march:
+            rows, planes, pw, srt = march_fields(march)
+            schedule = {"kind": "march", "band_rows": rows, "chunk_planes": planes, "producer_warps": pw,
+                        "consumer_warps": 24 - pw, "sorted": srt}
+            kps = 1
+        elif sched:
             schedule, kps = {"kind": "fused", "slab_planes": sched % 256, "lookahead": sched // 256}, 1
         elif wave:
             nslab = -(-int(L.info.nz) // (wave % 256))

@@ -25,7 +25,7 @@ module porescale_gpu
 
   type, bind(c) :: ps_lbm_info
     integer(c_int64_t) :: nl, nps, npb2, npb4, ns, nvox
-    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, occupancy, schedule, wave
+    integer(c_int32_t) :: nx, ny, nz, precision, tile_x, tile_y, occupancy, schedule, wave, march
     integer(c_int64_t) :: device_bytes
   end type
 
@@ -117,6 +117,11 @@ module porescale_gpu
       import :: c_int, c_int32_t, c_ptr
       type(c_ptr), value :: handle
       integer(c_int32_t), value :: polls
+    end function
+    integer(c_int) function ps_lbm_set_march(handle, rows, planes, producers, sort) bind(c, name='ps_lbm_set_march')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: rows, planes, producers, sort
     end function
     integer(c_int) function ps_lbm_set_wave(handle, planes, window) bind(c, name='ps_lbm_set_wave')
       import :: c_int, c_int32_t, c_ptr

@@ -67,6 +67,8 @@ typedef struct {
   int32_t tile_x, tile_y, occupancy;  /* step-kernel configuration */
   int32_t schedule;     /* 0: two-pass step; else fused: slab planes + 256 x look-ahead */
   int32_t wave;         /* 0: off; else wavefront graph: slab planes + 256 x window */
+  int32_t march;        /* 0: off; else marching step: band rows + 4096 x chunk planes
+                           + 2^25 x producer warps / 4 (+ 2^30 when not sorted) */
   int64_t device_bytes; /* device memory held by the handle */
 } ps_lbm_info;
 
@@ -134,8 +136,9 @@ int ps_lbm_set_tile(void *handle, int32_t tx, int32_t ty, int32_t occ);
  * whose wait gives up (bounded) makes the next synchronising call return
  * PS_ERR_TIMEOUT. */
 int ps_lbm_set_fused(void *handle, int32_t planes, int32_t ahead);
-/* Bound of the fused schedule's device waits, in polls of a density-tile
- * counter (about 32 ns apart); 0 restores the default 2^22.  A wait that
+/* Bound of the fused and marching schedules' device waits, in polls (of a
+ * density-tile counter, about 32 ns apart, or of an mbarrier); 0 restores
+ * the default 2^22.  A wait that
  * reaches it gives up, the tile collides with whatever colour field it
  * finds, and the next synchronising call (ps_lbm_sync, ps_lbm_observables,
  * ps_lbm_get_state, ...) returns PS_ERR_TIMEOUT: the state is then invalid
@@ -156,6 +159,22 @@ int ps_lbm_set_wait_limit(void *handle, int32_t polls);
  * finish with two-pass steps.  Turns the fused schedule off (and
  * ps_lbm_set_fused with planes > 0 turns this one off). */
 int ps_lbm_set_wave(void *handle, int32_t planes, int32_t window);
+/* Marching step: rows > 0 runs each step as ONE persistent launch (one CTA
+ * per SM) over items of `rows` y-rows (every x) times `planes` z-planes (0:
+ * about two items per SM).  Inside a CTA, `producers` warps (4 or 8; the
+ * other 24 - producers warps collide) walk the item in z computing the
+ * densities and stencil colours of each plane -- band plus one recomputed
+ * halo row per side, so no CTA waits for another -- into a 4-plane ring in
+ * shared memory, up to two planes ahead of the colliding warps, which read
+ * their populations again from L2.  The hand-off is by mbarriers whose waits
+ * are bounded (ps_lbm_set_wait_limit): one that gives up makes the next
+ * synchronising call return PS_ERR_TIMEOUT.  sort != 0 collides each plane's
+ * bulk nodes before its interface nodes (the producers record which is
+ * which), so that a warp runs one branch of the node update rather than
+ * both.  Results are identical to the two-pass step.  Needs FP32/16-bit
+ * storage; rows = 0 turns it off.  Turns the fused and wavefront schedules
+ * off (and they turn this one off). */
+int ps_lbm_set_march(void *handle, int32_t rows, int32_t planes, int32_t producers, int32_t sort);
 /* Times the candidate configurations (two-pass, fused, wavefront) on the current
  * state (restored afterwards) and keeps the fastest; writes its tile to
  * *tx, *ty, *occ (the schedules are in ps_lbm_info.schedule and .wave). */

@@ -35,7 +35,7 @@ class LbmInfo(C.Structure):
     _fields_ = [("nl", C.c_int64), ("nps", C.c_int64), ("npb2", C.c_int64), ("npb4", C.c_int64),
                 ("ns", C.c_int64), ("nvox", C.c_int64), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
                 ("precision", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32), ("occupancy", C.c_int32),
-                ("schedule", C.c_int32), ("wave", C.c_int32),
+                ("schedule", C.c_int32), ("wave", C.c_int32), ("march", C.c_int32),
                 ("device_bytes", C.c_int64)]
 
 
@@ -80,6 +80,7 @@ SIGNATURES = {
     "ps_lbm_autotune": (C.c_int, [_P, C.c_int32, _IP, _IP, _IP]),
     "ps_lbm_set_fused": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "ps_lbm_set_wait_limit": (C.c_int, [_P, C.c_int32]),
+    "ps_lbm_set_march": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "ps_lbm_set_wave": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "ps_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
     "ps_batch_destroy": (C.c_int, [_P]),

@@ -72,6 +72,9 @@ struct Lattice {
   // wavefront schedule (0 planes: off): z-slab launches in a graph of
   // kWaveSteps steps, one executable per starting buffer
   int wave_planes = 0, wave_window = 0;
+  // marching step (0 rows: off): band rows, chunk planes (march_req as
+  // requested, 0 = about two items per SM), producer warps, collide order
+  int march_rows = 0, march_planes = 0, march_req = 0, march_pw = 4, march_sort = 1;
   cudaGraphExec_t wave_exec[2] = {nullptr, nullptr};
   int wave_key[5] = {0, 0, 0, 0, 0};  // (tx, ty, occ, planes, window) of wave_exec
   int obs_blocks = 0;
@@ -524,7 +527,15 @@ int launch_steps(Lattice* L, int n)
     LbmLaunchArgs a = L->args(L->cur, 1 - L->cur);
     a.dst.recv = 0;
     cudaError_t e;
-    if (L->fused_planes > 0) {
+    if (L->march_rows > 0) {
+      MarchArgs A{};
+      A.rows = L->march_rows;
+      A.planes = L->march_planes;
+      A.sort = L->march_sort;
+      A.spin = L->spin_limit;
+      A.err = L->d_err;
+      e = PREC_DISPATCH(lbm_march_launch, L->prec, L->march_pw, A, a);
+    } else if (L->fused_planes > 0) {
       FusedArgs f;
       f.items = L->d_items;
       f.nitems = L->nitems;
@@ -553,7 +564,45 @@ int check_fused(Lattice* L)
   PS_CUDA(cudaMemcpy(&err, L->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (!err) return PS_OK;
   PS_CUDA(cudaMemset(L->d_err, 0, sizeof(int)));
-  return fail(PS_ERR_TIMEOUT, "fused step: a collide tile gave up waiting for its density tiles; the state is invalid");
+  return fail(PS_ERR_TIMEOUT, "fused or marching step: a bounded device wait gave up; the state is invalid");
+}
+
+// turns the marching step on with band rows `rows`, chunk planes `planes`
+// (0: about two items per SM), `pw` producer warps (4 or 8) and the sorted
+// collide order when sort; or off (rows 0)
+int set_march(Lattice* L, int rows, int planes, int pw, int sort)
+{
+  if (rows < 0 || planes < 0) return fail(PS_ERR_ARG, "ps_lbm_set_march: need rows >= 0 and planes >= 0");
+  if (rows == 0) {
+    L->march_rows = L->march_planes = 0;
+    return PS_OK;
+  }
+  if (L->prec == 0) return fail(PS_ERR_ARG, "ps_lbm_set_march: FP64 storage has no marching step");
+  if (pw != 4 && pw != 8) return fail(PS_ERR_ARG, "ps_lbm_set_march: producer warps must be 4 or 8, not %d", pw);
+  rows = std::min(rows, L->ny);
+  const int res = PREC_DISPATCH(lbm_march_resident, L->prec, pw, rows, L->nx);
+  if (res < 1) return fail(PS_ERR_ARG, "ps_lbm_set_march: a ring of %d rows x %d does not fit one CTA", rows, L->nx);
+  if (!L->d_err) {
+    PS_CUDA(cudaMalloc((void**)&L->d_err, sizeof(int)));
+    PS_CUDA(cudaMemsetAsync(L->d_err, 0, sizeof(int), L->stream));
+  }
+  const int req = planes;
+  if (planes == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int nband = (L->ny + rows - 1) / rows;
+    const int nchunk = std::max(1, std::min(L->nz, 2 * sms / nband));
+    planes = (L->nz + nchunk - 1) / nchunk;
+  }
+  L->march_req = req;
+  L->march_sort = sort ? 1 : 0;
+  L->march_pw = pw;
+  L->march_rows = rows;
+  L->march_planes = std::min(planes, L->nz);
+  L->fused_planes = 0;
+  L->wave_planes = 0;
+  return PS_OK;
 }
 
 bool fused_config(int tx, int occ) { return (occ == 0 && (tx == 128 || tx == 256)) || (tx == 128 && (occ == 6 || occ == 8)); }
@@ -881,6 +930,9 @@ int ps_lbm_get_info(void* h, ps_lbm_info* o)
   o->occupancy = L->zchunk;
   o->schedule = L->fused_planes > 0 ? L->fused_planes + 256 * L->fused_ahead : 0;
   o->wave = L->wave_planes > 0 ? L->wave_planes + 256 * L->wave_window : 0;
+  o->march = L->march_rows > 0 ? L->march_rows + 4096 * L->march_planes + (L->march_pw / 4 << 25) +
+                                     (L->march_sort ? 0 : (1 << 30))
+                               : 0;
   o->device_bytes = L->dev_bytes;
   return PS_OK;
 }
@@ -1286,7 +1338,7 @@ int ps_lbm_set_fused(void* h, int32_t planes, int32_t ahead)
     return fail(PS_ERR_ARG, "ps_lbm_set_fused: the step configuration (%d, %d, %d) has no fused form", L->tx, L->ty, L->zchunk);
   L->fused_planes = planes;
   L->fused_ahead = ahead;
-  if (planes > 0) L->wave_planes = 0;
+  if (planes > 0) L->wave_planes = L->march_rows = 0;
   return PS_OK;
 }
 
@@ -1306,8 +1358,14 @@ int ps_lbm_set_wave(void* h, int32_t planes, int32_t window)
     return fail(PS_ERR_ARG, "ps_lbm_set_wave: need planes >= 0 and window 0 or 2..64");
   L->wave_planes = planes;
   L->wave_window = window;
-  if (planes > 0) L->fused_planes = 0;
+  if (planes > 0) L->fused_planes = L->march_rows = 0;
   return PS_OK;
+}
+
+int ps_lbm_set_march(void* h, int32_t rows, int32_t planes, int32_t producers, int32_t sort)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_march: null handle");
+  return set_march(as_lattice(h), rows, planes, producers, sort);
 }
 
 int ps_lbm_set_tile(void* h, int32_t tx, int32_t ty, int32_t zchunk)
@@ -1345,7 +1403,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
 
   }
   struct Cfg {
-    int tx, ty, zc, planes, ahead, wplanes, window;
+    int tx, ty, zc, planes, ahead, wplanes, window, mrows, mpw, msort;
   };
   // two-pass configurations, fused ones (slab planes, look-ahead), then
   // wavefront graphs (slab planes, window)
@@ -1355,12 +1413,18 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
       {128, 256, 0, 4, 1, 0, 0}, {128, 256, 0, 8, 1, 0, 0},  {128, 256, 0, 4, 2, 0, 0}, {256, 256, 0, 4, 1, 0, 0},
       {128, 256, 6, 4, 1, 0, 0}, {128, 256, 8, 4, 1, 0, 0},  {128, 256, 6, 0, 1, 16, 0}, {128, 256, 6, 0, 1, 32, 0},
       {128, 256, 8, 0, 1, 32, 0}, {128, 256, 0, 0, 1, 32, 0}, {128, 256, 6, 0, 1, 64, 0}, {128, 256, 6, 0, 1, 128, 0}, {128, 256, 7, 0, 1, 0, 0},
-      {128, 256, 7, 0, 1, 64, 0}};
+      {128, 256, 7, 0, 1, 64, 0},
+      // marching steps (band rows, producer warps, sorted collide order)
+      {128, 256, 6, 0, 1, 0, 0, 4, 4, 1}, {128, 256, 6, 0, 1, 0, 0, 8, 4, 1}, {128, 256, 6, 0, 1, 0, 0, 16, 4, 1},
+      {128, 256, 6, 0, 1, 0, 0, 8, 8, 1}, {128, 256, 6, 0, 1, 0, 0, 16, 8, 1}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead, L->wave_planes, L->wave_window};
+  Cfg bc{L->tx, L->ty, L->zchunk, L->fused_planes, L->fused_ahead, L->wave_planes, L->wave_window, L->march_rows,
+         L->march_pw, L->march_sort};
+  const int bc_mreq = L->march_req;
+  bool bc_initial = true;
   const int saved_cur = L->cur, saved_recv[2] = {L->recv[0], L->recv[1]};
   const uint32_t saved_steps = L->nsteps;
   int rc = PS_OK;
@@ -1372,6 +1436,8 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
     L->fused_ahead = c.ahead;
     L->wave_planes = c.wplanes;
     L->wave_window = c.window;
+    L->march_rows = 0;
+    if (c.mrows > 0 && (L->prec == 0 || set_march(L, c.mrows, 0, c.mpw, c.msort) != PS_OK)) continue;  // no marching form
     // a wavefront candidate runs whole graphs (and builds its graph in the warm-up)
     const int n = c.wplanes > 0 ? std::max(steps, kWaveSteps) / kWaveSteps * kWaveSteps : steps;
     rc = launch_steps(L, c.wplanes > 0 ? kWaveSteps : 2);  // warm-up
@@ -1388,6 +1454,7 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
     if (ms < best) {
       best = ms;
       bc = c;
+      bc_initial = false;
     }
   }
   cudaEventDestroy(e0);
@@ -1409,6 +1476,8 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
   L->fused_ahead = bc.ahead;
   L->wave_planes = bc.wplanes;
   L->wave_window = bc.window;
+  L->march_rows = 0;
+  if (bc.mrows > 0 && rc == PS_OK) rc = set_march(L, bc.mrows, bc_initial ? bc_mreq : 0, bc.mpw, bc.msort);
   if (tx_out) *tx_out = bc.tx;
   if (ty_out) *ty_out = bc.ty;
   if (zc_out) *zc_out = bc.zc;

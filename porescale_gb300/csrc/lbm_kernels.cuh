@@ -566,14 +566,20 @@ __device__ __forceinline__ void read_node(const LbmConst<typename Store<PREC>::R
 // per-node bodies, shared by the single-lattice and the batched kernels
 
 // colour (and, for deviation storage, the current densities that the
-// collide step encodes against) of fluid node i for this step
+// collide step encodes against) of fluid node i for this step; returns the
+// node's stencil colour, its packed coordinates in *cw and, when iface is
+// given, whether both components are present (node_update's interface
+// branch; a scheduling hint, node_update decides from its own densities)
 template <int PREC>
-__device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& src, const BufDev& dst, typename Store<PREC>::R* cc, int i)
+__device__ __forceinline__ typename Store<PREC>::R dens_colour(const LbmConst<typename Store<PREC>::R>& K,
+                                                               const GeomDev& G, const BufDev& src,
+                                                               const BufDev& dst, int i, uint32_t* cw,
+                                                               bool* iface = nullptr)
 {
   using R = typename Store<PREC>::R;
   R rr, rb;
   const uint32_t c = __ldg(G.coord + i);
+  *cw = c;
   if constexpr (Store<PREC>::kSendRef) {
     const uint32_t m = __ldg(G.mask + i);
     const long long v = voxel_of(G, c);
@@ -598,31 +604,34 @@ __device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R
     read_node<PREC>(K, G, src, i, f);
     densities(f, rr, rb);
   }
-  int x, y, z;
-  unpack(c, x, y, z);
-  cc[x + G.nx * y + G.cplane * z] = stencil_colour(rr, rb, K.wet);
+  if (iface) *iface = !(rb <= K.ee) && !(rr <= K.ee);
+  return stencil_colour(rr, rb, K.wet);
 }
 
-// collision, CSF force, recolouring of fluid node i; pushes the
-// post-collision populations to their receivers.  kCoh: the colour field
-// and reference densities of this step come from other CTAs of the same
-// launch (the fused schedule) and are read through L2 only.
-template <int PREC, bool kCoh = false>
-__device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
-                                          const BufDev& src, const BufDev& dst,
-                                          const typename Store<PREC>::R* __restrict__ cc, int i)
+template <int PREC>
+__device__ __forceinline__ void dens_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, const BufDev& dst, typename Store<PREC>::R* cc, int i)
 {
-  using R = typename Store<PREC>::R;
-  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+  uint32_t c;
+  const auto q = dens_colour<PREC>(K, G, src, dst, i, &c);
   int x, y, z;
   unpack(c, x, y, z);
-  const int v = x + G.nx * y + G.cplane * z;
-  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.cplane, G.nz);
-  // plain (L1-cached) loads also in the fused schedule: every colour plane
-  // starts on a 128-byte line, and a collide tile reads only planes whose
-  // density tiles have all completed, so no line it caches is written later
-  // in the launch
-  auto col = [&](int a, int b, int e) -> R { return cc[v + o.x[a] + o.y[b] + o.z[e]]; };
+  cc[x + G.nx * y + G.cplane * z] = q;
+}
+
+// collision, CSF force, recolouring of fluid node i (coordinates c, mask m);
+// pushes the post-collision populations to their receivers.  col(a, b, e)
+// returns this step's stencil colour at offset (a-1, b-1, e-1).  kCoh: the
+// reference densities of this step come from other threads of the same
+// launch and are read through L2 (no non-coherent path).
+template <int PREC, bool kCoh, typename Col>
+__device__ __forceinline__ void coll_node_c(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                            const BufDev& src, const BufDev& dst, int i, uint32_t c, uint32_t m,
+                                            Col col)
+{
+  using R = typename Store<PREC>::R;
+  int x, y, z;
+  unpack(c, x, y, z);
   // FP32 storage: shifted arithmetic on the deviations (the storage is
   // precise enough for it to matter).  16-bit storage: its rounding (~1e-3
   // relative on the deviations) dominates either way, so the full-value
@@ -652,6 +661,26 @@ __device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R
     pull_sources(G, i, c, m, s);
     push_node<PREC, kCoh>(K, G, dst, i, ri, m, s, outr, outb);
   }
+}
+
+// the same with the colour read from the dense colour field cc of the
+// two-pass step.  Plain (L1-cached) loads also in the fused schedule: every
+// colour plane starts on a 128-byte line, and a collide tile reads only
+// planes whose density tiles have all completed, so no line it caches is
+// written later in the launch.
+template <int PREC, bool kCoh = false>
+__device__ __forceinline__ void coll_node(const LbmConst<typename Store<PREC>::R>& K, const GeomDev& G,
+                                          const BufDev& src, const BufDev& dst,
+                                          const typename Store<PREC>::R* __restrict__ cc, int i)
+{
+  using R = typename Store<PREC>::R;
+  const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+  int x, y, z;
+  unpack(c, x, y, z);
+  const int v = x + G.nx * y + G.cplane * z;
+  const NbOff o = nb_offsets(m, G.nx, G.nx * G.ny, G.cplane, G.nz);
+  auto col = [&](int a, int b, int e) -> R { return cc[v + o.x[a] + o.y[b] + o.z[e]]; };
+  coll_node_c<PREC, kCoh>(K, G, src, dst, i, c, m, col);
 }
 
 // Both step kernels work on the fluid nodes [i0, i1): the whole lattice,
@@ -789,6 +818,184 @@ __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK)
       __syncthreads();
       if (i < w.z) coll_node<PREC, true>(K, G, src, dst, cc, i);
     }
+  }
+}
+
+// ---- marching step: one persistent launch per step, warp-specialised -----
+// The box is cut into items: a band of A.rows y-rows (every x) times a chunk
+// of A.planes z-planes; CTA b takes items b, b + grid, ...  Inside a CTA,
+// PW producer warps compute the densities and stencil colours of plane p of
+// the band plus one halo row on each side (the halo rows are recomputed, so
+// no CTA waits for another) into a ring of 4 colour planes in shared memory
+// (non-fluid voxels hold the wetting colour), and CW consumer warps collide
+// plane p-1 of the band from ring planes p-2..p.  Producers run up to two
+// planes ahead of consumers; the hand-off is two mbarriers per ring slot
+// (full: the producers wrote it; empty: the consumers are done with it), so
+// no barrier spans the whole CTA and memory-bound density work overlaps
+// compute-bound collide work.  Consumers re-read a plane's populations
+// shortly after the producers read them (L2 hits), so each population comes
+// from DRAM about once per step.  Every chunk starts one plane early and
+// ends one late (the densities its stencils need).  Producers also write
+// each plane's collide order: bulk nodes first when A.sort, so that a
+// consumer warp runs one branch of the node update instead of both.  The
+// per-node arithmetic is the two-pass step's (dens_colour, coll_node_c), so
+// the state is identical.  Every wait is bounded (A.spin polls); one that
+// gives up sets *A.err and goes on, so the launch always ends (with an
+// invalid state), and every index used comes from the geometry.
+struct MarchArgs {
+  int rows, planes, nband, nitems;  // band height, chunk depth, bands across y, bands x chunks
+  int sort;                         // collide bulk nodes before interface nodes
+  unsigned spin;                    // polls before a wait gives up
+  int* err;                         // set to 1 when a wait gave up
+};
+
+// dynamic shared memory of one CTA: 8 mbarriers, 4 x 2 order counters, 4
+// ring planes of (rows + 2) x nx colours, 4 collide orders of rows x nx
+template <typename R>
+__host__ __device__ constexpr size_t march_smem_bytes(int rows, int nx)
+{
+  return 64 + 32 + sizeof(R) * 4 * (size_t)(rows + 2) * (size_t)nx + 2 * 4 * (size_t)rows * (size_t)nx;
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b)
+{
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(b))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* b, unsigned parity)
+{
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// waits (bounded) for the completion of the barrier's phase of parity `parity`
+__device__ __forceinline__ void mbar_wait(uint64_t* b, unsigned parity, const MarchArgs& A)
+{
+  for (unsigned n = 0; !mbar_test(b, parity); n++)
+    if (n >= A.spin) {
+      atomicExch(A.err, 1);
+      return;
+    }
+}
+// named barrier among the `count` threads of one role
+__device__ __forceinline__ void role_sync(int id, int count)
+{
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+template <int PREC, int PW, int CW>
+__global__ void __launch_bounds__(32 * (PW + CW), 1)
+    k_lbm_march(const __grid_constant__ LbmConst<typename Store<PREC>::R> K, const __grid_constant__ GeomDev G,
+                const BufDev src, const BufDev dst, const MarchArgs A)
+{
+  using R = typename Store<PREC>::R;
+  constexpr int NP = 32 * PW, NC = 32 * CW;
+  extern __shared__ __align__(16) unsigned char march_smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(march_smem);  // [4]
+  uint64_t* empty = full + 4;                                // [4]
+  int* cnt = reinterpret_cast<int*>(march_smem + 64);        // [4][2] bulk / interface counters
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  R* ring = reinterpret_cast<R*>(march_smem + 96);
+  const int maxb = A.rows * nx;  // band nodes of one plane, at most
+  const int slab = (A.rows + 2) * nx;
+  uint16_t* order = reinterpret_cast<uint16_t*>(ring + 4 * slab);  // [4][maxb]
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 4; k++) {
+      mbar_init(full + k, NP);
+      mbar_init(empty + k, NC);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool producer = threadIdx.x < NP;
+  const R wet = K.wet;
+  unsigned t0 = 0;  // ring sequence number of the item's first plane
+  for (int item = blockIdx.x; item < A.nitems; item += gridDim.x) {
+    const int band = item % A.nband, chunk = item / A.nband;
+    const int y0 = band * A.rows;
+    const int nr = min(A.rows, ny - y0);  // rows of this band
+    const int z0 = chunk * A.planes, z1 = min(nz, z0 + A.planes);
+    const int sl = (nr + 2) * nx;  // colours of a ring plane in use
+    const int ylo = y0 == 0 ? ny - 1 : y0 - 1, yhi = y0 + nr == ny ? 0 : y0 + nr;
+    if (producer) {
+      const int tid = threadIdx.x;
+      for (int p = z0 - 1; p <= z1; p++) {
+        const unsigned t = t0 + (unsigned)(p - (z0 - 1));
+        const int s = t & 3;
+        if (t >= 4) mbar_wait(empty + s, ((t >> 2) - 1) & 1, A);  // the consumers are done with its last plane
+        R* r = ring + s * slab;
+        for (int k = tid; k < sl; k += NP) r[k] = wet;
+        if (tid == 0) cnt[2 * s] = cnt[2 * s + 1] = 0;
+        role_sync(1, NP);
+        const int pz = p < 0 ? p + nz : (p >= nz ? p - nz : p);
+        const int rb = ny * pz;
+        const int a0 = __ldg(G.rowstart + rb + ylo), na = __ldg(G.rowstart + rb + ylo + 1) - a0;
+        const int b0 = __ldg(G.rowstart + rb + y0), nb = __ldg(G.rowstart + rb + y0 + nr) - b0;
+        const int c0 = __ldg(G.rowstart + rb + yhi), nc = __ldg(G.rowstart + rb + yhi + 1) - c0;
+        uint16_t* ord = order + s * maxb;
+        for (int k = tid; k < na + nb + nc; k += NP) {
+          const bool lo = k < na, hi = k >= na + nb;
+          const int i = lo ? a0 + k : (hi ? c0 + (k - na - nb) : b0 + (k - na));
+          uint32_t cw;
+          bool iface;
+          const R q = dens_colour<PREC>(K, G, src, dst, i, &cw, &iface);
+          int x, y, z;
+          unpack(cw, x, y, z);
+          r[(lo ? 0 : (hi ? nr + 1 : y - y0 + 1)) * nx + x] = q;
+          if (!lo && !hi) {
+            const int j = k - na;
+            if (!A.sort) ord[j] = (uint16_t)j;
+            else if (iface) ord[nb - 1 - atomicAdd(cnt + 2 * s + 1, 1)] = (uint16_t)j;
+            else ord[atomicAdd(cnt + 2 * s, 1)] = (uint16_t)j;
+          }
+        }
+        mbar_arrive(full + s);
+      }
+    } else {
+      const int tid = threadIdx.x - NP;
+      for (int q = z0; q < z1; q++) {
+        const unsigned tq = t0 + (unsigned)(q - (z0 - 1));  // sequence number of plane q
+        mbar_wait(full + ((tq + 1) & 3), ((tq + 1) >> 2) & 1, A);  // plane q+1 written (so q-1, q too)
+        const int rb = ny * q;
+        const int b0 = __ldg(G.rowstart + rb + y0), nq = __ldg(G.rowstart + rb + y0 + nr) - b0;
+        const R *s0 = ring + ((tq - 1) & 3) * slab, *s1 = ring + (tq & 3) * slab, *s2 = ring + ((tq + 1) & 3) * slab;
+        const uint16_t* ord = order + (tq & 3) * maxb;
+        for (int j = tid; j < nq; j += NC) {
+          // an order entry is below nq once the producers wrote this plane;
+          // the check keeps a wait that gave up inside the plane's band nodes
+          const int o = (int)ord[j];
+          if (o >= nq) continue;
+          const int i = b0 + o;
+          const uint32_t c = __ldg(G.coord + i), m = __ldg(G.mask + i);
+          int x, y, z;
+          unpack(c, x, y, z);
+          const int base = (y - y0 + 1) * nx + x;
+          const int ox0 = (m & (1u << (kWrapShift + 0))) ? nx - 1 : -1;
+          const int ox2 = (m & (1u << (kWrapShift + 1))) ? 1 - nx : 1;
+          auto col = [&](int a, int b, int e) -> R {
+            const R* pl = e == 0 ? s0 : (e == 1 ? s1 : s2);
+            return pl[base + (b - 1) * nx + (a == 0 ? ox0 : (a == 1 ? 0 : ox2))];
+          };
+          coll_node_c<PREC, true>(K, G, src, dst, i, c, m, col);
+        }
+        mbar_arrive(empty + ((tq - 1) & 3));  // plane q-1 is not read again
+      }
+      // nor are the item's last two planes
+      const unsigned tl = t0 + (unsigned)(z1 - (z0 - 1));
+      mbar_arrive(empty + ((tl - 1) & 3));
+      mbar_arrive(empty + (tl & 3));
+    }
+    t0 += (unsigned)(z1 - z0 + 2);
   }
 }
 

@@ -44,6 +44,8 @@ size_t lbm_step_smem(int prec, int tx, int ty, int occ);
 #define PS_DECL_PREC(P)                                                                                     \
   cudaError_t lbm_step_launch_##P(int tx, int ty, int zchunk, const LbmLaunchArgs& a);                     \
   cudaError_t lbm_fused_launch_##P(int tx, int occ, const LbmLaunchArgs& a, const FusedArgs& f);           \
+  cudaError_t lbm_march_launch_##P(int pw, const MarchArgs& A, const LbmLaunchArgs& a);                    \
+  int lbm_march_resident_##P(int pw, int rows, int nx);                                                   \
   cudaError_t lbm_wave_graph_##P(int tx, int ty, int occ, const LbmLaunchArgs* a, int steps, const int* first, \
                                  int S, int window, cudaGraph_t* g);                                        \
   cudaError_t lbm_batch_step_launch_##P(int tx, int ty, int occ, const BatchLaunchArgs& b);                \

@@ -139,6 +139,56 @@ cudaError_t step_fused_blk(const LbmLaunchArgs& a, const FusedArgs& f)
                             a.dst, static_cast<R*>(a.cc), f);
 }
 
+// one marching step (k_lbm_march): items of `rows` band rows x `planes`
+// chunk planes over a persistent grid of one CTA per SM with PW producer and
+// CW consumer warps.  FP64 has no marching form (its step is bound by the
+// FP64 pipe, not by memory).
+template <int PREC, int PW, int CW>
+cudaError_t step_march_blk(const LbmLaunchArgs& a, const MarchArgs& A0)
+{
+  if constexpr (PREC == 0) {
+    return cudaErrorInvalidValue;
+  } else {
+    using R = typename Store<PREC>::R;
+    if (a.G.nl == 0) return cudaSuccess;
+    MarchArgs A = A0;
+    A.nband = (a.G.ny + A.rows - 1) / A.rows;
+    A.nitems = A.nband * ((a.G.nz + A.planes - 1) / A.planes);
+    const size_t smem = march_smem_bytes<R>(A.rows, a.G.nx);
+    cudaError_t e = cudaFuncSetAttribute(k_lbm_march<PREC, PW, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_lbm_march<PREC, PW, CW><<<(unsigned)std::min(sms, A.nitems), 32 * (PW + CW), smem, a.stream>>>(
+        *static_cast<const LbmConst<R>*>(a.K), a.G, a.src, a.dst, A);
+    return cudaGetLastError();
+  }
+}
+
+// resident CTAs per SM of the marching kernel with its ring for `rows` band
+// rows (0: the ring does not fit, or the collide order would overflow 16 bits)
+template <int PREC, int PW, int CW>
+int march_resident(int rows, int nx)
+{
+  if constexpr (PREC == 0) {
+    return 0;
+  } else {
+    using R = typename Store<PREC>::R;
+    const size_t smem = march_smem_bytes<R>(rows, nx);
+    if (smem > 227 * 1024 || (size_t)rows * nx > 65535) return 0;
+    if (cudaFuncSetAttribute(k_lbm_march<PREC, PW, CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_lbm_march<PREC, PW, CW>, 32 * (PW + CW), smem) !=
+        cudaSuccess)
+      return 0;
+    return n;
+  }
+}
+
 template <int PREC>
 cudaError_t fields(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc)
 {
@@ -250,6 +300,18 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
     if (tx == 128 && ty == 256 && occ == 8) return detail::step_batch_blk<P, 128, 256, 8>(b);              \
     if (tx == 256 && ty == 256 && occ == 3) return detail::step_batch_blk<P, 256, 256, 3>(b);              \
     return cudaErrorInvalidValue;                                                                          \
+  }                                                                                                        \
+  cudaError_t lbm_march_launch_##P(int pw, const MarchArgs& A, const LbmLaunchArgs& a)                     \
+  {                                                                                                        \
+    if (pw == 4) return detail::step_march_blk<P, 4, 20>(a, A);                                            \
+    if (pw == 8) return detail::step_march_blk<P, 8, 16>(a, A);                                            \
+    return cudaErrorInvalidValue;                                                                          \
+  }                                                                                                        \
+  int lbm_march_resident_##P(int pw, int rows, int nx)                                                    \
+  {                                                                                                        \
+    if (pw == 4) return detail::march_resident<P, 4, 20>(rows, nx);                                        \
+    if (pw == 8) return detail::march_resident<P, 8, 16>(rows, nx);                                        \
+    return 0;                                                                                              \
   }                                                                                                        \
   cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc) \
   {                                                                                                        \

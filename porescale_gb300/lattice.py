@@ -129,8 +129,17 @@ class Lattice:
         """Fused one-launch step over z-slabs of `planes` planes (0: two-pass)."""
         check(self._lib.ps_lbm_set_fused(self._h, planes, ahead))
 
+    def set_march(self, rows: int, planes: int = 0, producers: int = 4, sort: bool = True) -> None:
+        """Marching one-launch step over items of `rows` y-rows and `planes`
+        z-planes (0: about two per SM), `producers` density warps per CTA,
+        bulk nodes collided before interface nodes when sort; rows 0 turns
+        it off."""
+        check(self._lib.ps_lbm_set_march(self._h, rows, planes, producers, int(bool(sort))))
+        self.info = self.get_info()
+
     def set_wait_limit(self, polls: int) -> None:
-        """Polls before a fused-step wait gives up (0: the default 2^22)."""
+        """Polls before a fused- or marching-step wait gives up (0: the
+        default 2^22)."""
         check(self._lib.ps_lbm_set_wait_limit(self._h, polls))
 
     def set_wave(self, planes: int, window: int = 0) -> None:

@@ -345,3 +345,87 @@ def test_fused_wait_gives_up_and_recovers(gpu):
         R.step(6)
         want = R.get_state()
     assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3])
+@pytest.mark.parametrize("rows,planes,producers,sort", [(4, 0, 4, True), (1, 1, 4, True), (5, 7, 8, True),
+                                                        (18, 3, 4, False), (64, 64, 8, True), (3, 2, 4, True)])
+def test_march_schedule_matches_two_pass(gpu, prec, rows, planes, producers, sort):
+    """The marching one-launch step (items of `rows` rows by `planes`
+    planes walked by producer and consumer warps, halo rows recomputed)
+    gives the two-pass step's state bit for bit: partial last band and
+    chunk, one-row bands, one band or one chunk over the whole box, several
+    items per CTA, solid planes, sorted and natural collide order, and the
+    restart step that reads a state set from outside."""
+    ind = geo.sphere_pack((22, 18, 20), 0.45, 3.0, seed=17)
+    ind[:, :, 8:10] = 1  # two solid planes
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    out = []
+    for march in (False, True):
+        with Lattice(p, ind, prec) as L:
+            L.init_random(0.5)
+            if march:
+                L.set_march(rows, planes, producers, sort)
+                m = L.get_info().march
+                assert m & 4095 == min(rows, 18) and (m >> 12) & 0x1FFF >= 1
+                assert ((m >> 25) & 3) * 4 == producers and bool((m >> 30) & 1) == (not sort)
+            L.step(13)
+            fr, fb = L.get_state()
+            L.set_state(fr, fb)
+            L.step(4)
+            L.sync()
+            out.append(L.get_state())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_march_argument_errors(gpu):
+    ind = geo.sphere_pack((12, 12, 12), 0.45, 3.0, seed=3)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    with Lattice(p, ind, PREC_F64) as L:
+        with pytest.raises(PorescaleError):
+            L.set_march(4, 0)  # FP64 has no marching form
+    with Lattice(p, ind, PREC_F16) as L:
+        with pytest.raises(PorescaleError):
+            L.set_march(4, 0, producers=6)  # 4 or 8 producer warps
+        L.set_march(4, 0)
+        L.set_wave(4)
+        assert L.get_info().march == 0
+        L.set_march(2, 3)
+        assert L.get_info().wave == 0 and L.get_info().march & 0x1FFFFFF == 2 + 4096 * 3
+
+
+def test_march_wait_gives_up_and_recovers(gpu):
+    """The marching step's bounded mbarrier waits, run out on purpose: with
+    one poll the colliding warps find their planes unwritten, give up, and
+    the next synchronising call returns PS_ERR_TIMEOUT; the launch ends
+    (every wait returns, every thread arrives on every barrier, every index
+    comes from the geometry).  After ps_lbm_set_state the lattice, back on
+    the default limit, steps as a fresh one."""
+    ind = geo.sphere_pack((48, 40, 40), 0.45, 3.0, seed=19)
+    p = make_params(B=0.7, sig=1e-3, vir=1 / 6, vib=0.1, wet=0.5, bfr=(1e-5, 0, 0), bfb=(1e-5, 0, 0))
+    with Lattice(p, ind, PREC_F16) as L:
+        L.init_random(0.5)
+        fr0, fb0 = L.get_state()
+        L.set_march(4, 0)
+        L.set_wait_limit(1)
+        timed_out = False
+        for _ in range(20):
+            L.step(1)
+            try:
+                L.sync()
+            except PorescaleError as exc:
+                assert exc.code == 4  # PS_ERR_TIMEOUT
+                timed_out = True
+                break
+        assert timed_out
+        L.sync()
+        L.set_wait_limit(0)
+        L.set_state(fr0, fb0)
+        L.step(6)
+        L.sync()
+        got = L.get_state()
+    with Lattice(p, ind, PREC_F16) as R:
+        R.set_state(fr0, fb0)
+        R.step(6)
+        want = R.get_state()
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
