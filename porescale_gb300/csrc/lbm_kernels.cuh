@@ -867,25 +867,29 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b)
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(b))
                : "memory");
 }
+// non-blocking test of the completion of the phase of parity `parity`
 __device__ __forceinline__ bool mbar_test(uint64_t* b, unsigned parity)
 {
   unsigned ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(smem_addr(b)), "r"(parity)
       : "memory");
   return ok != 0;
 }
-// waits (bounded) for the completion of the barrier's phase of parity `parity`
+// waits for that phase, at most A.spin polls about 32 ns apart (2^22 polls:
+// a fraction of a second), then gives up and flags the error
 __device__ __forceinline__ void mbar_wait(uint64_t* b, unsigned parity, const MarchArgs& A)
 {
-  for (unsigned n = 0; !mbar_test(b, parity); n++)
+  for (unsigned n = 0; !mbar_test(b, parity); n++) {
     if (n >= A.spin) {
       atomicExch(A.err, 1);
       return;
     }
+    __nanosleep(32);
+  }
 }
 // named barrier among the `count` threads of one role
 __device__ __forceinline__ void role_sync(int id, int count)
