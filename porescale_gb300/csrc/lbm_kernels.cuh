@@ -266,6 +266,13 @@ struct Pop {
   {
     *(static_cast<T2*>(b.pop) + (long long)d * pitch + i) = from_f2<T2>(gr * DevScale<T>::up, gb * DevScale<T>::up);
   }
+  // the same, stochastically rounded with the random bits rnd (16-bit)
+  __device__ __forceinline__ static void put_dev_sr(const BufDev& b, int d, int i, long long pitch, R gr, R gb,
+                                                    uint32_t rnd)
+  {
+    *(static_cast<T2*>(b.pop) + (long long)d * pitch + i) =
+        from_f2_sr<T2>(gr * DevScale<T>::up, gb * DevScale<T>::up, rnd);
+  }
   // writes the (red, blue) pair (vr, vb) into slot (d, i) whose node has
   // deviation references rho; 16-bit storage rounds stochastically with the
   // random bits rnd
@@ -545,6 +552,55 @@ __device__ __forceinline__ NbOff box_offsets(const GeomDev& G, uint32_t m)
   return nb_offsets(m, G.nx, G.nx * G.ny, G.nx * G.ny, G.nz);
 }
 
+// 16-bit (sender-reference) storage in deviation form: node i's stored
+// deviations re-expressed against its own densities of the step that wrote
+// them, own = src.rho[v]: g'_d = g_d + t_d (rho_writer(d) - own), the
+// difference of two nearby FP32 densities being exact.  Returns own.
+template <int PREC>
+__device__ __forceinline__ float2 read_node_s_dev(const LbmConst<float>& K, const GeomDev& G, const BufDev& src,
+                                                  int i, uint32_t m, long long v, const NbOff& o, float* gr,
+                                                  float* gb)
+{
+  const float2* rv = src.rho + v;
+  const float2 own = __ldg(rv);
+  const uint32_t wm = src.recv ? 0u : m;  // links whose slot another node wrote
+  Pop<PREC>::load_dev(src, 0, i, G.pitch, gr[0], gb[0]);
+#pragma unroll
+  for (int d = 1; d < 19; d++) {
+    float a, b;
+    Pop<PREC>::load_dev(src, d, i, G.pitch, a, b);
+    if (wm & (1u << (d - 1))) {
+      const float2 rw = __ldg(rv + o.x[1 - cvx(d)] + o.y[1 - cvy(d)] + o.z[1 - cvz(d)]);
+      a = a + K.t[0][wcls(d)] * (rw.x - own.x);
+      b = b + K.t[1][wcls(d)] * (rw.y - own.y);
+    }
+    gr[d] = a;
+    gb[d] = b;
+  }
+  return own;
+}
+
+// pushes out_c[d] = t^c_d S_c + Z_c[d] (node_update_dev) to the receivers
+// under sender-reference storage: every population against node i's own
+// current densities rn, t^c_d (S_c - rn_c) + Z_c[d], stochastically rounded
+template <int PREC>
+__device__ __forceinline__ void push_node_s_dev(const LbmConst<float>& K, const GeomDev& G, const BufDev& dst, int i,
+                                                uint32_t m, const int* s, float Sr, float Sb, const float* Zr,
+                                                const float* Zb, float2 rn)
+{
+  const uint32_t seed = dither_seed((uint32_t)i, step_of(dst));
+  const float dr = Sr - rn.x, db = Sb - rn.y;
+  Pop<PREC>::put_dev_sr(dst, 0, i, G.pitch, K.t[0][0] * dr + Zr[0], K.t[1][0] * db + Zb[0], dither_bits(seed, 0));
+#pragma unroll
+  for (int e = 1; e < 19; e++) {
+    const int oe = opp(e);
+    const bool stream = m & (1u << (oe - 1));
+    const int w = wcls(e);
+    Pop<PREC>::put_dev_sr(dst, stream ? e : oe, stream ? s[oe] : i, G.pitch, K.t[0][w] * dr + Zr[e],
+                          K.t[1][w] * db + Zb[e], dither_bits(seed, e));
+  }
+}
+
 // The 19 post-streaming populations of both components of node i from its
 // own slots: f[0..18] red, f[19..37] blue.
 template <int PREC>
@@ -632,11 +688,20 @@ __device__ __forceinline__ void coll_node_c(const LbmConst<typename Store<PREC>:
   using R = typename Store<PREC>::R;
   int x, y, z;
   unpack(c, x, y, z);
-  // FP32 storage: shifted arithmetic on the deviations (the storage is
-  // precise enough for it to matter).  16-bit storage: its rounding (~1e-3
-  // relative on the deviations) dominates either way, so the full-value
-  // form, ~10% fewer instructions, is used.
-  if constexpr (PREC == 1) {
+  // FP32 and 16-bit storage: shifted arithmetic on the deviations.  The
+  // full-value form would round every population at ~4e-9 absolute (ulp of
+  // t_d ~ 0.05), which a steady flow repeats step after step: the body-force
+  // increment (~1e-6) then carries a fixed error of ~1e-3 relative.
+  if constexpr (Store<PREC>::kSendRef) {
+    float gr[19], gb[19], Zr[19], Zb[19], Sr, Sb;
+    const long long v = x + (long long)G.nx * (y + (long long)G.ny * z);
+    const float2 own = read_node_s_dev<PREC>(K, G, src, i, m, v, box_offsets(G, m), gr, gb);
+    const float2 rn = ld_step(dst.rho + v, kCoh);  // this step's densities (density pass)
+    node_update_dev(K, gr, gb, own.x, own.y, rn.x, rn.y, col, Sr, Sb, Zr, Zb);
+    int s[19];
+    pull_sources(G, i, c, m, s);
+    push_node_s_dev<PREC>(K, G, dst, i, m, s, Sr, Sb, Zr, Zb, rn);
+  } else if constexpr (PREC == 1) {
     float gr[19], gb[19], Zr[19], Zb[19], Sr, Sb;
     const float2 ro = read_node_dev<PREC>(G, src, i, gr, gb);
     const float2 rn = ld_step(dst.rho + i, kCoh);  // this step's densities (density pass)
