@@ -212,12 +212,25 @@ __device__ __forceinline__ uint32_t step_of(const BufDev& b)
 // (a, b) to a 16-bit pair, stochastically rounded with the random bits r
 template <typename T2>
 __device__ __forceinline__ T2 from_f2_sr(float a, float b, uint32_t r);
+// x dithered for a conversion to FP16 by rounding toward zero, with 13
+// random bits r: in FP16's normal range the random integer goes below the
+// 13 mantissa bits the conversion drops; below 2^-14, where FP16's grid is
+// 2^-24 whatever the exponent (subnormals), x is rounded stochastically on
+// that grid directly, so that tiny values are not pulled toward zero
+__device__ __forceinline__ float dither_f16(float x, uint32_t r)
+{
+  if (fabsf(x) >= 6.103515625e-05f) return __uint_as_float(__float_as_uint(x) + r);
+  const float q = x * 16777216.0f;  // x / 2^-24, exact
+  const float fl = floorf(q);
+  const float u = (float)r * (1.0f / 8192.0f);  // uniform in [0, 1)
+  return (fl + (q - fl > u ? 1.0f : 0.0f)) * 5.9604644775390625e-08f;  // on the grid: converts exactly
+}
 template <>
 __device__ __forceinline__ __half2 from_f2_sr<__half2>(float a, float b, uint32_t r)
 {
   // FP16 keeps 10 of FP32's 23 mantissa bits: 13 random bits each
-  const float ad = __uint_as_float(__float_as_uint(a) + (r & 0x1FFFu));
-  const float bd = __uint_as_float(__float_as_uint(b) + ((r >> 16) & 0x1FFFu));
+  const float ad = dither_f16(a, r & 0x1FFFu);
+  const float bd = dither_f16(b, (r >> 16) & 0x1FFFu);
   uint32_t h;
   asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(bd), "f"(ad));
   return *reinterpret_cast<__half2*>(&h);
@@ -696,8 +709,16 @@ __device__ __forceinline__ void coll_node_c(const LbmConst<typename Store<PREC>:
     float gr[19], gb[19], Zr[19], Zb[19], Sr, Sb;
     const long long v = x + (long long)G.nx * (y + (long long)G.ny * z);
     const float2 own = read_node_s_dev<PREC>(K, G, src, i, m, v, box_offsets(G, m), gr, gb);
-    const float2 rn = ld_step(dst.rho + v, kCoh);  // this step's densities (density pass)
-    node_update_dev(K, gr, gb, own.x, own.y, rn.x, rn.y, col, Sr, Sb, Zr, Zb);
+    const float2 rn = ld_step(dst.rho + v, kCoh);  // this step's densities (density pass): the push reference
+    // the collision's densities in its own terms, own + sum g' (the density
+    // pass sums t_d rho_writer + g, whose rounded weights do not add to 1)
+    float sr = gr[0], sb = gb[0];
+#pragma unroll
+    for (int d = 1; d < 19; d++) {
+      sr = sr + gr[d];
+      sb = sb + gb[d];
+    }
+    node_update_dev(K, gr, gb, own.x, own.y, own.x + sr, own.y + sb, col, Sr, Sb, Zr, Zb);
     int s[19];
     pull_sources(G, i, c, m, s);
     push_node_s_dev<PREC>(K, G, dst, i, m, s, Sr, Sb, Zr, Zb, rn);
