@@ -373,7 +373,9 @@ def accuracy(args, cfg):
         if q == "f64" and ref_hist is not None and [r["step"] for r in ref_hist] == expected:
             hist[q] = ref_hist
             continue
-        L = Lattice(p, ind, PREC_ID["f64" if q in ("f64p", "f64n") else q])
+        L = Lattice(p, ind, PREC_ID["f64" if q in ("f64p", "f64n") else q.split(":")[0]])
+        if ":" in q:  # "f16:k": the same storage with rounding seed k
+            L.set_rounding_seed(int(q.split(":")[1]))
         if q == "f64n":
             # a perturbation of the size of FP32 rounding (1e-7 relative,
             # seeded): an FP64 run that diverges from the unperturbed one as

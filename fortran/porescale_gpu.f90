@@ -123,6 +123,16 @@ module porescale_gpu
       type(c_ptr), value :: handle
       integer(c_int32_t), value :: rows, planes, producers, sort
     end function
+    integer(c_int) function ps_lbm_set_sort(handle, on) bind(c, name='ps_lbm_set_sort')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: on
+    end function
+    integer(c_int) function ps_lbm_set_rounding_seed(handle, seed) bind(c, name='ps_lbm_set_rounding_seed')
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: handle
+      integer(c_int32_t), value :: seed
+    end function
     integer(c_int) function ps_lbm_set_wave(handle, planes, window) bind(c, name='ps_lbm_set_wave')
       import :: c_int, c_int32_t, c_ptr
       type(c_ptr), value :: handle

@@ -175,6 +175,17 @@ int ps_lbm_set_wave(void *handle, int32_t planes, int32_t window);
  * storage; rows = 0 turns it off.  Turns the fused and wavefront schedules
  * off (and they turn this one off). */
 int ps_lbm_set_march(void *handle, int32_t rows, int32_t planes, int32_t producers, int32_t sort);
+/* Two-pass (and wavefront) collide kernel: on != 0 lets each CTA collide
+ * its bulk nodes before its interface nodes (classes read from the density
+ * pass's densities), so that a warp runs one branch of the node update
+ * rather than both; every node's arithmetic is unchanged (FP32 and 16-bit
+ * storage).  No counterpart in the reference: a kernel option. */
+int ps_lbm_set_sort(void *handle, int32_t on);
+/* Seed of the stochastic rounding of 16-bit stores (default 0): the random
+ * bits are a hash of (node, direction, step number + a seed offset), so runs
+ * with different seeds are independent samples of the rounding and runs
+ * with the same seed are identical.  No counterpart in the reference. */
+int ps_lbm_set_rounding_seed(void *handle, uint32_t seed);
 /* Times the candidate configurations (two-pass, fused, wavefront) on the current
  * state (restored afterwards) and keeps the fastest; writes its tile to
  * *tx, *ty, *occ (the schedules are in ps_lbm_info.schedule and .wave). */

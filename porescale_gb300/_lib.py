@@ -80,6 +80,8 @@ SIGNATURES = {
     "ps_lbm_autotune": (C.c_int, [_P, C.c_int32, _IP, _IP, _IP]),
     "ps_lbm_set_fused": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "ps_lbm_set_wait_limit": (C.c_int, [_P, C.c_int32]),
+    "ps_lbm_set_sort": (C.c_int, [_P, C.c_int32]),
+    "ps_lbm_set_rounding_seed": (C.c_int, [_P, C.c_uint32]),
     "ps_lbm_set_march": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "ps_lbm_set_wave": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "ps_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),

@@ -75,6 +75,7 @@ struct Lattice {
   // marching step (0 rows: off): band rows, chunk planes (march_req as
   // requested, 0 = about two items per SM), producer warps, collide order
   int march_rows = 0, march_planes = 0, march_req = 0, march_pw = 4, march_sort = 1;
+  int coll_sort = 0;  // two-pass collide: order each CTA's nodes bulk first
   cudaGraphExec_t wave_exec[2] = {nullptr, nullptr};
   int wave_key[5] = {0, 0, 0, 0, 0};  // (tx, ty, occ, planes, window) of wave_exec
   int obs_blocks = 0;
@@ -83,6 +84,7 @@ struct Lattice {
   // rounding of 16-bit stores (graph replays read it from d_stepbase)
   uint32_t nsteps = 0;
   uint32_t* d_stepbase = nullptr;
+  uint32_t rseed = 0;  // seed of the stochastic rounding (offsets every step number)
   // per buffer: 16-bit slots stored against the reading node's densities (a
   // state set from outside; the first step reads it so, every step writes
   // against the writing node's)
@@ -107,6 +109,7 @@ struct Lattice {
     g.ref = d_ref;
     g.rowstart = d_rowstart;
     g.rowbits = d_rowbits;
+    g.sort = coll_sort;
     return g;
   }
   BufDev buf(int b) const
@@ -115,7 +118,7 @@ struct Lattice {
     r.pop = d_pop[b];
     r.rho = d_rho[b];
     r.recv = recv[b];
-    r.step = nsteps;
+    r.step = nsteps + rseed * 0x632BE5ABu;
     r.stepbase = nullptr;
     return r;
   }
@@ -460,6 +463,15 @@ int ensure_schedule(Lattice* L)
   return PS_OK;
 }
 
+// the instantiated wavefront graphs are rebuilt on their next use
+void drop_wave_graphs(Lattice* L)
+{
+  for (cudaGraphExec_t& x : L->wave_exec) {
+    if (x) cudaGraphExecDestroy(x);
+    x = nullptr;
+  }
+}
+
 constexpr int kWaveSteps = 8;  // steps per wavefront graph (even: the buffers end where they began)
 
 // the wavefront graph starting from buffer L->cur for the current
@@ -483,7 +495,7 @@ int ensure_wave(Lattice* L)
     const int b = L->cur ^ (s & 1);
     a[s] = L->args(b, 1 - b);
     a[s].src.recv = a[s].dst.recv = 0;
-    a[s].dst.step = (uint32_t)s;  // plus the step base set before each replay
+    a[s].dst.step = (uint32_t)s + L->rseed * 0x632BE5ABu;  // plus the step base set before each replay
     a[s].dst.stepbase = L->d_stepbase;
   }
   cudaGraph_t g = nullptr;
@@ -694,7 +706,7 @@ VolTable batch_table(const Batch* B, int flip, bool first = false, int graph_ste
     T.v[v].dst = L->buf(c ^ 1);
     T.v[v].dst.recv = 0;
     if (graph_step >= 0) {  // captured: the step counts from the lattice's step base
-      T.v[v].dst.step = (uint32_t)graph_step;
+      T.v[v].dst.step = (uint32_t)graph_step + L->rseed * 0x632BE5ABu;
       T.v[v].dst.stepbase = L->d_stepbase;
     }
     if (!first) T.v[v].src.recv = 0;
@@ -735,6 +747,7 @@ int batch_steps(Batch* B, int n)
   }
   std::vector<int> cur;
   for (Lattice* L : B->L) cur.push_back(L->cur);
+  for (Lattice* L : B->L) cur.push_back((int)L->rseed);  // captured steps carry the rounding seeds
   const bool valid = B->exec && B->g_tx == B->tx && B->g_ty == B->ty && B->g_occ == B->occ && B->graph_cur == cur;
   if (n >= kGraphSteps && !valid) {
     if (B->exec) cudaGraphExecDestroy(B->exec);
@@ -775,7 +788,6 @@ int batch_steps(Batch* B, int n)
   }
   for (; done < n; done++) {
     VolTable T = batch_table(B, done & 1);
-    for (size_t v = 0; v < B->L.size(); v++) T.v[v].dst.step = B->L[v]->nsteps;  // buffers flipped, counts not yet
     cudaError_t e = batch_launch(B, T);
     if (e != cudaSuccess) return cuda_fail(e, "batch step");
     for (Lattice* L : B->L) L->nsteps++;
@@ -1359,6 +1371,24 @@ int ps_lbm_set_wave(void* h, int32_t planes, int32_t window)
   L->wave_planes = planes;
   L->wave_window = window;
   if (planes > 0) L->fused_planes = L->march_rows = 0;
+  return PS_OK;
+}
+
+int ps_lbm_set_rounding_seed(void* h, uint32_t seed)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_rounding_seed: null handle");
+  Lattice* L = as_lattice(h);
+  L->rseed = seed;
+  drop_wave_graphs(L);  // their steps carry the seed
+  return PS_OK;
+}
+
+int ps_lbm_set_sort(void* h, int32_t on)
+{
+  if (!h) return fail(PS_ERR_ARG, "ps_lbm_set_sort: null handle");
+  Lattice* L = as_lattice(h);
+  L->coll_sort = on ? 1 : 0;
+  drop_wave_graphs(L);  // their launches carry the option
   return PS_OK;
 }
 

@@ -99,6 +99,7 @@ struct GeomDev {
   const int32_t* ref;      // [nl] reference fluid index (i outer, k inner order)
   const int32_t* rowstart; // [ny*nz + 1]
   const uint2* rowbits;    // [ny*nz*nwords] (fluid bits, fluid count before the word)
+  int sort;                // step option: the collide kernel orders each CTA's nodes bulk first
 };
 
 // one population buffer: pop -> 19*pitch (red, blue) pairs, rho -> pitch
@@ -719,14 +720,37 @@ __global__ void __launch_bounds__(BLK, (PREC == 0 ? 1024 : 2048) / BLK) k_lbm_de
 
 // MINB > 0 asks the register allocator for MINB resident CTAs per SM;
 // 0 keeps 640 resident threads per SM (the allocator's unconstrained
-// choice for this kernel uses too many registers for that)
+// choice for this kernel uses too many registers for that).  With G.sort
+// (FP32 and 16-bit storage) a CTA first reads its nodes' current densities
+// (the density pass wrote them) and collides its bulk nodes before its
+// interface nodes, thread t taking the t-th node of that order, so that a
+// warp runs one branch of the node update instead of both; every node's
+// arithmetic is unchanged.
 template <int PREC, int BLK, int MINB>
 __global__ void __launch_bounds__(BLK, MINB > 0 ? MINB : 640 / BLK) k_lbm_coll(const __grid_constant__ LbmConst<typename Store<PREC>::R> K,
                                                   const __grid_constant__ GeomDev G, const BufDev src,
                                                   const BufDev dst, const typename Store<PREC>::R* __restrict__ cc,
                                                   int i0, int i1)
 {
-  const int i = i0 + blockIdx.x * BLK + threadIdx.x;
+  const int base = i0 + blockIdx.x * BLK;
+  int i = base + threadIdx.x;
+  if constexpr (Store<PREC>::kDev) {
+    if (G.sort) {
+      __shared__ int order[BLK], cnt[2];
+      if (threadIdx.x == 0) cnt[0] = cnt[1] = 0;
+      __syncthreads();
+      if (i < i1) {
+        const long long ri = Store<PREC>::kSendRef ? voxel_of(G, __ldg(G.coord + i)) : (long long)i;
+        const float2 r = __ldg(dst.rho + ri);
+        const bool iface = !(r.y <= K.ee) && !(r.x <= K.ee);
+        if (iface) order[BLK - 1 - atomicAdd(cnt + 1, 1)] = i;
+        else order[atomicAdd(cnt, 1)] = i;
+      }
+      __syncthreads();
+      const int t = threadIdx.x;
+      i = (t < cnt[0] || t >= BLK - cnt[1]) ? order[t] : i1;  // the gap: threads past the end
+    }
+  }
   if (i < i1) coll_node<PREC>(K, G, src, dst, cc, i);
 }
 

@@ -137,6 +137,14 @@ class Lattice:
         check(self._lib.ps_lbm_set_march(self._h, rows, planes, producers, int(bool(sort))))
         self.info = self.get_info()
 
+    def set_sort(self, on: bool) -> None:
+        """Two-pass collide: bulk nodes before interface nodes in each CTA."""
+        check(self._lib.ps_lbm_set_sort(self._h, int(bool(on))))
+
+    def set_rounding_seed(self, seed: int) -> None:
+        """Seed of the stochastic rounding of 16-bit stores (default 0)."""
+        check(self._lib.ps_lbm_set_rounding_seed(self._h, int(seed) & 0xFFFFFFFF))
+
     def set_wait_limit(self, polls: int) -> None:
         """Polls before a fused- or marching-step wait gives up (0: the
         default 2^22)."""
