@@ -722,6 +722,7 @@ def main():
     ap.add_argument("--tile", default="", help="tx,ty,occ: pin the step configuration instead of autotuning")
     ap.add_argument("--wave", default="", help="planes,window: with --tile, pin the wavefront schedule")
     ap.add_argument("--march", default="", help="rows,planes,producers,sort: with --tile, pin the marching step")
+    ap.add_argument("--sort", type=int, default=-1, help="with --tile: 1/0 pins the sorted collide order")
     ap.add_argument("--no-lsm", action="store_true", help="skip the lattice-spring leg")
     ap.add_argument("--lsm-cpu-budget", type=float, default=10.0,
                     help="seconds of each CPU spring-solve baseline (CG, relaxation)")
@@ -803,6 +804,8 @@ def main():
                 L.set_wave(*[int(v) for v in args.wave.split(",")])
             if args.march:
                 L.set_march(*[int(v) for v in args.march.split(",")])
+            if args.sort >= 0:
+                L.set_sort(bool(args.sort))
             L.info = L.get_info()
         elif not args.no_autotune:
             L.autotune(4 if q != "f64" else 2)
