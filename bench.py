@@ -139,6 +139,37 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def load_accuracy(prec: str, cfg):
+    """The k_r errors of storage precision `prec` against FP64 from the
+    committed 20,000-step record of this workload (profiles/accuracy_256.json,
+    written by --accuracy-steps 20000 --accuracy-every 100), or None.  For
+    stochastically rounded storage the mean over the recorded rounding
+    seeds, with the largest and the error of the seed ensemble."""
+    path = os.path.join(ROOT, "profiles", "accuracy_256.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    if d.get("workload") != cfg["workload"] or prec not in d.get("kr_err", {}):
+        return None
+    k = d["kr_err"]
+    out = {"kr_err_red": k[prec]["red"], "kr_err_blue": k[prec]["blue"], "definition": k["definition"],
+           "window": k["window"], "samples": k["samples"], "steps": d["steps"],
+           "floor_f64_one_ulp": [k["f64p"]["red"], k["f64p"]["blue"]],
+           "max_sample_rel_err": [d["rel_err_vs_f64"][prec]["permr"], d["rel_err_vs_f64"][prec]["permb"]],
+           "source": "profiles/accuracy_256.json"}
+    if "f64n" in k:
+        out["floor_f64_perturbed_1e-7"] = [k["f64n"]["red"], k["f64n"]["blue"]]
+    seeds = k.get(prec + "_over_seeds")
+    if seeds:
+        out.update({"kr_err_red": seeds["red_mean"], "kr_err_blue": seeds["blue_mean"],
+                    "kr_err_max_over_seeds": [seeds["red_max"], seeds["blue_max"]],
+                    "kr_err_of_seed_ensemble": [seeds["ensemble_mean_error"]["red"],
+                                                seeds["ensemble_mean_error"]["blue"]],
+                    "rounding_seeds": seeds["seeds"]})
+    return out
+
+
 def load_traffic(prec: str, nl: int, kind: str = "two-pass"):
     """DRAM bytes of one step from the committed ncu summary (scaled to this
     workload's fluid-node count; key "<prec>" for the two-pass step,
@@ -936,6 +967,7 @@ def main():
                      "frac": h["frac"], "traffic": traffic, "peak_kind": peak_kind,
                      "algo_bytes_per_node": ALGO_BYTES[args.prec]},
         "e2e": res.get("e2e"),
+        "accuracy": load_accuracy(args.prec, cfg) if args.size == 256 else None,
         "cpu_baseline": cpu,
         "gpu_launches": (h["steps"] // 8 * 8 * h["kernels_per_step"] + h["steps"] % 8 * 2
                          if h["schedule"]["kind"] == "wave" else h["steps"] * h["kernels_per_step"]),
