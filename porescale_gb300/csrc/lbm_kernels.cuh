@@ -1019,7 +1019,11 @@ __global__ void __launch_bounds__(32 * (PW + CW), 1)
         const int b0 = __ldg(G.rowstart + rb + y0), nq = __ldg(G.rowstart + rb + y0 + nr) - b0;
         const R *s0 = ring + ((tq - 1) & 3) * slab, *s1 = ring + (tq & 3) * slab, *s2 = ring + ((tq + 1) & 3) * slab;
         const uint16_t* ord = order + (tq & 3) * maxb;
-        for (int j = tid; j < nq; j += NC) {
+        // a plane has a little more band nodes than colliding threads: the
+        // threads that take a second node rotate from plane to plane, so the
+        // ring's two planes of slack even the work out
+        const int rot = (int)((tq * 97u) % (unsigned)NC);
+        for (int j = tid >= rot ? tid - rot : tid - rot + NC; j < nq; j += NC) {
           // an order entry is below nq once the producers wrote this plane;
           // the check keeps a wait that gave up inside the plane's band nodes
           const int o = (int)ord[j];
