@@ -955,6 +955,10 @@ def main():
     lsm = None
     if rank == 0 and not args.no_lsm:
         lsm = lsm_leg(cpu_budget=0.0 if args.no_cpu_baseline else args.lsm_cpu_budget)
+        # the same solve at 128^3 (the differentiation workload's size), where
+        # the CG vectors no longer fit in L2
+        big = lsm_leg(size=128)
+        lsm["size128"] = {k: v for k, v in big.items() if k != "cpu_baseline"}
     h = res[args.prec]
     traffic = load_traffic(args.prec, nl, h["schedule"]["kind"])
     line = {
