@@ -53,7 +53,7 @@ def workload_config(size: int):
 
 def march_fields(m: int):
     """(rows, planes, producer warps, sorted) of ps_lbm_info.march."""
-    return m & 4095, (m >> 12) & 0x1FFF, ((m >> 25) & 3) * 4, not (m >> 30) & 1
+    return m & 4095, (m >> 12) & 0x1FFF, ((m >> 25) & 3) * 4, not (m >> 30) & 1  # producer warps 4, 8, 12
 
 
 def bench_config(cfg, nl):
@@ -881,8 +881,8 @@ def main():
                 L.set_state(fr, fb)
                 study[f"w{planes}/{window}"] = nl * 48 / time_steps(L, 48, 8, torch) / 1e6
             # marching one-launch steps (band rows, producer warps, sorted order)
-            for rows, pw, srt in ((4, 4, True), (8, 4, True), (16, 4, True), (8, 8, True), (16, 8, True),
-                                  (8, 4, False)):
+            for rows, pw, srt in ((8, 4, True), (8, 8, True), (16, 8, True), (8, 12, True), (16, 12, True),
+                                  (8, 8, False)):
                 L.set_wave(0)
                 L.set_march(rows, 0, pw, srt)
                 L.set_state(fr, fb)

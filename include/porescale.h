@@ -161,8 +161,8 @@ int ps_lbm_set_wait_limit(void *handle, int32_t polls);
 int ps_lbm_set_wave(void *handle, int32_t planes, int32_t window);
 /* Marching step: rows > 0 runs each step as ONE persistent launch (one CTA
  * per SM) over items of `rows` y-rows (every x) times `planes` z-planes (0:
- * about two items per SM).  Inside a CTA, `producers` warps (4 or 8; the
- * other 24 - producers warps collide) walk the item in z computing the
+ * about three items per SM).  Inside a CTA, `producers` warps (4, 8 or 12;
+ * the other 24 - producers warps collide) walk the item in z computing the
  * densities and stencil colours of each plane -- band plus one recomputed
  * halo row per side, so no CTA waits for another -- into a 4-plane ring in
  * shared memory, up to two planes ahead of the colliding warps, which read

@@ -580,7 +580,7 @@ int check_fused(Lattice* L)
 }
 
 // turns the marching step on with band rows `rows`, chunk planes `planes`
-// (0: about two items per SM), `pw` producer warps (4 or 8) and the sorted
+// (0: about three items per SM), `pw` producer warps (4, 8 or 12) and the sorted
 // collide order when sort; or off (rows 0)
 int set_march(Lattice* L, int rows, int planes, int pw, int sort)
 {
@@ -590,7 +590,8 @@ int set_march(Lattice* L, int rows, int planes, int pw, int sort)
     return PS_OK;
   }
   if (L->prec == 0) return fail(PS_ERR_ARG, "ps_lbm_set_march: FP64 storage has no marching step");
-  if (pw != 4 && pw != 8) return fail(PS_ERR_ARG, "ps_lbm_set_march: producer warps must be 4 or 8, not %d", pw);
+  if (pw != 4 && pw != 8 && pw != 12)
+    return fail(PS_ERR_ARG, "ps_lbm_set_march: producer warps must be 4, 8 or 12, not %d", pw);
   rows = std::min(rows, L->ny);
   const int res = PREC_DISPATCH(lbm_march_resident, L->prec, pw, rows, L->nx);
   if (res < 1) return fail(PS_ERR_ARG, "ps_lbm_set_march: a ring of %d rows x %d does not fit one CTA", rows, L->nx);
@@ -604,7 +605,7 @@ int set_march(Lattice* L, int rows, int planes, int pw, int sort)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int nband = (L->ny + rows - 1) / rows;
-    const int nchunk = std::max(1, std::min(L->nz, 2 * sms / nband));
+    const int nchunk = std::max(1, std::min(L->nz, 3 * sms / nband));
     planes = (L->nz + nchunk - 1) / nchunk;
   }
   L->march_req = req;
@@ -1446,7 +1447,8 @@ int ps_lbm_autotune(void* h, int32_t steps, int32_t* tx_out, int32_t* ty_out, in
       {128, 256, 7, 0, 1, 64, 0},
       // marching steps (band rows, producer warps, sorted collide order)
       {128, 256, 6, 0, 1, 0, 0, 4, 4, 1}, {128, 256, 6, 0, 1, 0, 0, 8, 4, 1}, {128, 256, 6, 0, 1, 0, 0, 16, 4, 1},
-      {128, 256, 6, 0, 1, 0, 0, 8, 8, 1}, {128, 256, 6, 0, 1, 0, 0, 16, 8, 1}};
+      {128, 256, 6, 0, 1, 0, 0, 8, 8, 1}, {128, 256, 6, 0, 1, 0, 0, 16, 8, 1}, {128, 256, 6, 0, 1, 0, 0, 8, 12, 1},
+      {128, 256, 6, 0, 1, 0, 0, 16, 12, 1}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -992,7 +992,8 @@ __global__ void __launch_bounds__(32 * (PW + CW), 1)
         const int b0 = __ldg(G.rowstart + rb + y0), nb = __ldg(G.rowstart + rb + y0 + nr) - b0;
         const int c0 = __ldg(G.rowstart + rb + yhi), nc = __ldg(G.rowstart + rb + yhi + 1) - c0;
         uint16_t* ord = order + s * maxb;
-        for (int k = tid; k < na + nb + nc; k += NP) {
+        const int ntot = na + nb + nc;
+        auto one = [&](int k) {
           const bool lo = k < na, hi = k >= na + nb;
           const int i = lo ? a0 + k : (hi ? c0 + (k - na - nb) : b0 + (k - na));
           uint32_t cw;
@@ -1007,7 +1008,14 @@ __global__ void __launch_bounds__(32 * (PW + CW), 1)
             else if (iface) ord[nb - 1 - atomicAdd(cnt + 2 * s + 1, 1)] = (uint16_t)j;
             else ord[atomicAdd(cnt + 2 * s, 1)] = (uint16_t)j;
           }
+        };
+        // two nodes per pass, so that the loads of both are in flight together
+        int k = tid;
+        for (; k + NP < ntot; k += 2 * NP) {
+          one(k);
+          one(k + NP);
         }
+        if (k < ntot) one(k);
         mbar_arrive(full + s);
       }
     } else {

@@ -305,12 +305,14 @@ cudaError_t wall_load(const LbmLaunchArgs& a, double fq1, double fq2, double ppp
   {                                                                                                        \
     if (pw == 4) return detail::step_march_blk<P, 4, 20>(a, A);                                            \
     if (pw == 8) return detail::step_march_blk<P, 8, 16>(a, A);                                            \
+    if (pw == 12) return detail::step_march_blk<P, 12, 12>(a, A);                                          \
     return cudaErrorInvalidValue;                                                                          \
   }                                                                                                        \
   int lbm_march_resident_##P(int pw, int rows, int nx)                                                    \
   {                                                                                                        \
     if (pw == 4) return detail::march_resident<P, 4, 20>(rows, nx);                                        \
     if (pw == 8) return detail::march_resident<P, 8, 16>(rows, nx);                                        \
+    if (pw == 12) return detail::march_resident<P, 12, 12>(rows, nx);                                      \
     return 0;                                                                                              \
   }                                                                                                        \
   cudaError_t lbm_fields_launch_##P(const LbmLaunchArgs& a, double* rr, double* rb, double* cf, double* cc) \

@@ -131,7 +131,8 @@ class Lattice:
 
     def set_march(self, rows: int, planes: int = 0, producers: int = 4, sort: bool = True) -> None:
         """Marching one-launch step over items of `rows` y-rows and `planes`
-        z-planes (0: about two per SM), `producers` density warps per CTA,
+        z-planes (0: about three per SM), `producers` density warps per CTA
+        (4, 8 or 12),
         bulk nodes collided before interface nodes when sort; rows 0 turns
         it off."""
         check(self._lib.ps_lbm_set_march(self._h, rows, planes, producers, int(bool(sort))))

@@ -349,7 +349,8 @@ def test_fused_wait_gives_up_and_recovers(gpu):
 
 @pytest.mark.parametrize("prec", [1, 2, 3])
 @pytest.mark.parametrize("rows,planes,producers,sort", [(4, 0, 4, True), (1, 1, 4, True), (5, 7, 8, True),
-                                                        (18, 3, 4, False), (64, 64, 8, True), (3, 2, 4, True)])
+                                                        (18, 3, 4, False), (64, 64, 8, True), (3, 2, 4, True),
+                                                        (6, 5, 12, True)])
 def test_march_schedule_matches_two_pass(gpu, prec, rows, planes, producers, sort):
     """The marching one-launch step (items of `rows` rows by `planes`
     planes walked by producer and consumer warps, halo rows recomputed)
