@@ -214,30 +214,33 @@ __device__ __forceinline__ uint32_t step_of(const BufDev& b)
 // (a, b) to a 16-bit pair, stochastically rounded with the random bits r
 template <typename T2>
 __device__ __forceinline__ T2 from_f2_sr(float a, float b, uint32_t r);
-// x dithered for a conversion to FP16 by rounding toward zero, with 13
-// random bits r: in FP16's normal range the random integer goes below the
-// 13 mantissa bits the conversion drops; below 2^-14, where FP16's grid is
-// 2^-24 whatever the exponent (subnormals), x is rounded stochastically on
-// that grid directly, so that tiny values are not pulled toward zero (a
-// real branch: it is rare)
-static __device__ __noinline__ float dither_f16_sub(float x, uint32_t r)
+// x stochastically rounded onto FP16's subnormal grid 2^-24 (|x| < 2^-14)
+// with 13 random bits r; the result converts exactly
+__device__ __forceinline__ float sr_f16_sub(float x, uint32_t r)
 {
   const float q = x * 16777216.0f;  // x / 2^-24, exact
   const float fl = floorf(q);
   const float u = (float)r * (1.0f / 8192.0f);  // uniform in [0, 1)
-  return (fl + (q - fl > u ? 1.0f : 0.0f)) * 5.9604644775390625e-08f;  // on the grid: converts exactly
-}
-__device__ __forceinline__ float dither_f16(float x, uint32_t r)
-{
-  if (__builtin_expect(fabsf(x) < 6.103515625e-05f, 0)) return dither_f16_sub(x, r);
-  return __uint_as_float(__float_as_uint(x) + r);
+  return (fl + (q - fl > u ? 1.0f : 0.0f)) * 5.9604644775390625e-08f;
 }
 template <>
 __device__ __forceinline__ __half2 from_f2_sr<__half2>(float a, float b, uint32_t r)
 {
-  // FP16 keeps 10 of FP32's 23 mantissa bits: 13 random bits each
-  const float ad = dither_f16(a, r & 0x1FFFu);
-  const float bd = dither_f16(b, (r >> 16) & 0x1FFFu);
+  // FP16 keeps 10 of FP32's 23 mantissa bits: 13 random bits each, added
+  // below the bits the round-toward-zero conversion drops.  Below 2^-14
+  // FP16's grid is 2^-24 whatever the exponent (subnormals) and that dither
+  // would cover only part of the dropped bits, pulling tiny values toward
+  // zero (the minority component's populations at an interface, which
+  // matter): those are rounded on the grid directly.  They are rare, so the
+  // warp takes that path only when one of its lanes needs it.
+  const uint32_t ra = r & 0x1FFFu, rb = (r >> 16) & 0x1FFFu;
+  float ad = __uint_as_float(__float_as_uint(a) + ra);
+  float bd = __uint_as_float(__float_as_uint(b) + rb);
+  const bool sub = fminf(fabsf(a), fabsf(b)) < 6.103515625e-05f;
+  if (__any_sync(__activemask(), sub)) {
+    if (fabsf(a) < 6.103515625e-05f) ad = sr_f16_sub(a, ra);
+    if (fabsf(b) < 6.103515625e-05f) bd = sr_f16_sub(b, rb);
+  }
   uint32_t h;
   asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(bd), "f"(ad));
   return *reinterpret_cast<__half2*>(&h);
