@@ -72,7 +72,7 @@ struct Springs {
   LsmGeom geom() const
   {
     return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_K32, d_S64, {(float)p.alf1, (float)p.alf2},
-                   {(float)p.bet1, (float)p.bet2}};
+                   {(float)p.bet1, (float)p.bet2}, {p.alf1, p.alf2}, {p.bet1, p.bet2}};
   }
 };
 
@@ -297,8 +297,8 @@ int cg(Springs* S, T* x, T* r, T* p, T* q, double tol, long long maxit, long lon
 int residual(Springs* S, double* rnorm2)
 {
   const int n3 = 3 * S->nvox;
-  const int nb = blocks_for(S->nvox), nb3 = blocks_for(n3);
-  lsm::k_lsm_matvec<double, kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
+  const int nb3 = blocks_for(n3);
+  lsm::k_lsm_matvec<double, kBlk><<<mv_tiles(S->nvox), kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
   k_axpy_res<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->q64, S->r, S->part);
   PS_CUDA(cudaGetLastError());
   if (int e = project_mean(S, S->r)) return e;
@@ -734,6 +734,22 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
       }
   S->nnode = nn;
   S->ncube = nc;
+  // node classes on the device (lsm_kernels.cuh): 1 surface node, 2 / 3
+  // bulk node of material 1 / 2 (its 8 cubes all of that material)
+  std::vector<uint8_t> cls(S->node);
+  for (int z = 0; z < nz; z++)
+    for (int y = 0; y < ny; y++)
+      for (int x = 0; x < nx; x++) {
+        const int v = x + nx * (y + ny * z);
+        if (!cls[v]) continue;
+        const int m = S->mat[v];
+        bool bulk = m != 0;
+        for (int e = 1; e < 8 && bulk; e++) {
+          const int cx = (x - (e & 1) + nx) % nx, cy = (y - ((e >> 1) & 1) + ny) % ny, cz = (z - (e >> 2) + nz) % nz;
+          bulk = S->mat[cx + nx * (cy + ny * cz)] == m;
+        }
+        if (bulk) cls[v] = (uint8_t)(1 + m);
+      }
   // cube matrices, per material
   static const lsm::CubeMatrices M = [] {  // built once, thread-safe
     lsm::CubeMatrices m;
@@ -762,7 +778,7 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   if (int r = dalloc(S.get(), &S->d_mat, nv)) return r;
   if (int r = dalloc(S.get(), &S->d_node, nv)) return r;
   PS_CUDA(cudaMemcpyAsync(S->d_mat, S->mat.data(), nv, cudaMemcpyHostToDevice, S->stream));
-  PS_CUDA(cudaMemcpyAsync(S->d_node, S->node.data(), nv, cudaMemcpyHostToDevice, S->stream));
+  PS_CUDA(cudaMemcpyAsync(S->d_node, cls.data(), nv, cudaMemcpyHostToDevice, S->stream));
   const size_t b64 = sizeof(double) * 3 * (size_t)nv, b32 = sizeof(float) * 3 * (size_t)nv;
   for (double** v : {&S->b, &S->x, &S->r, &S->p64, &S->q64})
     if (int r = dalloc(S.get(), v, b64)) return r;
@@ -1152,12 +1168,12 @@ int ps_lsm_dyn_step(void* h, int32_t nsteps, double dt, double rsi, double damp)
   Springs* S = static_cast<Springs*>(h);
   if (int e = ensure_dyn(S)) return e;
   const int nv = S->nvox, n3 = 3 * nv;
-  const int nb = blocks_for(nv), nb3 = blocks_for(n3);
+  const int nb3 = blocks_for(n3);
   const double* f = S->has_load ? S->fext : nullptr;
   const double* bj = S->p.gstrain != 0.0 ? S->bj : nullptr;
   for (int s = 0; s < nsteps; s++) {
     lsm::k_dyn_kick_drift<<<nb3, kBlk, 0, S->stream>>>(n3, dt, f, S->x, S->dv, S->da);
-    lsm::k_lsm_matvec<double, kBlk><<<nb, kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
+    lsm::k_lsm_matvec<double, kBlk><<<mv_tiles(nv), kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
     lsm::k_dyn_force_kick<<<nb3, kBlk, 0, S->stream>>>(n3, dt, rsi, damp, bj, S->q64, f, S->dv, S->da);
   }
   PS_CUDA(cudaGetLastError());

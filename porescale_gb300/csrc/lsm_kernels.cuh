@@ -9,6 +9,15 @@
 // rows of its corner from the (at most 8) solid cubes around it; nodes
 // outside the solid return 0.  Nothing is scattered, so the product is
 // deterministic and needs no atomics.
+//
+// node[v] classifies the node: 0 no node, 1 a node on a pore surface or a
+// material interface, 2 / 3 a bulk node (all 8 cubes of material 1 / 2).
+// A bulk node's row is the fixed 27-point stencil alpha kBulkKa + beta
+// kBulkKb, applied to the neighbours' differences from the node in +-d
+// pairs (about 100 operations); the other nodes take the per-cube gather
+// (about 650 in FP32).  Each CTA does its bulk nodes first and then its
+// listed surface nodes on all its threads, so that the costly path runs on
+// full warps.
 #pragma once
 #include <stdint.h>
 
@@ -25,7 +34,29 @@ struct LsmGeom {
   const float* K32;
   const double* S64;    // per-material cube stress rows [2][9][24]
   float alf[2], bet[2];  // spring constants of the two materials (FP32 matvec)
+  double alfd[2], betd[2];  // the same in FP64 (FP64 bulk stencil)
 };
+
+// the bulk stencil's properties that bulk_node relies on: the block of
+// offset d equals that of -d, and every row sums to zero (a rigid
+// translation feels no force), so that row r of K p is
+// sum over the 13 pairs of S_d (p_{v+d} + p_{v-d} - 2 p_v)
+constexpr bool bulk_stencil_ok()
+{
+  for (int d = 0; d < 27; d++)
+    for (int j = 0; j < 9; j++)
+      if (kBulkKa[d][j] != kBulkKa[26 - d][j] || kBulkKb[d][j] != kBulkKb[26 - d][j]) return false;
+  for (int j = 0; j < 9; j++) {
+    double a = 0.0, b = 0.0;
+    for (int d = 0; d < 27; d++) {
+      a += kBulkKa[d][j];
+      b += kBulkKb[d][j];
+    }
+    if (a != 0.0 || b != 0.0) return false;
+  }
+  return true;
+}
+static_assert(bulk_stencil_ok(), "bulk stencil must be symmetric in d and have zero row sums");
 
 // the generated cube matrices in device-readable form; every read below
 // has indices fixed by full unrolling, so it folds to a literal and the
@@ -50,6 +81,17 @@ __device__ const double kKb[24][24] = {
     PS_ROW(16), PS_ROW(17), PS_ROW(18), PS_ROW(19), PS_ROW(20), PS_ROW(21), PS_ROW(22), PS_ROW(23)
 #undef PS_ROW
 };
+
+// the bulk stencil in device-readable form (indices fixed by unrolling, as above)
+#define PS_ROW(t, d) {t[d][0], t[d][1], t[d][2], t[d][3], t[d][4], t[d][5], t[d][6], t[d][7], t[d][8]}
+#define PS_TAB(t) {PS_ROW(t, 0), PS_ROW(t, 1), PS_ROW(t, 2), PS_ROW(t, 3), PS_ROW(t, 4), PS_ROW(t, 5), \
+    PS_ROW(t, 6), PS_ROW(t, 7), PS_ROW(t, 8), PS_ROW(t, 9), PS_ROW(t, 10), PS_ROW(t, 11), PS_ROW(t, 12), \
+    PS_ROW(t, 13), PS_ROW(t, 14), PS_ROW(t, 15), PS_ROW(t, 16), PS_ROW(t, 17), PS_ROW(t, 18), PS_ROW(t, 19), \
+    PS_ROW(t, 20), PS_ROW(t, 21), PS_ROW(t, 22), PS_ROW(t, 23), PS_ROW(t, 24), PS_ROW(t, 25), PS_ROW(t, 26)}
+__device__ const double kBKa[27][9] = PS_TAB(kBulkKa);
+__device__ const double kBKb[27][9] = PS_TAB(kBulkKb);
+#undef PS_TAB
+#undef PS_ROW
 
 template <typename T>
 __device__ __forceinline__ T kval(const LsmGeom& G, int m, int r, int c);
@@ -134,6 +176,103 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
   }
   return pq;
 }
+// (A p) at a bulk node v of material index mi (0, 1), written to q; returns
+// p_v . (A p)_v.  Every node of the 26 around v exists (its cubes are solid).
+template <typename T>
+__device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v, int mi)
+{
+  const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
+  const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+  const int xs[3] = {wrap_add(x, -1, nx), x, wrap_add(x, 1, nx)};
+  const int ys[3] = {wrap_add(y, -1, ny), y, wrap_add(y, 1, ny)};
+  const int zs[3] = {wrap_add(z, -1, nz), z, wrap_add(z, 1, nz)};
+  T al, be;
+  if constexpr (sizeof(T) == 4) {
+    al = mi ? G.alf[1] : G.alf[0];
+    be = mi ? G.bet[1] : G.bet[0];
+  } else {
+    al = mi ? G.alfd[1] : G.alfd[0];
+    be = mi ? G.betd[1] : G.betd[0];
+  }
+  const T u0[3] = {p[v], p[nv + v], p[2 * nv + v]};
+  T acc[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int d = 0; d < 13; d++) {  // offset d and its mirror 26 - d
+    const int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
+    bool used[3] = {false, false, false};
+#pragma unroll
+    for (int j = 0; j < 9; j++)
+      if (kBKa[d][j] != 0.0 || kBKb[d][j] != 0.0) used[j % 3] = true;
+    if (!(used[0] || used[1] || used[2])) continue;
+    const int vp = xs[1 + dx] + nx * (ys[1 + dy] + ny * zs[1 + dz]);
+    const int vm = xs[1 - dx] + nx * (ys[1 - dy] + ny * zs[1 - dz]);
+    T s[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      if (used[c]) s[c] = (p[c * nv + vp] + p[c * nv + vm]) - T(2) * u0[c];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double ka = kBKa[d][3 * r + c], kb = kBKb[d][3 * r + c];
+        if (ka == 0.0 && kb == 0.0) continue;
+        T k;
+        if (ka == 0.0) k = be * T(kb);
+        else if (kb == 0.0) k = al * T(ka);
+        else k = al * T(ka) + be * T(kb);
+        acc[r] += k * s[c];
+      }
+  }
+  q[v] = acc[0];
+  q[nv + v] = acc[1];
+  q[2 * nv + v] = acc[2];
+  return (double)(u0[0] * acc[0] + u0[1] * acc[1] + u0[2] * acc[2]);
+}
+
+// q = A p over the kMvPer * BLK nodes from v0 on (one CTA); returns this
+// thread's part of p.q.  Bulk nodes and non-nodes are done in place; the
+// surface nodes are listed (in node order, so the work of every thread is
+// fixed by the geometry and the sums are reproducible) and then shared
+// out over all threads.
+constexpr int kMvPer = 4;  // nodes per thread and tile
+template <typename T, int BLK>
+__device__ __forceinline__ double mv_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v0)
+{
+  __shared__ int list[kMvPer * BLK];
+  __shared__ int wcount[BLK / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nv = G.nvox;
+  const int v1 = min(v0 + kMvPer * BLK, nv);
+  double pq = 0.0;
+  int base = 0;
+#pragma unroll 1
+  for (int k = 0; k < kMvPer; k++) {
+    const int v = v0 + k * BLK + (int)threadIdx.x;
+    const int cls = v < v1 ? G.node[v] : -1;
+    if (cls >= 2) {
+      pq += bulk_node<T>(G, p, q, v, cls - 2);
+    } else if (cls == 0) {
+      q[v] = T(0);
+      q[nv + v] = T(0);
+      q[2 * nv + v] = T(0);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, cls == 1);
+    if (lane == 0) wcount[warp] = __popc(bal);
+    __syncthreads();
+    int off = base, tot = base;
+#pragma unroll
+    for (int w = 0; w < BLK / 32; w++) {
+      const int c = wcount[w];
+      off += w < warp ? c : 0;
+      tot += c;
+    }
+    if (cls == 1) list[off + __popc(bal & ((1u << lane) - 1u))] = v;
+    base = tot;
+    __syncthreads();
+  }
+  for (int i = (int)threadIdx.x; i < base; i += BLK) pq += matvec_node<T>(G, p, q, list[i]);
+  return pq;
+}
+
 // CG direction update p' = r + beta p (one expression for every caller)
 template <typename T>
 __device__ __forceinline__ T next_dir(T r, T beta, T p)
@@ -158,12 +297,12 @@ __device__ __forceinline__ void block_sum_to(double t, double* out)
 
 // q = A p on every node, with the FP64 partial sums of p.q per block
 // (dot[blockIdx]).  T = storage / arithmetic type of p and q.
+// (one CTA per tile of kMvPer * BLK nodes)
 template <typename T, int BLK>
 __global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __restrict__ p, T* __restrict__ q,
                                                     double* __restrict__ dot)
 {
-  const int v = blockIdx.x * BLK + threadIdx.x;
-  const double pq = v < G.nvox ? matvec_node<T>(G, p, q, v) : 0.0;
+  const double pq = mv_tile<T, BLK>(G, p, q, blockIdx.x * kMvPer * BLK);
   block_sum_to<BLK>(pq, dot + blockIdx.x);
 }
 
@@ -441,15 +580,12 @@ __device__ __forceinline__ void cg_beta_fin(double* scal, double rn)
 // striding by BLK): few CTAs, so few partials and counter updates per
 // reduction.  The batched kernels use the same tiles, so a network sums in
 // the same order either way.
-constexpr int kMvPer = 1, kVecPer = 8;  // nodes / elements per thread
+constexpr int kVecPer = 8;  // elements per thread (node tiles: kMvPer)
 
 template <typename T, int BLK>
 __device__ __forceinline__ double cg_mv_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v0)
 {
-  double pq = 0.0;
-  const int v1 = min(v0 + kMvPer * BLK, G.nvox);
-  for (int v = v0 + (int)threadIdx.x; v < v1; v += BLK) pq += matvec_node<T>(G, p, q, v);
-  return pq;
+  return mv_tile<T, BLK>(G, p, q, v0);
 }
 template <typename T, int BLK>
 __device__ __forceinline__ double cg_xr_tile(int n3, T al, T* __restrict__ x, T* __restrict__ r,

@@ -31,7 +31,7 @@ def _params():
 def _s1_corners(ind):
     """(x, y, z) of the coupled driver's LSM nodes in their number order
     (corner dilation with periodic wrap, k-j-i, S1:541-602)."""
-    solid = ind == 0
+    solid = (ind == 0) | (ind == 3)
     nz, ny, nx = ind.shape
     out = []
     for k in range(nz):
@@ -125,6 +125,43 @@ def test_periodic_network_in_s1_order(gpu, oracle_lib):
     want = osp.dyn_state()
     for g, w in zip(got, want):
         assert _close(g, w[idx], 1e-11)
+
+
+@pytest.mark.parametrize("case", ["two-solid", "pore-space"])
+def test_spring_forces_of_a_random_state(gpu, oracle_lib, case):
+    """One undamped step (dt 1) from rest at a random displacement, with no
+    load, leaves r in place and sets a = F(r) (and v = a / 2, the closing
+    half kick): the operator's bulk stencil (nodes
+    whose 8 cubes share one material) and its per-cube gather (surface and
+    interface nodes) against the oracle's bond and angle loops, at 1e-12 of
+    the largest force.  The periodic network is compared through the
+    oracle's tied layout (a duplicate-plane node carries its partner's
+    displacement, and the tied forces are the periodic ones)."""
+    if case == "two-solid":
+        ind = geo.inclusions((10, 12, 14), 0.3, 2.5, seed=3)
+        consts = (1.0, 0.4, 0.3, 0.1)
+    else:
+        ind = geo.sphere_pack(SHAPE, 0.45, 3.0, seed=7)
+        consts = (0.8, 0.3, 0.8, 0.3)
+    osp = oracle_lib.OracleSprings(ind, *consts, 0.0, LOAD_XSTRETCH)
+    idx = _oracle_index(osp, ind, 0)
+    ns = len(idx)
+    r = np.random.default_rng(11).standard_normal((ns, 3))
+    with SpringNetwork(ind, *consts, 0.0, LOAD_NONE, LSM_F64) as S:
+        S.set_dyn_state(r)
+        S.dyn_step(1, 1.0, 1.0, 0.0)
+        got_r, got_v, got_a = S.dyn_state(ns)
+    assert np.array_equal(got_r, r) and np.array_equal(got_v, 0.5 * got_a)
+    icors = osp.tables()[0]
+    where = {tuple(c): n for n, c in enumerate(icors)}
+    u = np.zeros((osp.ns, 3))
+    u[idx] = r
+    nx = ind.shape[2]
+    for n, c in enumerate(icors):
+        if c[0] == nx + 1 and (1, c[1], c[2]) in where:
+            u[n] = u[where[(1, c[1], c[2])]]
+    want = osp.forces(u)[idx]
+    assert _close(got_a, want, 1e-12)
 
 
 @pytest.mark.parametrize("load", [LOAD_XSTRETCH, LOAD_YZSHEAR])
