@@ -15,7 +15,9 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -33,6 +35,7 @@ namespace {
 using lsm::LsmGeom;
 
 constexpr int kBlk = 256;
+constexpr int kBatchStreams = 2;  // concurrent batches of ps_lsm_batch_solve (mixed precision)
 
 // A captured batch of CG iterations (CUDA graph) for one vector set
 struct CgGraph {
@@ -49,6 +52,8 @@ struct Springs {
   std::vector<uint8_t> mat, node;
   cudaStream_t stream = nullptr;
   uint8_t *d_mat = nullptr, *d_node = nullptr;
+  int* d_surf = nullptr;  // surface nodes (node class 1) in node order
+  int nsurf = 0;
   double *d_K64 = nullptr, *d_S64 = nullptr;  // per-material cube matrices of this handle
   double* d_Kab = nullptr;                      // material-independent Ka, Kb (modulus gradients)
   double* fext = nullptr;                       // external nodal load [3][nvox] (fluid wall load)
@@ -72,7 +77,7 @@ struct Springs {
   LsmGeom geom() const
   {
     return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_K32, d_S64, {(float)p.alf1, (float)p.alf2},
-                   {(float)p.bet1, (float)p.bet2}, {p.alf1, p.alf2}, {p.bet1, p.bet2}};
+                   {(float)p.bet1, (float)p.bet2}, {p.alf1, p.alf2}, {p.bet1, p.bet2}, d_surf, nsurf};
   }
 };
 
@@ -81,6 +86,7 @@ void free_springs(Springs* S)
   if (!S) return;
   cudaFree(S->d_mat);
   cudaFree(S->d_node);
+  cudaFree(S->d_surf);
   cudaFree(S->d_K64);
   cudaFree(S->d_K32);
   cudaFree(S->d_S64);
@@ -210,11 +216,24 @@ __global__ void k_set_scal(double* scal, double rr, double bb)
 }
 
 int blocks_for(long long n) { return (int)((n + kBlk - 1) / kBlk); }
-// CTAs of the CG kernels: one per tile of kMvPer (kVecPer) elements per thread
+// CTAs of the CG kernels: one per tile of kMvPer nodes (bulk), kSfPer
+// surface nodes (at least one CTA, whose last CTA ends the p.q sum) or
+// kVecPer elements per thread
 int mv_tiles(long long n) { return (int)((n + lsm::kMvPer * kBlk - 1) / (lsm::kMvPer * kBlk)); }
+int sf_tiles(long long n) { return std::max(1, (int)((n + lsm::kSfPer * kBlk - 1) / (lsm::kSfPer * kBlk))); }
 int vec_tiles(long long n) { return (int)((n + lsm::kVecPer * kBlk - 1) / (lsm::kVecPer * kBlk)); }
 
 // ---- host-side solve ---------------------------------------------------------
+// q = A u in FP64 (bulk then surface kernel; their p.q partials in part[])
+int matvec64(Springs* S, const double* u, double* q)
+{
+  const int tm = mv_tiles(S->nvox);
+  lsm::k_lsm_matvec<double, kBlk><<<tm, kBlk, 0, S->stream>>>(S->geom(), u, q, S->part);
+  lsm::k_lsm_matvec_surf<double, kBlk><<<sf_tiles(S->nsurf), kBlk, 0, S->stream>>>(S->geom(), u, q, S->part + tm);
+  PS_CUDA(cudaGetLastError());
+  return PS_OK;
+}
+
 int sum_parts(Springs* S, int n, double* d_out)
 {
   lsm::k_sum<<<1, 1024, 0, S->stream>>>(S->part, n, d_out);
@@ -268,9 +287,10 @@ int cg(Springs* S, T* x, T* r, T* p, T* q, double tol, long long maxit, long lon
     cgg.exec = nullptr;
     cudaGraph_t graph = nullptr;
     PS_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
-    const int tm = mv_tiles(S->nvox), tv = vec_tiles(n3);
+    const int tm = mv_tiles(S->nvox), ts = sf_tiles(S->nsurf), tv = vec_tiles(n3);
     for (int k = 0; k < batch; k++) {
-      lsm::k_cg_mv<T, kBlk><<<tm, kBlk, 0, S->stream>>>(G, S->scal, p, q, S->part, S->ctr, tol2);
+      lsm::k_cg_mv<T, kBlk><<<tm, kBlk, 0, S->stream>>>(G, S->scal, p, q, S->part);
+      lsm::k_cg_mv_surf<T, kBlk><<<ts, kBlk, 0, S->stream>>>(G, S->scal, p, q, S->part, tm, S->ctr, tol2);
       lsm::k_cg_xr<T, kBlk><<<tv, kBlk, 0, S->stream>>>(n3, S->scal, x, r, p, q, S->part, S->ctr);
       lsm::k_cg_p<T, kBlk><<<tv, kBlk, 0, S->stream>>>(n3, S->scal, r, p);
     }
@@ -298,7 +318,7 @@ int residual(Springs* S, double* rnorm2)
 {
   const int n3 = 3 * S->nvox;
   const int nb3 = blocks_for(n3);
-  lsm::k_lsm_matvec<double, kBlk><<<mv_tiles(S->nvox), kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
+  if (int e = matvec64(S, S->x, S->q64)) return e;
   k_axpy_res<<<nb3, kBlk, 0, S->stream>>>(n3, S->b, S->q64, S->r, S->part);
   PS_CUDA(cudaGetLastError());
   if (int e = project_mean(S, S->r)) return e;
@@ -511,6 +531,27 @@ int each_network(int n, F f)
   return err;
 }
 
+// The table's list of the networks a batched launch covers (in the given
+// order) and the first bulk / surface / element tile of each.
+void set_live(lsm::LsmTable& tab, const std::vector<int>& live)
+{
+  tab.nlive = (int)live.size();
+  int a = 0, b = 0, c = 0;
+  for (int k = 0; k < tab.nlive; k++) {
+    const lsm::LsmSys& d = tab.s[live[k]];
+    tab.live[k] = live[k];
+    tab.f1[k] = a;
+    tab.fs[k] = b;
+    tab.f3[k] = c;
+    a += d.nt1;
+    b += d.nts;
+    c += d.nt3;
+  }
+  tab.f1[tab.nlive] = a;
+  tab.fs[tab.nlive] = b;
+  tab.f3[tab.nlive] = c;
+}
+
 // ---- batched CG over several networks ---------------------------------------
 // CG on A x = r0 (x = 0, p = r0 set by the caller) for every network of the
 // list at once: the iteration of cg<T> with each kernel launched once for
@@ -527,7 +568,6 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
   lsm::LsmTable tab;
   memset(&tab, 0, sizeof tab);
   tab.n = n;
-  std::vector<int2> t1, t3;
   for (int s = 0; s < n; s++) {
     Springs* S = sys[s];
     lsm::LsmSys& d = tab.s[s];
@@ -548,20 +588,16 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
     d.ctr = S->ctr;
     d.n3 = 3 * S->nvox;
     d.nt1 = mv_tiles(S->nvox);
+    d.nts = sf_tiles(S->nsurf);
     d.nt3 = vec_tiles(d.n3);
-    t1.resize(t1.size() + d.nt1);
-    t3.resize(t3.size() + d.nt3);
     // |r0|^2 into scal[0] on the network's own stream
     lsm::k_sq_norm_t<T, kBlk><<<blocks_for(d.n3), kBlk, 0, S->stream>>>(d.n3, static_cast<const T*>(d.r), S->part);
     if (int e = sum_parts(S, blocks_for(d.n3), S->scal)) return e;
     PS_CUDA(cudaStreamSynchronize(S->stream));
   }
-  int2 *d1 = nullptr, *d3 = nullptr;
   double* ddone = nullptr;
   cudaGraphExec_t exec = nullptr;
   auto release = [&]() {
-    cudaFree(d1);
-    cudaFree(d3);
     cudaFree(ddone);
     if (exec) cudaGraphExecDestroy(exec);
   };
@@ -570,24 +606,20 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
   std::vector<double> done((size_t)n, 0.0);
   // tile lists of the networks not yet converged, and the graph over them
   auto rebuild = [&]() -> int {
-    t1.clear();
-    t3.clear();
-    for (int s = 0; s < n; s++) {
-      if (done[s] > 0.0) continue;
-      for (int b = 0; b < tab.s[s].nt1; b++) t1.push_back(make_int2(s, b * lsm::kMvPer * kBlk));
-      for (int b = 0; b < tab.s[s].nt3; b++) t3.push_back(make_int2(s, b * lsm::kVecPer * kBlk));
-    }
+    std::vector<int> live;
+    for (int s = 0; s < n; s++)
+      if (!(done[s] > 0.0)) live.push_back(s);
+    set_live(tab, live);
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
-    if (t1.empty()) return PS_OK;
-    PS_CUDA(cudaMemcpyAsync(d1, t1.data(), sizeof(int2) * t1.size(), cudaMemcpyHostToDevice, st));
-    PS_CUDA(cudaMemcpyAsync(d3, t3.data(), sizeof(int2) * t3.size(), cudaMemcpyHostToDevice, st));
+    if (live.empty()) return PS_OK;
     cudaGraph_t graph = nullptr;
     PS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < batch; k++) {
-      lsm::k_cg_mv_batch<T, kBlk><<<(unsigned)t1.size(), kBlk, 0, st>>>(tab, d1, tol2);
-      lsm::k_cg_xr_batch<T, kBlk><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
-      lsm::k_cg_p_batch<T, kBlk><<<(unsigned)t3.size(), kBlk, 0, st>>>(tab, d3);
+      lsm::k_cg_mv_batch<T, kBlk><<<(unsigned)tab.f1[tab.nlive], kBlk, 0, st>>>(tab);
+      lsm::k_cg_mv_surf_batch<T, kBlk><<<(unsigned)tab.fs[tab.nlive], kBlk, 0, st>>>(tab, tol2);
+      lsm::k_cg_xr_batch<T, kBlk><<<(unsigned)tab.f3[tab.nlive], kBlk, 0, st>>>(tab);
+      lsm::k_cg_p_batch<T, kBlk><<<(unsigned)tab.f3[tab.nlive], kBlk, 0, st>>>(tab);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
     if (ce != cudaSuccess) return cuda_fail(ce, "batched CG capture");
@@ -600,9 +632,7 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
     return PS_OK;
   };
   auto run = [&]() -> int {
-    PS_CUDA(cudaMalloc((void**)&d1, sizeof(int2) * t1.size()));
-    PS_CUDA(cudaMalloc((void**)&d3, sizeof(int2) * t3.size()));
-    PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * n));
+    PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * 2 * n));
     lsm::k_cg_init_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab);
     PS_CUDA(cudaGetLastError());
     if (int e = rebuild()) return e;
@@ -616,7 +646,7 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
       for (int s = 0; s < n; s++)
         if (!(now[s] > 0.0)) live += (size_t)tab.s[s].nt1;
       done = now;
-      if (live == 0 || 4 * live < 3 * t1.size())
+      if (live == 0 || 4 * live < 3 * (size_t)tab.f1[tab.nlive])
         if (int e = rebuild()) return e;
     }
     return PS_OK;
@@ -625,6 +655,235 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
   cudaStreamSynchronize(st);
   release();
   return r;
+}
+
+// ---- batched mixed-precision solve -------------------------------------------
+// ps_lsm_solve's FP64 refinement around FP32 CG for every network of the
+// list, the inner CGs advanced together by the batched kernels, with no
+// barrier between refinement rounds: a network whose inner CG has
+// converged (or spent its iteration budget) leaves the batch at the next
+// poll (every 16 iterations), is refined on a worker thread and its own
+// stream (x += |r| x32, the FP64 residual, the next inner system) while the
+// others keep iterating, and joins the batch again at the poll after that.
+// Each network does the arithmetic of ps_lsm_solve's loop in the same order
+// (same tiles, same scalars), so the results equal the individual solves'.
+// bb[s] = |b|^2; the per-network counts go to out[s].  nworkers host
+// threads do the refinement steps.
+int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb, double rtol, long long maxit,
+                ps_lsm_result* out, cudaStream_t st, int nworkers)
+{
+  const int n = (int)sys.size();
+  lsm::LsmTable tab;
+  memset(&tab, 0, sizeof tab);
+  tab.n = n;
+  for (int s = 0; s < n; s++) {
+    Springs* S = sys[s];
+    lsm::LsmSys& d = tab.s[s];
+    d.G = S->geom();
+    d.x = S->x32;
+    d.r = S->r32;
+    d.p = S->p32;
+    d.q = S->q32;
+    d.part = S->part;
+    d.scal = S->scal;
+    d.ctr = S->ctr;
+    d.n3 = 3 * S->nvox;
+    d.nt1 = mv_tiles(S->nvox);
+    d.nts = sf_tiles(S->nsurf);
+    d.nt3 = vec_tiles(d.n3);
+  }
+  std::vector<long long> budget((size_t)n, maxit);
+  std::vector<double> rn((size_t)n, 0.0);
+  std::vector<char> begun((size_t)n, 0);
+  // the step between two inner solves of network s; *next = true when
+  // another inner solve follows (its r32, p32, x32 and |r0|^2 in scal[0] set)
+  auto refine = [&](int s, bool* next) -> int {
+    Springs* S = sys[s];
+    const int n3 = 3 * S->nvox, nb3 = blocks_for(n3);
+    double rn2 = 0.0;
+    *next = false;
+    if (!begun[s]) {
+      begun[s] = 1;
+      PS_CUDA(cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream));
+      rn2 = bb[s];
+    } else {
+      double h8[8];
+      if (int e = read_scal(S, h8, 8)) return e;
+      const long long its = (long long)h8[7];
+      out[s].inner_iterations += its;
+      out[s].iterations++;
+      budget[s] -= its;
+      k_ir_update<<<nb3, kBlk, 0, S->stream>>>(n3, rn[s], S->x32, S->x);
+      PS_CUDA(cudaGetLastError());
+      if (int e = residual(S, &rn2)) return e;
+    }
+    if (!(bb[s] > 0.0) || rn2 <= rtol * rtol * bb[s] || budget[s] <= 0 || out[s].refinements >= 60) return PS_OK;
+    rn[s] = std::sqrt(rn2);
+    k_ir_start<<<nb3, kBlk, 0, S->stream>>>(n3, 1.0 / rn[s], S->r, S->r32, S->p32, S->x32);
+    lsm::k_sq_norm_t<float, kBlk><<<nb3, kBlk, 0, S->stream>>>(n3, S->r32, S->part);
+    if (int e = sum_parts(S, nb3, S->scal + 0)) return e;
+    PS_CUDA(cudaStreamSynchronize(S->stream));
+    out[s].refinements++;
+    *next = true;
+    return PS_OK;
+  };
+
+  // worker threads: refinement steps of the networks in `todo`; the
+  // networks with another inner solve go to `ready`
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<int> todo;
+  std::vector<int> ready;
+  int pending = n, err = PS_OK;
+  bool quit = false;
+  std::string msg;
+  for (int s = 0; s < n; s++) todo.push_back(s);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    for (;;) {
+      int s;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return quit || !todo.empty(); });
+        if (todo.empty()) return;
+        s = todo.front();
+        todo.pop_front();
+      }
+      bool next = false;
+      const int e = refine(s, &next);
+      {
+        std::lock_guard<std::mutex> g(mu);
+        if (e && !err) {
+          err = e;
+          msg = last_error();
+        }
+        if (!e && next) ready.push_back(s);
+        pending--;
+      }
+      cv.notify_all();
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 0; t < std::min(n, nworkers); t++) th.emplace_back(worker);
+
+  double* ddone = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<int> run;  // networks in the batch
+  const double tol2 = 1e-4 * 1e-4;
+  const int batch = 16;
+  // the captured iterations over the networks in `run`
+  auto rebuild = [&]() -> int {
+    set_live(tab, run);
+    if (run.empty()) {
+      if (exec) cudaGraphExecDestroy(exec);
+      exec = nullptr;
+      return PS_OK;
+    }
+    cudaGraph_t graph = nullptr;
+    PS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < batch; k++) {
+      lsm::k_cg_mv_batch<float, kBlk><<<(unsigned)tab.f1[tab.nlive], kBlk, 0, st>>>(tab);
+      lsm::k_cg_mv_surf_batch<float, kBlk><<<(unsigned)tab.fs[tab.nlive], kBlk, 0, st>>>(tab, tol2);
+      lsm::k_cg_xr_batch<float, kBlk><<<(unsigned)tab.f3[tab.nlive], kBlk, 0, st>>>(tab);
+      lsm::k_cg_p_batch<float, kBlk><<<(unsigned)tab.f3[tab.nlive], kBlk, 0, st>>>(tab);
+    }
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess) return cuda_fail(ce, "batched CG capture");
+    // the graphs differ only in grid sizes and the table's list: update the
+    // instantiated one in place (microseconds) rather than instantiating anew
+    cudaGraphExecUpdateResultInfo info;
+    if (exec && cudaGraphExecUpdate(exec, graph, &info) != cudaSuccess) {
+      cudaGetLastError();  // clear the failed update
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+    if (!exec) {
+      ce = cudaGraphInstantiate(&exec, graph, 0);
+      if (ce != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        exec = nullptr;
+        return cuda_fail(ce, "batched CG instantiate");
+      }
+    }
+    cudaGraphDestroy(graph);
+    return PS_OK;
+  };
+  auto drive = [&]() -> int {
+    PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * 2 * n));
+    std::vector<double> now((size_t)2 * n, 0.0);
+    for (;;) {
+      std::vector<int> admit;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        if (run.empty()) cv.wait(lk, [&] { return err || !ready.empty() || pending == 0; });
+        if (err) return PS_OK;  // the worker's error is returned below
+        admit.swap(ready);
+        if (run.empty() && admit.empty() && pending == 0) return PS_OK;
+      }
+      bool changed = false;
+      if (!admit.empty()) {
+        lsm::LsmList L{};
+        L.n = (int)admit.size();
+        for (int i = 0; i < L.n; i++) L.s[i] = admit[i];
+        lsm::k_cg_admit_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, L);
+        PS_CUDA(cudaGetLastError());
+        run.insert(run.end(), admit.begin(), admit.end());
+        std::sort(run.begin(), run.end());
+        changed = true;
+      }
+      size_t live = 0;
+      for (int s : run) live += (size_t)tab.s[s].nt1;
+      if (changed || 4 * live < 3 * (size_t)tab.f1[tab.nlive])
+        if (int e = rebuild()) return e;
+      if (!exec) continue;
+      PS_CUDA(cudaGraphLaunch(exec, st));
+      lsm::k_cg_done_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, ddone);
+      PS_CUDA(cudaMemcpyAsync(now.data(), ddone, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st));
+      PS_CUDA(cudaStreamSynchronize(st));
+      std::vector<int> stay, leave;
+      lsm::LsmList stop{};
+      for (int s : run) {
+        const bool conv = now[s] > 0.0, spent = (long long)now[n + s] >= budget[s];
+        if (!conv && spent) stop.s[stop.n++] = s;
+        (conv || spent ? leave : stay).push_back(s);
+      }
+      if (stop.n) {
+        lsm::k_cg_stop_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, stop);
+        PS_CUDA(cudaGetLastError());
+        PS_CUDA(cudaStreamSynchronize(st));
+      }
+      run.swap(stay);
+      if (!leave.empty()) {
+        {
+          std::lock_guard<std::mutex> g(mu);
+          for (int s : leave) todo.push_back(s);
+          pending += (int)leave.size();
+        }
+        cv.notify_all();
+      }
+    }
+  };
+  const int rc = drive();
+  {  // drop queued steps (none unless an error ended the loop); the
+     // workers finish the steps they are running and return
+    std::lock_guard<std::mutex> g(mu);
+    pending -= (int)todo.size();
+    todo.clear();
+    quit = true;
+  }
+  cv.notify_all();
+  for (std::thread& t : th) t.join();
+  cudaStreamSynchronize(st);
+  cudaFree(ddone);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (rc) return rc;
+  if (err) {
+    last_error() = msg;
+    return err;
+  }
+  return PS_OK;
 }
 
 // Calls f(k, v, dup) for the reference's nodes k = 0, 1, ... in their order:
@@ -750,6 +1009,10 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
         }
         if (bulk) cls[v] = (uint8_t)(1 + m);
       }
+  std::vector<int> surf;
+  for (int v = 0; v < nv; v++)
+    if (cls[v] == 1) surf.push_back(v);
+  S->nsurf = (int)surf.size();
   // cube matrices, per material
   static const lsm::CubeMatrices M = [] {  // built once, thread-safe
     lsm::CubeMatrices m;
@@ -779,6 +1042,9 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   if (int r = dalloc(S.get(), &S->d_node, nv)) return r;
   PS_CUDA(cudaMemcpyAsync(S->d_mat, S->mat.data(), nv, cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_node, cls.data(), nv, cudaMemcpyHostToDevice, S->stream));
+  if (int r = dalloc(S.get(), &S->d_surf, sizeof(int) * std::max<size_t>(1, surf.size()))) return r;
+  if (!surf.empty())
+    PS_CUDA(cudaMemcpyAsync(S->d_surf, surf.data(), sizeof(int) * surf.size(), cudaMemcpyHostToDevice, S->stream));
   const size_t b64 = sizeof(double) * 3 * (size_t)nv, b32 = sizeof(float) * 3 * (size_t)nv;
   for (double** v : {&S->b, &S->x, &S->r, &S->p64, &S->q64})
     if (int r = dalloc(S.get(), v, b64)) return r;
@@ -1027,66 +1293,53 @@ int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t max
       out[s].iterations = out[s].inner_iterations = (long long)h8[7];
     }
   } else {
-    // FP64 refinement rounds around one batched FP32 CG per round over the
-    // networks that have not reached rtol
-    std::vector<int> rounds((size_t)n, 0);
-    long long budget = maxit;
-    std::vector<double> rn((size_t)n, 0.0);
-    std::vector<long long> its((size_t)n, 0);
-    for (int round = 0; round < 60 && rc == PS_OK && budget > 0; round++) {
-      // residual of every network (first refinement pass: r = b); those above rtol start
-      // an FP32 inner solve on r / |r|
-      std::vector<char> on((size_t)n, 0);
-      rc = each_network(n, [&](int s) {
-        Springs* S = sys[s];
-        const int n3 = 3 * S->nvox;
-        double rn2 = 0.0;
-        if (round == 0) {
-          cudaError_t e = cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream);
-          if (e != cudaSuccess) return cuda_fail(e, "ps_lsm_batch_solve");
-          rn2 = bb[s];
-        } else if (int e = residual(S, &rn2)) {
-          return e;
-        }
-        if (!(bb[s] > 0.0) || rn2 <= rtol * rtol * bb[s]) return PS_OK;
-        rn[s] = std::sqrt(rn2);
-        k_ir_start<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, 1.0 / rn[s], S->r, S->r32, S->p32, S->x32);
-        cudaError_t e = cudaStreamSynchronize(S->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "ps_lsm_batch_solve");
-        on[s] = 1;
-        return PS_OK;
-      });
-      std::vector<Springs*> act;
-      std::vector<int> idx;
-      for (int s = 0; s < n; s++)
-        if (on[s]) {
-          act.push_back(sys[s]);
-          idx.push_back(s);
-          rounds[s]++;
-        }
-      if (rc != PS_OK || act.empty()) break;
-      if ((rc = batch_cg<float>(act, 1e-4, budget, st))) break;
-      // x64 += |r| x32 for every network of the round
-      rc = each_network((int)act.size(), [&](int a) {
-        Springs* S = act[a];
-        const int s = idx[a];
-        double h8[8];
-        if (int e = read_scal(S, h8, 8)) return e;
-        its[s] = (long long)h8[7];
-        const int n3 = 3 * S->nvox;
-        k_ir_update<<<blocks_for(n3), kBlk, 0, S->stream>>>(n3, rn[s], S->x32, S->x);
-        cudaError_t e = cudaStreamSynchronize(S->stream);
-        return e == cudaSuccess ? PS_OK : cuda_fail(e, "ps_lsm_batch_solve");
-      });
-      long long most = 0;
-      for (int s : idx) {
-        out[s].inner_iterations += its[s];
-        out[s].iterations++;
-        most = std::max(most, its[s]);
-      }
-      budget -= most;
+    // the networks in kBatchStreams groups of about equal node counts, each
+    // group a batch on its own stream and host thread: the groups' matvecs
+    // (arithmetic-bound) overlap the other groups' vector updates
+    // (bandwidth-bound) instead of alternating with them
+    const int ng = std::min(n, kBatchStreams);
+    std::vector<std::vector<int>> grp((size_t)ng);
+    std::vector<long long> load((size_t)ng, 0);
+    std::vector<int> order(n);
+    for (int s = 0; s < n; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a]->nnode > sys[b]->nnode; });
+    for (int s : order) {
+      const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      grp[g].push_back(s);
+      load[g] += sys[s]->nnode;
     }
-    for (int s = 0; s < n; s++) out[s].refinements = rounds[s];
+    std::vector<int> grc((size_t)ng, PS_OK);
+    std::vector<std::string> gmsg((size_t)ng);
+    std::vector<cudaStream_t> gst((size_t)ng, nullptr);
+    gst[0] = st;
+    for (int g = 1; g < ng; g++) PS_CUDA(cudaStreamCreateWithFlags(&gst[g], cudaStreamNonBlocking));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto run_group = [&](int g) {
+      cudaSetDevice(dev);
+      std::sort(grp[g].begin(), grp[g].end());
+      std::vector<Springs*> gs;
+      std::vector<double> gbb;
+      std::vector<ps_lsm_result> gout(grp[g].size());
+      for (int s : grp[g]) {
+        gs.push_back(sys[s]);
+        gbb.push_back(bb[s]);
+      }
+      for (size_t i = 0; i < gout.size(); i++) gout[i] = out[grp[g][i]];
+      grc[g] = batch_mixed(gs, gbb, rtol, maxit, gout.data(), gst[g], std::max(1, 8 / ng));
+      if (grc[g]) gmsg[g] = last_error();
+      for (size_t i = 0; i < gout.size(); i++) out[grp[g][i]] = gout[i];
+    };
+    std::vector<std::thread> gth;
+    for (int g = 1; g < ng; g++) gth.emplace_back(run_group, g);
+    run_group(0);
+    for (std::thread& t : gth) t.join();
+    for (int g = 1; g < ng; g++) cudaStreamDestroy(gst[g]);
+    for (int g = 0; g < ng && rc == PS_OK; g++)
+      if (grc[g]) {
+        rc = grc[g];
+        last_error() = gmsg[g];
+      }
   }
   cudaStreamDestroy(st);
   if (rc != PS_OK) return rc;
@@ -1173,7 +1426,7 @@ int ps_lsm_dyn_step(void* h, int32_t nsteps, double dt, double rsi, double damp)
   const double* bj = S->p.gstrain != 0.0 ? S->bj : nullptr;
   for (int s = 0; s < nsteps; s++) {
     lsm::k_dyn_kick_drift<<<nb3, kBlk, 0, S->stream>>>(n3, dt, f, S->x, S->dv, S->da);
-    lsm::k_lsm_matvec<double, kBlk><<<mv_tiles(nv), kBlk, 0, S->stream>>>(S->geom(), S->x, S->q64, S->part);
+    if (int e = matvec64(S, S->x, S->q64)) return e;
     lsm::k_dyn_force_kick<<<nb3, kBlk, 0, S->stream>>>(n3, dt, rsi, damp, bj, S->q64, f, S->dv, S->da);
   }
   PS_CUDA(cudaGetLastError());

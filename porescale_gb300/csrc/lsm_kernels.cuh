@@ -15,9 +15,10 @@
 // A bulk node's row is the fixed 27-point stencil alpha kBulkKa + beta
 // kBulkKb, applied to the neighbours' differences from the node in +-d
 // pairs (about 100 operations); the other nodes take the per-cube gather
-// (about 650 in FP32).  Each CTA does its bulk nodes first and then its
-// listed surface nodes on all its threads, so that the costly path runs on
-// full warps.
+// (about 650 in FP32).  The two kinds run as two kernels: one over the
+// node box for the bulk nodes (and the zero rows of non-nodes), one over
+// the list of surface nodes (surf[], in node order), so that the costly
+// path runs on full warps and the cheap one at its own occupancy.
 #pragma once
 #include <stdint.h>
 
@@ -35,6 +36,8 @@ struct LsmGeom {
   const double* S64;    // per-material cube stress rows [2][9][24]
   float alf[2], bet[2];  // spring constants of the two materials (FP32 matvec)
   double alfd[2], betd[2];  // the same in FP64 (FP64 bulk stencil)
+  const int* surf;  // the surface nodes (class 1) in node order
+  int nsurf;
 };
 
 // the bulk stencil's properties that bulk_node relies on: the block of
@@ -108,7 +111,10 @@ __device__ __forceinline__ float kval<float>(const LsmGeom& G, int m, int r, int
 
 __device__ __forceinline__ int wrap_add(int c, int d, int n) { return c + d < 0 ? c + d + n : (c + d >= n ? c + d - n : c + d); }
 
-// (A p) at node v, written to q; returns p_v . (A p)_v in FP64
+// (A p) at node v, written to q; returns p_v . (A p)_v in FP64.  p is
+// read through the read-only path (__ldg; q never aliases it), which the
+// batched kernels, whose vectors come from a table, need as much as the
+// single ones.
 template <typename T>
 __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v)
 {
@@ -117,7 +123,7 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
     const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
     const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
     T acc[3] = {T(0), T(0), T(0)};
-    if (G.node[v]) {
+    if (__ldg(G.node + v)) {
       const int xs[3] = {wrap_add(x, -1, nx), x, wrap_add(x, 1, nx)};
       const int ys[3] = {wrap_add(y, -1, ny), y, wrap_add(y, 1, ny)};
       const int zs[3] = {wrap_add(z, -1, nz), z, wrap_add(z, 1, nz)};
@@ -125,7 +131,7 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
       for (int e = 0; e < 8; e++) {  // cube with low corner at node - e; this node is its corner e
         const int ex = e & 1, ey = (e >> 1) & 1, ez = e >> 2;
         const int cv = xs[1 - ex] + nx * (ys[1 - ey] + ny * zs[1 - ez]);
-        const int m = G.mat[cv];
+        const int m = __ldg(G.mat + cv);
         if (m == 0) continue;
         if constexpr (sizeof(T) == 4) {
           // FP32: K = alf Ka + bet Kb with Ka, Kb literal (zeros skipped)
@@ -135,7 +141,7 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
             if (b == (e ^ 7)) continue;  // no spring couples opposite corners
             const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
             const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
-            const T u[3] = {p[nvb], p[nv + nvb], p[2 * nv + nvb]};
+            const T u[3] = {__ldg(p + nvb), __ldg(p + nv + nvb), __ldg(p + 2 * nv + nvb)};
 #pragma unroll
             for (int r = 0; r < 3; r++)
 #pragma unroll
@@ -154,7 +160,7 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
             if (b == (e ^ 7)) continue;  // no spring couples opposite corners
             const int bx = b & 1, by = (b >> 1) & 1, bz = b >> 2;
             const int nvb = xs[1 - ex + bx] + nx * (ys[1 - ey + by] + ny * zs[1 - ez + bz]);
-            const T u[3] = {p[nvb], p[nv + nvb], p[2 * nv + nvb]};
+            const T u[3] = {__ldg(p + nvb), __ldg(p + nv + nvb), __ldg(p + 2 * nv + nvb)};
             // FP64: the handle's K of material m; entries zero in both Ka
             // and Kb (known at compile time) are skipped
 #pragma unroll
@@ -168,7 +174,7 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
       }
       // the node's p.(Ap) in T (FP32: one conversion instead of three FP64
       // products on GB300's small FP64 pipe); sums across nodes stay FP64
-      pq = (double)(p[v] * acc[0] + p[nv + v] * acc[1] + p[2 * nv + v] * acc[2]);
+      pq = (double)(__ldg(p + v) * acc[0] + __ldg(p + nv + v) * acc[1] + __ldg(p + 2 * nv + v) * acc[2]);
     }
     q[v] = acc[0];
     q[nv + v] = acc[1];
@@ -179,10 +185,10 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
 // (A p) at a bulk node v of material index mi (0, 1), written to q; returns
 // p_v . (A p)_v.  Every node of the 26 around v exists (its cubes are solid).
 template <typename T>
-__device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v, int mi)
+__device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v, int x,
+                                            int y, int z, int mi)
 {
   const int nx = G.nx, ny = G.ny, nz = G.nz, nv = G.nvox;
-  const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
   const int xs[3] = {wrap_add(x, -1, nx), x, wrap_add(x, 1, nx)};
   const int ys[3] = {wrap_add(y, -1, ny), y, wrap_add(y, 1, ny)};
   const int zs[3] = {wrap_add(z, -1, nz), z, wrap_add(z, 1, nz)};
@@ -194,7 +200,7 @@ __device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restric
     al = mi ? G.alfd[1] : G.alfd[0];
     be = mi ? G.betd[1] : G.betd[0];
   }
-  const T u0[3] = {p[v], p[nv + v], p[2 * nv + v]};
+  const T u0[3] = {__ldg(p + v), __ldg(p + nv + v), __ldg(p + 2 * nv + v)};
   T acc[3] = {T(0), T(0), T(0)};
 #pragma unroll
   for (int d = 0; d < 13; d++) {  // offset d and its mirror 26 - d
@@ -209,7 +215,7 @@ __device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restric
     T s[3];
 #pragma unroll
     for (int c = 0; c < 3; c++)
-      if (used[c]) s[c] = (p[c * nv + vp] + p[c * nv + vm]) - T(2) * u0[c];
+      if (used[c]) s[c] = (__ldg(p + c * nv + vp) + __ldg(p + c * nv + vm)) - T(2) * u0[c];
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
@@ -229,47 +235,51 @@ __device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restric
   return (double)(u0[0] * acc[0] + u0[1] * acc[1] + u0[2] * acc[2]);
 }
 
-// q = A p over the kMvPer * BLK nodes from v0 on (one CTA); returns this
-// thread's part of p.q.  Bulk nodes and non-nodes are done in place; the
-// surface nodes are listed (in node order, so the work of every thread is
-// fixed by the geometry and the sums are reproducible) and then shared
-// out over all threads.
-constexpr int kMvPer = 4;  // nodes per thread and tile
+// q = A p on the bulk nodes and the non-nodes among the kMvPer * BLK nodes
+// from v0 on (one CTA; surface nodes are left to mv_surf_tile); returns
+// this thread's part of p.q.  The node coordinates advance by BLK nodes
+// per pass without a division.
+constexpr int kMvPer = 4;  // nodes per thread and bulk tile
+constexpr int kSfPer = 1;  // surface nodes per thread and surface tile
 template <typename T, int BLK>
-__device__ __forceinline__ double mv_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v0)
+__device__ __forceinline__ double mv_bulk_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v0)
 {
-  __shared__ int list[kMvPer * BLK];
-  __shared__ int wcount[BLK / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nv = G.nvox;
-  const int v1 = min(v0 + kMvPer * BLK, nv);
+  const int nv = G.nvox, nx = G.nx, ny = G.ny, v1 = min(v0 + kMvPer * BLK, nv);
   double pq = 0.0;
-  int base = 0;
+  int v = v0 + (int)threadIdx.x;
+  int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+  const int ax = BLK % nx, ay = BLK / nx;
 #pragma unroll 1
-  for (int k = 0; k < kMvPer; k++) {
-    const int v = v0 + k * BLK + (int)threadIdx.x;
-    const int cls = v < v1 ? G.node[v] : -1;
+  for (; v < v1; v += BLK) {
+    const int cls = __ldg(G.node + v);
     if (cls >= 2) {
-      pq += bulk_node<T>(G, p, q, v, cls - 2);
+      pq += bulk_node<T>(G, p, q, v, x, y, z, cls - 2);
     } else if (cls == 0) {
       q[v] = T(0);
       q[nv + v] = T(0);
       q[2 * nv + v] = T(0);
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, cls == 1);
-    if (lane == 0) wcount[warp] = __popc(bal);
-    __syncthreads();
-    int off = base, tot = base;
-#pragma unroll
-    for (int w = 0; w < BLK / 32; w++) {
-      const int c = wcount[w];
-      off += w < warp ? c : 0;
-      tot += c;
+    x += ax;
+    y += ay;
+    if (x >= nx) {
+      x -= nx;
+      y++;
     }
-    if (cls == 1) list[off + __popc(bal & ((1u << lane) - 1u))] = v;
-    base = tot;
-    __syncthreads();
+    while (y >= ny) {
+      y -= ny;
+      z++;
+    }
   }
-  for (int i = (int)threadIdx.x; i < base; i += BLK) pq += matvec_node<T>(G, p, q, list[i]);
+  return pq;
+}
+// q = A p on the surface nodes surf[i0 .. i0 + kSfPer * BLK)
+template <typename T, int BLK>
+__device__ __forceinline__ double mv_surf_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int i0)
+{
+  const int i1 = min(i0 + kSfPer * BLK, G.nsurf);
+  double pq = 0.0;
+#pragma unroll 1
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += BLK) pq += matvec_node<T>(G, p, q, __ldg(G.surf + i));
   return pq;
 }
 
@@ -295,14 +305,21 @@ __device__ __forceinline__ void block_sum_to(double t, double* out)
   }
 }
 
-// q = A p on every node, with the FP64 partial sums of p.q per block
-// (dot[blockIdx]).  T = storage / arithmetic type of p and q.
-// (one CTA per tile of kMvPer * BLK nodes)
+// q = A p: k_lsm_matvec over the bulk tiles, then k_lsm_matvec_surf over
+// the surface tiles, each with the FP64 partial sums of p.q per CTA in
+// dot[blockIdx].  T = storage / arithmetic type of p and q.
 template <typename T, int BLK>
 __global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __restrict__ p, T* __restrict__ q,
                                                     double* __restrict__ dot)
 {
-  const double pq = mv_tile<T, BLK>(G, p, q, blockIdx.x * kMvPer * BLK);
+  const double pq = mv_bulk_tile<T, BLK>(G, p, q, blockIdx.x * kMvPer * BLK);
+  block_sum_to<BLK>(pq, dot + blockIdx.x);
+}
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_lsm_matvec_surf(const LsmGeom G, const T* __restrict__ p,
+                                                         T* __restrict__ q, double* __restrict__ dot)
+{
+  const double pq = mv_surf_tile<T, BLK>(G, p, q, blockIdx.x * kSfPer * BLK);
   block_sum_to<BLK>(pq, dot + blockIdx.x);
 }
 
@@ -503,13 +520,15 @@ __global__ void __launch_bounds__(BLK) k_sq_norm_t(int n3, const T* __restrict__
   }
 }
 
-// Sum over all nblk CTAs of a launch of one FP64 value per thread: each CTA
+// Sum over all ncta CTAs of a launch of one FP64 value per thread: each CTA
 // stores its partial in part[slot] and counts itself in *ctr; the CTA that
-// counts last adds the partials in index order (the same order every
-// time), resets *ctr for the next launch and returns true in its thread 0
-// with the sum in *total.  No CTA waits for another.
+// counts last adds the partials part[0 .. nblk) in index order (the same
+// order every time; slots below those of this launch hold partials of an
+// earlier launch), resets *ctr for the next launch and returns true in its
+// thread 0 with the sum in *total.  No CTA waits for another.
 template <int BLK>
-__device__ __forceinline__ bool grid_sum_last(double t, double* part, int slot, unsigned* ctr, int nblk, double* total)
+__device__ __forceinline__ bool grid_sum_last(double t, double* part, int slot, unsigned* ctr, int ncta, int nblk,
+                                              double* total)
 {
   __shared__ double red[BLK / 32];
   __shared__ int last;
@@ -521,7 +540,7 @@ __device__ __forceinline__ bool grid_sum_last(double t, double* part, int slot, 
     for (int w = 0; w < BLK / 32; w++) s += red[w];
     part[slot] = s;
     __threadfence();
-    last = atomicAdd(ctr, 1u) == (unsigned)(nblk - 1);
+    last = atomicAdd(ctr, 1u) == (unsigned)(ncta - 1);
   }
   __syncthreads();
   if (!last) return false;
@@ -569,57 +588,86 @@ __device__ __forceinline__ void cg_beta_fin(double* scal, double rn)
   scal[0] = rn;
 }
 
-// One CG iteration is three launches: k_cg_mv (q = A p, p.q over the grid,
-// its last CTA sets alpha or the stop flag), k_cg_xr (x and r along p, |r|^2
-// over the grid, its last CTA sets beta) and k_cg_p (p = r + beta p).  A
-// converged system (scal[6] set) returns at once, so replayed iterations
+// One CG iteration is four launches: k_cg_mv and k_cg_mv_surf (q = A p on
+// the bulk and the surface nodes, p.q over both grids, the surface
+// kernel's last CTA sets alpha or the stop flag), k_cg_xr (x and r along p,
+// |r|^2 over the grid, its last CTA sets beta) and k_cg_p (p = r + beta p).
+// A converged system (scal[6] set) returns at once, so replayed iterations
 // past convergence change nothing.  (Forming p on the fly inside the matvec
-// would save the third launch but repeats the update for every neighbour
+// would save the last launch but repeats the update for every neighbour
 // read; the matvec is arithmetic-bound, so that is slower.)
-// Each CTA covers one tile of kMvTile nodes / kVecTile elements (threads
-// striding by BLK): few CTAs, so few partials and counter updates per
-// reduction.  The batched kernels use the same tiles, so a network sums in
-// the same order either way.
+// Each CTA covers one tile of kMvPer / kSfPer nodes or kVecPer elements per
+// thread (threads striding by BLK): few CTAs, so few partials and counter
+// updates per reduction.  The batched kernels use the same tiles, so a
+// network sums in the same order either way.
 constexpr int kVecPer = 8;  // elements per thread (node tiles: kMvPer)
 
-template <typename T, int BLK>
-__device__ __forceinline__ double cg_mv_tile(const LsmGeom& G, const T* __restrict__ p, T* __restrict__ q, int v0)
-{
-  return mv_tile<T, BLK>(G, p, q, v0);
-}
 template <typename T, int BLK>
 __device__ __forceinline__ double cg_xr_tile(int n3, T al, T* __restrict__ x, T* __restrict__ r,
                                              const T* __restrict__ p, const T* __restrict__ q, int i0)
 {
-  // the thread's kVecPer squares summed in T (FP32: one conversion to FP64
-  // per thread), the sums across threads in FP64
+  // every load of the thread's kVecPer elements before the first store (the
+  // batched kernels' vectors come from a table, with no restrict for the
+  // compiler to reorder by); the thread's squares summed in T (FP32: one
+  // conversion to FP64 per thread), the sums across threads in FP64
+  const int i = i0 + (int)threadIdx.x;
+  T xv[kVecPer], rv[kVecPer], pv[kVecPer], qv[kVecPer];
+#pragma unroll
+  for (int k = 0; k < kVecPer; k++)
+    if (i + k * BLK < n3) {
+      xv[k] = x[i + k * BLK];
+      rv[k] = r[i + k * BLK];
+      pv[k] = __ldg(p + i + k * BLK);
+      qv[k] = __ldg(q + i + k * BLK);
+    }
   T rr = T(0);
-  const int i1 = min(i0 + kVecPer * BLK, n3);
-  for (int i = i0 + (int)threadIdx.x; i < i1; i += BLK) {
-    const T xi = x[i] + al * p[i];
-    const T ri = r[i] - al * q[i];
-    x[i] = xi;
-    r[i] = ri;
-    rr += ri * ri;
-  }
+#pragma unroll
+  for (int k = 0; k < kVecPer; k++)
+    if (i + k * BLK < n3) {
+      const T xi = xv[k] + al * pv[k];
+      const T ri = rv[k] - al * qv[k];
+      x[i + k * BLK] = xi;
+      r[i + k * BLK] = ri;
+      rr += ri * ri;
+    }
   return (double)rr;
 }
 template <typename T, int BLK>
 __device__ __forceinline__ void cg_p_tile(int n3, T beta, const T* __restrict__ r, T* __restrict__ p, int i0)
 {
-  const int i1 = min(i0 + kVecPer * BLK, n3);
-  for (int i = i0 + (int)threadIdx.x; i < i1; i += BLK) p[i] = next_dir(r[i], beta, p[i]);
+  const int i = i0 + (int)threadIdx.x;
+  T rv[kVecPer], pv[kVecPer];
+#pragma unroll
+  for (int k = 0; k < kVecPer; k++)
+    if (i + k * BLK < n3) {
+      rv[k] = __ldg(r + i + k * BLK);
+      pv[k] = p[i + k * BLK];
+    }
+#pragma unroll
+  for (int k = 0; k < kVecPer; k++)
+    if (i + k * BLK < n3) p[i + k * BLK] = next_dir(rv[k], beta, pv[k]);
 }
 
+// q = A p on the bulk tiles (partials of p.q in part[0 .. nt1)), then on
+// the surface tiles (part[nt1 ..]), whose last CTA sums both and sets alpha
 template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_cg_mv(const LsmGeom G, double* __restrict__ scal, const T* __restrict__ p,
-                                               T* __restrict__ q, double* __restrict__ part,
-                                               unsigned* __restrict__ ctr, double tol2)
+__global__ void __launch_bounds__(BLK) k_cg_mv(const LsmGeom G, const double* __restrict__ scal,
+                                               const T* __restrict__ p, T* __restrict__ q, double* __restrict__ part)
 {
   if (scal[6] > 0.0) return;
-  const double pq = cg_mv_tile<T, BLK>(G, p, q, blockIdx.x * kMvPer * BLK);
+  const double pq = mv_bulk_tile<T, BLK>(G, p, q, blockIdx.x * kMvPer * BLK);
+  block_sum_to<BLK>(pq, part + blockIdx.x);
+}
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_cg_mv_surf(const LsmGeom G, double* __restrict__ scal,
+                                                    const T* __restrict__ p, T* __restrict__ q, double* __restrict__ part,
+                                                    int nt1, unsigned* __restrict__ ctr, double tol2)
+{
+  if (scal[6] > 0.0) return;
+  const double pq = mv_surf_tile<T, BLK>(G, p, q, blockIdx.x * kSfPer * BLK);
   double tot;
-  if (grid_sum_last<BLK>(pq, part, blockIdx.x, ctr, gridDim.x, &tot)) cg_alpha_fin(scal, tot, tol2);
+  if (grid_sum_last<BLK>(pq, part, nt1 + blockIdx.x, ctr, gridDim.x, nt1 + gridDim.x, &tot))
+    cg_alpha_fin(scal, tot, tol2);
 }
 
 // x += alpha p; r -= alpha q; |r|^2 over the grid, then beta
@@ -631,7 +679,7 @@ __global__ void __launch_bounds__(BLK) k_cg_xr(int n3, double* __restrict__ scal
   if (scal[6] > 0.0) return;
   const double rr = cg_xr_tile<T, BLK>(n3, (T)scal[2], x, r, p, q, blockIdx.x * kVecPer * BLK);
   double tot;
-  if (grid_sum_last<BLK>(rr, part, blockIdx.x, ctr, gridDim.x, &tot)) cg_beta_fin(scal, tot);
+  if (grid_sum_last<BLK>(rr, part, blockIdx.x, ctr, gridDim.x, gridDim.x, &tot)) cg_beta_fin(scal, tot);
 }
 
 // p = r + beta p
@@ -645,8 +693,10 @@ __global__ void __launch_bounds__(BLK) k_cg_p(int n3, const double* __restrict__
 
 // ---- batched CG: many networks advanced by the same launches ------------
 // The descriptor table (kernel parameter) holds each network's geometry,
-// CG vectors, partial-sum buffer, counter and scalar block; tiles list
-// (network, first element) for the node-wise and the element-wise kernels.
+// CG vectors, partial-sum buffer, counter and scalar block, and the list of
+// networks whose tiles a launch covers with the first tile of each: a CTA
+// finds its (network, first element) by a binary search of that list in
+// the parameter space (no dependent global load before its work starts).
 // Every network runs the single-network iteration above on its own
 // scalars, its last tile finishing its sums; a converged network's tiles
 // return at once.
@@ -657,44 +707,77 @@ struct LsmSys {
   double* part;   // per-tile partial sums
   double* scal;   // CG scalars (layout of cg_alpha_fin / cg_beta_fin)
   unsigned* ctr;  // last-tile counter
-  int n3, nt1, nt3;  // 3 nvox, node tiles (kMvPer BLK nodes), element tiles (kVecPer BLK elements)
+  int n3, nt1, nts, nt3;  // 3 nvox, bulk tiles (kMvPer BLK nodes), surface tiles (kSfPer BLK, at least 1),
+                          // element tiles (kVecPer BLK elements)
 };
 struct LsmTable {
   LsmSys s[kLsmBatchMax];
   int n;
+  int nlive;                    // networks of the launches' tiles, in tile order
+  int live[kLsmBatchMax];
+  int f1[kLsmBatchMax + 1];     // first bulk tile of each listed network (f1[nlive] = grid size)
+  int fs[kLsmBatchMax + 1];     // first surface tile
+  int f3[kLsmBatchMax + 1];     // first element tile
 };
 
-// k_cg_mv over the node tiles of every network (tile = (network, first node))
-template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_cg_mv_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles,
-                                                     double tol2)
+// (network, first node / list entry / element) of this CTA's tile; first[]
+// is one of the table's f1, fs, f3 and per the tile's length
+__device__ __forceinline__ int2 batch_tile(const LsmTable& B, const int* first, int per)
 {
-  const int2 tl = __ldg(tiles + blockIdx.x);
-  const LsmSys& S = B.s[tl.x];
-  if (S.scal[6] > 0.0) return;  // converged network (whole CTA)
-  const double pq = cg_mv_tile<T, BLK>(S.G, static_cast<const T*>(S.p), static_cast<T*>(S.q), tl.y);
-  double tot;
-  if (grid_sum_last<BLK>(pq, S.part, tl.y / (kMvPer * BLK), S.ctr, S.nt1, &tot)) cg_alpha_fin(S.scal, tot, tol2);
+  const int b = (int)blockIdx.x;
+  int lo = 0, hi = B.nlive - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return make_int2(B.live[lo], (b - first[lo]) * per);
 }
 
-// k_cg_xr over the element tiles of every network
+// k_cg_mv over the bulk tiles of the listed networks, then k_cg_mv_surf
+// over their surface tiles
 template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_cg_xr_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles)
+__global__ void __launch_bounds__(BLK) k_cg_mv_batch(const __grid_constant__ LsmTable B)
 {
-  const int2 tl = __ldg(tiles + blockIdx.x);
+  const int2 tl = batch_tile(B, B.f1, kMvPer * BLK);
+  const LsmSys& S = B.s[tl.x];
+  if (S.scal[6] > 0.0) return;  // converged network (whole CTA)
+  const LsmGeom G = S.G;  // fields read once, not at every use through the indexed table
+  const double pq = mv_bulk_tile<T, BLK>(G, static_cast<const T*>(S.p), static_cast<T*>(S.q), tl.y);
+  block_sum_to<BLK>(pq, S.part + tl.y / (kMvPer * BLK));
+}
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_cg_mv_surf_batch(const __grid_constant__ LsmTable B,
+                                                                                  double tol2)
+{
+  const int2 tl = batch_tile(B, B.fs, kSfPer * BLK);
+  const LsmSys& S = B.s[tl.x];
+  if (S.scal[6] > 0.0) return;
+  const LsmGeom G = S.G;
+  const double pq = mv_surf_tile<T, BLK>(G, static_cast<const T*>(S.p), static_cast<T*>(S.q), tl.y);
+  double tot;
+  if (grid_sum_last<BLK>(pq, S.part, S.nt1 + tl.y / (kSfPer * BLK), S.ctr, S.nts, S.nt1 + S.nts, &tot))
+    cg_alpha_fin(S.scal, tot, tol2);
+}
+
+// k_cg_xr over the element tiles of the listed networks
+template <typename T, int BLK>
+__global__ void __launch_bounds__(BLK) k_cg_xr_batch(const __grid_constant__ LsmTable B)
+{
+  const int2 tl = batch_tile(B, B.f3, kVecPer * BLK);
   const LsmSys& S = B.s[tl.x];
   if (S.scal[6] > 0.0) return;
   const double rr = cg_xr_tile<T, BLK>(S.n3, (T)S.scal[2], static_cast<T*>(S.x), static_cast<T*>(S.r),
                                        static_cast<const T*>(S.p), static_cast<const T*>(S.q), tl.y);
   double tot;
-  if (grid_sum_last<BLK>(rr, S.part, tl.y / (kVecPer * BLK), S.ctr, S.nt3, &tot)) cg_beta_fin(S.scal, tot);
+  if (grid_sum_last<BLK>(rr, S.part, tl.y / (kVecPer * BLK), S.ctr, S.nt3, S.nt3, &tot)) cg_beta_fin(S.scal, tot);
 }
 
-// k_cg_p over the element tiles of every network
+// k_cg_p over the element tiles of the listed networks
 template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_cg_p_batch(const __grid_constant__ LsmTable B, const int2* __restrict__ tiles)
+__global__ void __launch_bounds__(BLK) k_cg_p_batch(const __grid_constant__ LsmTable B)
 {
-  const int2 tl = __ldg(tiles + blockIdx.x);
+  const int2 tl = batch_tile(B, B.f3, kVecPer * BLK);
   const LsmSys& S = B.s[tl.x];
   if (S.scal[6] > 0.0) return;
   cg_p_tile<T, BLK>(S.n3, (T)S.scal[3], static_cast<const T*>(S.r), static_cast<T*>(S.p), tl.y);
@@ -712,11 +795,39 @@ __global__ void k_cg_init_batch(const __grid_constant__ LsmTable B)
   scal[7] = 0.0;
 }
 
-// done flags of every network into out[s]
+// done flags of every network into out[s], iteration counts into out[n + s]
 __global__ void k_cg_done_batch(const __grid_constant__ LsmTable B, double* out)
 {
   const int s = threadIdx.x;
-  if (s < B.n) out[s] = B.s[s].scal[6];
+  if (s < B.n) {
+    out[s] = B.s[s].scal[6];
+    out[B.n + s] = B.s[s].scal[7];
+  }
+}
+
+// a list of networks of a table
+struct LsmList {
+  int s[kLsmBatchMax];
+  int n;
+};
+// networks joining the batch with a new inner system whose |r0|^2 is in
+// scal[0]: the CG scalars of its first iteration
+__global__ void k_cg_admit_batch(const __grid_constant__ LsmTable B, const LsmList L)
+{
+  const int i = threadIdx.x;
+  if (i >= L.n) return;
+  double* scal = B.s[L.s[i]].scal;
+  scal[3] = 0.0;
+  scal[5] = scal[0];
+  scal[6] = 0.0;
+  scal[7] = 0.0;
+}
+// networks leaving the batch with their iteration budget spent: their
+// tiles of the captured iterations return at once from now on
+__global__ void k_cg_stop_batch(const __grid_constant__ LsmTable B, const LsmList L)
+{
+  const int i = threadIdx.x;
+  if (i < L.n) B.s[L.s[i]].scal[6] = 1.0;
 }
 
 }  // namespace lsm
