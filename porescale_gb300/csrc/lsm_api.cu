@@ -35,7 +35,12 @@ namespace {
 using lsm::LsmGeom;
 
 constexpr int kBlk = 256;
-constexpr int kBatchStreams = 2;  // concurrent batches of ps_lsm_batch_solve (mixed precision)
+// ps_lsm_batch_solve (mixed precision): host threads and streams running
+// groups at a time, and the FP32 CG vector bytes a group of networks may
+// hold (measured on 48 networks each of 24^3 ... 64^3 and on the 48
+// subvolumes of 48^3 ... 128^3: 8, 16 and 40 MB; 40 MB was best or level)
+constexpr int kBatchThreads = 8;
+constexpr long long kGroupBytes = 40LL << 20;
 
 // A captured batch of CG iterations (CUDA graph) for one vector set
 struct CgGraph {
@@ -657,6 +662,43 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
   return r;
 }
 
+// FP64 iterative refinement around FP32 CG on the network's own stream
+// (after prepare(), |b|^2 = bb): rounds of an inner CG to 1e-4 on r / |r|
+// until the FP64 residual is below rtol, maxit inner iterations are spent
+// or 60 rounds are done; the counts go to out.
+int mixed_ir(Springs* S, double bb, double rtol, long long maxit, ps_lsm_result* out)
+{
+  const int n3 = 3 * S->nvox, nb3 = blocks_for(n3);
+  const double inner_tol = 1e-4;
+  long long budget = maxit, iters = 0, inner = 0;
+  int refinements = 0;
+  for (refinements = 0; refinements < 60; refinements++) {
+    double rn2 = 0.0;
+    if (refinements == 0) {
+      PS_CUDA(cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream));
+      rn2 = bb;
+    } else if (int e = residual(S, &rn2)) {
+      return e;
+    }
+    if (!(bb > 0.0) || rn2 <= rtol * rtol * bb || budget <= 0) break;
+    const double rn = std::sqrt(rn2);
+    k_ir_start<<<nb3, kBlk, 0, S->stream>>>(n3, 1.0 / rn, S->r, S->r32, S->p32, S->x32);
+    PS_CUDA(cudaGetLastError());
+    long long it = 0;
+    double rel2 = 0.0;
+    if (int e = cg<float>(S, S->x32, S->r32, S->p32, S->q32, inner_tol, budget, &it, &rel2)) return e;
+    inner += it;
+    budget -= it;
+    k_ir_update<<<nb3, kBlk, 0, S->stream>>>(n3, rn, S->x32, S->x);
+    PS_CUDA(cudaGetLastError());
+    iters++;
+  }
+  out->iterations = iters;
+  out->inner_iterations = inner;
+  out->refinements = refinements;
+  return PS_OK;
+}
+
 // ---- batched mixed-precision solve -------------------------------------------
 // ps_lsm_solve's FP64 refinement around FP32 CG for every network of the
 // list, the inner CGs advanced together by the batched kernels, with no
@@ -665,8 +707,13 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
 // poll (every 16 iterations), is refined on a worker thread and its own
 // stream (x += |r| x32, the FP64 residual, the next inner system) while the
 // others keep iterating, and joins the batch again at the poll after that.
-// Each network does the arithmetic of ps_lsm_solve's loop in the same order
-// (same tiles, same scalars), so the results equal the individual solves'.
+// The captured iterations cover every network not yet finished, so that a
+// network joining or leaving changes only its scalars (a network outside
+// the batch has its stop flag set and its tiles return at once); the graph
+// is rebuilt over the unfinished networks when they hold under 3/4 of its
+// tiles.  Each network does the arithmetic of ps_lsm_solve's loop in the
+// same order (same tiles, same scalars), so the results equal the
+// individual solves'.
 // bb[s] = |b|^2; the per-network counts go to out[s].  nworkers host
 // threads do the refinement steps.
 int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb, double rtol, long long maxit,
@@ -734,6 +781,7 @@ int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb,
   std::condition_variable cv;
   std::deque<int> todo;
   std::vector<int> ready;
+  std::vector<char> fin((size_t)n, 0);  // no further inner solve
   int pending = n, err = PS_OK;
   bool quit = false;
   std::string msg;
@@ -760,6 +808,7 @@ int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb,
           msg = last_error();
         }
         if (!e && next) ready.push_back(s);
+        if (!e && !next) fin[s] = 1;
         pending--;
       }
       cv.notify_all();
@@ -773,10 +822,10 @@ int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb,
   std::vector<int> run;  // networks in the batch
   const double tol2 = 1e-4 * 1e-4;
   const int batch = 16;
-  // the captured iterations over the networks in `run`
-  auto rebuild = [&]() -> int {
-    set_live(tab, run);
-    if (run.empty()) {
+  // the captured iterations over the networks in `cover`
+  auto rebuild = [&](const std::vector<int>& cover) -> int {
+    set_live(tab, cover);
+    if (cover.empty()) {
       if (exec) cudaGraphExecDestroy(exec);
       exec = nullptr;
       return PS_OK;
@@ -813,16 +862,24 @@ int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb,
   auto drive = [&]() -> int {
     PS_CUDA(cudaMalloc((void**)&ddone, sizeof(double) * 2 * n));
     std::vector<double> now((size_t)2 * n, 0.0);
+    {  // every network starts outside the batch
+      lsm::LsmList all{};
+      all.n = n;
+      for (int s = 0; s < n; s++) all.s[s] = s;
+      lsm::k_cg_stop_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, all);
+      PS_CUDA(cudaGetLastError());
+    }
     for (;;) {
-      std::vector<int> admit;
+      std::vector<int> admit, cover;
       {
         std::unique_lock<std::mutex> lk(mu);
         if (run.empty()) cv.wait(lk, [&] { return err || !ready.empty() || pending == 0; });
         if (err) return PS_OK;  // the worker's error is returned below
         admit.swap(ready);
         if (run.empty() && admit.empty() && pending == 0) return PS_OK;
+        for (int s = 0; s < n; s++)
+          if (!fin[s]) cover.push_back(s);
       }
-      bool changed = false;
       if (!admit.empty()) {
         lsm::LsmList L{};
         L.n = (int)admit.size();
@@ -831,13 +888,12 @@ int batch_mixed(const std::vector<Springs*>& sys, const std::vector<double>& bb,
         PS_CUDA(cudaGetLastError());
         run.insert(run.end(), admit.begin(), admit.end());
         std::sort(run.begin(), run.end());
-        changed = true;
       }
       size_t live = 0;
-      for (int s : run) live += (size_t)tab.s[s].nt1;
-      if (changed || 4 * live < 3 * (size_t)tab.f1[tab.nlive])
-        if (int e = rebuild()) return e;
-      if (!exec) continue;
+      for (int s : cover) live += (size_t)tab.s[s].nt1;
+      if (!exec || 4 * live < 3 * (size_t)tab.f1[tab.nlive])
+        if (int e = rebuild(cover)) return e;
+      if (!exec || run.empty()) continue;
       PS_CUDA(cudaGraphLaunch(exec, st));
       lsm::k_cg_done_batch<<<1, lsm::kLsmBatchMax, 0, st>>>(tab, ddone);
       PS_CUDA(cudaMemcpyAsync(now.data(), ddone, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st));
@@ -1116,30 +1172,10 @@ int ps_lsm_solve(void* h, double rtol, int32_t maxit, ps_lsm_result* out)
     if (int e = cg<double>(S, S->x, S->r, S->p64, S->q64, rtol, maxit, &iters, &rel2)) return e;
     inner = iters;
   } else {
-    // FP64 iterative refinement around FP32 CG
-    const double inner_tol = 1e-4;
-    long long budget = maxit;
-    for (refinements = 0; refinements < 60; refinements++) {
-      double rn2 = 0.0;
-      if (refinements == 0) {
-        PS_CUDA(cudaMemcpyAsync(S->r, S->b, sizeof(double) * n3, cudaMemcpyDeviceToDevice, S->stream));
-        rn2 = bb;
-      } else if (int e = residual(S, &rn2)) {
-        return e;
-      }
-      if (!(bb > 0.0) || rn2 <= rtol * rtol * bb || budget <= 0) break;
-      const double rn = std::sqrt(rn2);
-      k_ir_start<<<nb3, kBlk, 0, S->stream>>>(n3, 1.0 / rn, S->r, S->r32, S->p32, S->x32);
-      PS_CUDA(cudaGetLastError());
-      long long it = 0;
-      double rel2 = 0.0;
-      if (int e = cg<float>(S, S->x32, S->r32, S->p32, S->q32, inner_tol, budget, &it, &rel2)) return e;
-      inner += it;
-      budget -= it;
-      k_ir_update<<<nb3, kBlk, 0, S->stream>>>(n3, rn, S->x32, S->x);
-      PS_CUDA(cudaGetLastError());
-      iters++;
-    }
+    if (int e = mixed_ir(S, bb, rtol, maxit, out)) return e;
+    iters = out->iterations;
+    inner = out->inner_iterations;
+    refinements = out->refinements;
   }
   out->iterations = iters;
   out->inner_iterations = inner;
@@ -1293,48 +1329,64 @@ int ps_lsm_batch_solve(void* const* handles, int32_t n, double rtol, int32_t max
       out[s].iterations = out[s].inner_iterations = (long long)h8[7];
     }
   } else {
-    // the networks in kBatchStreams groups of about equal node counts, each
-    // group a batch on its own stream and host thread: the groups' matvecs
-    // (arithmetic-bound) overlap the other groups' vector updates
-    // (bandwidth-bound) instead of alternating with them
-    const int ng = std::min(n, kBatchStreams);
-    std::vector<std::vector<int>> grp((size_t)ng);
-    std::vector<long long> load((size_t)ng, 0);
+    // Groups of networks whose FP32 CG vectors (x, r, p, q: 48 bytes per
+    // box voxel) fit kGroupBytes together, so that a batched iteration
+    // finds them in L2 between its launches; up to kBatchThreads groups run
+    // at a time, each on its own host thread and stream.  A network above
+    // the budget is a group of its own and runs the individual solve's
+    // refinement (its launches fill the GPU by themselves); smaller ones
+    // share the batched launches.
     std::vector<int> order(n);
     for (int s = 0; s < n; s++) order[s] = s;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a]->nnode > sys[b]->nnode; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a]->nvox > sys[b]->nvox; });
+    std::vector<std::vector<int>> grp;
+    long long used = 0;
     for (int s : order) {
-      const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-      grp[g].push_back(s);
-      load[g] += sys[s]->nnode;
+      const long long bytes = 48LL * sys[s]->nvox;
+      if (grp.empty() || used + bytes > kGroupBytes) {
+        grp.emplace_back();
+        used = 0;
+      }
+      grp.back().push_back(s);
+      used += bytes;
     }
+    const int ng = (int)grp.size(), nth = std::min(ng, kBatchThreads);
     std::vector<int> grc((size_t)ng, PS_OK);
     std::vector<std::string> gmsg((size_t)ng);
-    std::vector<cudaStream_t> gst((size_t)ng, nullptr);
-    gst[0] = st;
-    for (int g = 1; g < ng; g++) PS_CUDA(cudaStreamCreateWithFlags(&gst[g], cudaStreamNonBlocking));
+    std::atomic<int> next{0};
     int dev = 0;
     cudaGetDevice(&dev);
-    auto run_group = [&](int g) {
+    auto run_groups = [&]() {
       cudaSetDevice(dev);
-      std::sort(grp[g].begin(), grp[g].end());
-      std::vector<Springs*> gs;
-      std::vector<double> gbb;
-      std::vector<ps_lsm_result> gout(grp[g].size());
-      for (int s : grp[g]) {
-        gs.push_back(sys[s]);
-        gbb.push_back(bb[s]);
+      cudaStream_t gs = nullptr;
+      if (cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking) != cudaSuccess) gs = nullptr;
+      for (int g = next++; g < ng; g = next++) {
+        std::sort(grp[g].begin(), grp[g].end());
+        if (grp[g].size() == 1) {
+          const int s = grp[g][0];
+          grc[g] = mixed_ir(sys[s], bb[s], rtol, maxit, out + s);
+        } else if (!gs) {
+          grc[g] = fail(PS_ERR_CUDA, "ps_lsm_batch_solve: no stream for a batch");
+        } else {
+          std::vector<Springs*> gsys;
+          std::vector<double> gbb;
+          std::vector<ps_lsm_result> gout(grp[g].size());
+          for (size_t i = 0; i < grp[g].size(); i++) {
+            gsys.push_back(sys[grp[g][i]]);
+            gbb.push_back(bb[grp[g][i]]);
+            gout[i] = out[grp[g][i]];
+          }
+          grc[g] = batch_mixed(gsys, gbb, rtol, maxit, gout.data(), gs, 1);
+          for (size_t i = 0; i < gout.size(); i++) out[grp[g][i]] = gout[i];
+        }
+        if (grc[g]) gmsg[g] = last_error();
       }
-      for (size_t i = 0; i < gout.size(); i++) gout[i] = out[grp[g][i]];
-      grc[g] = batch_mixed(gs, gbb, rtol, maxit, gout.data(), gst[g], std::max(1, 8 / ng));
-      if (grc[g]) gmsg[g] = last_error();
-      for (size_t i = 0; i < gout.size(); i++) out[grp[g][i]] = gout[i];
+      if (gs) cudaStreamDestroy(gs);
     };
     std::vector<std::thread> gth;
-    for (int g = 1; g < ng; g++) gth.emplace_back(run_group, g);
-    run_group(0);
+    for (int t = 1; t < nth; t++) gth.emplace_back(run_groups);
+    run_groups();
     for (std::thread& t : gth) t.join();
-    for (int g = 1; g < ng; g++) cudaStreamDestroy(gst[g]);
     for (int g = 0; g < ng && rc == PS_OK; g++)
       if (grc[g]) {
         rc = grc[g];
