@@ -560,12 +560,12 @@ void set_live(lsm::LsmTable& tab, const std::vector<int>& live)
 // ---- batched CG over several networks ---------------------------------------
 // CG on A x = r0 (x = 0, p = r0 set by the caller) for every network of the
 // list at once: the iteration of cg<T> with each kernel launched once for
-// all networks (tile lists over their nodes / elements), 16 iterations per
-// captured graph, until every network has converged or maxit is reached.
-// When the networks still running hold under 3/4 of the node tiles the
-// graph was captured with, the tile lists are rebuilt over them (and the
-// graph re-captured), so the slowest networks' last iterations do not
-// launch the finished networks' tiles.
+// all networks (the launch table lists them with their first tiles), 16
+// iterations per captured graph, until every network has converged or
+// maxit is reached.  When the networks still running hold under 3/4 of the
+// bulk tiles the graph was captured with, the graph is captured anew over
+// them, so the slowest networks' last iterations do not launch the
+// finished networks' tiles.
 template <typename T>
 int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cudaStream_t st)
 {
@@ -609,7 +609,7 @@ int batch_cg(const std::vector<Springs*>& sys, double tol, long long maxit, cuda
   const double tol2 = tol * tol;
   const int batch = 16;
   std::vector<double> done((size_t)n, 0.0);
-  // tile lists of the networks not yet converged, and the graph over them
+  // the graph over the networks not yet converged
   auto rebuild = [&]() -> int {
     std::vector<int> live;
     for (int s = 0; s < n; s++)
