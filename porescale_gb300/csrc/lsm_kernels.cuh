@@ -41,9 +41,10 @@ struct LsmGeom {
 };
 
 // the bulk stencil's properties that bulk_node relies on: the block of
-// offset d equals that of -d, and every row sums to zero (a rigid
-// translation feels no force), so that row r of K p is
-// sum over the 13 pairs of S_d (p_{v+d} + p_{v-d} - 2 p_v)
+// offset d equals that of -d, every row sums to zero (a rigid translation
+// feels no force) and the node's own block is diagonal, so that row r of
+// K p is sum over the 13 pairs of S_d (p_{v+d} + p_{v-d} - 2 p_v), or
+// S_own p_v + sum over the pairs of S_d (p_{v+d} + p_{v-d})
 constexpr bool bulk_stencil_ok()
 {
   for (int d = 0; d < 27; d++)
@@ -56,10 +57,11 @@ constexpr bool bulk_stencil_ok()
       b += kBulkKb[d][j];
     }
     if (a != 0.0 || b != 0.0) return false;
+    if (j % 4 != 0 && (kBulkKa[13][j] != 0.0 || kBulkKb[13][j] != 0.0)) return false;  // diagonal own block
   }
   return true;
 }
-static_assert(bulk_stencil_ok(), "bulk stencil must be symmetric in d and have zero row sums");
+static_assert(bulk_stencil_ok(), "bulk stencil: symmetric in d, zero row sums, diagonal own block");
 
 // the generated cube matrices in device-readable form; every read below
 // has indices fixed by full unrolling, so it folds to a literal and the
@@ -202,6 +204,16 @@ __device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restric
   }
   const T u0[3] = {__ldg(p + v), __ldg(p + nv + v), __ldg(p + 2 * nv + v)};
   T acc[3] = {T(0), T(0), T(0)};
+  // FP64 (bound by GB300's FP64 pipe): the pairs' sums p_{v+d} + p_{v-d}
+  // and the node's own diagonal block, whose entries are -2 x the pairs'
+  // diagonal entries (off its diagonal the pairs' entries cancel), one
+  // operation per pair and component fewer; FP32 keeps the differences
+  // from the node, which cancel nothing large
+  constexpr bool kSums = sizeof(T) == 8;
+  if constexpr (kSums) {
+#pragma unroll
+    for (int r = 0; r < 3; r++) acc[r] = (al * T(kBKa[13][4 * r]) + be * T(kBKb[13][4 * r])) * u0[r];
+  }
 #pragma unroll
   for (int d = 0; d < 13; d++) {  // offset d and its mirror 26 - d
     const int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
@@ -215,7 +227,10 @@ __device__ __forceinline__ double bulk_node(const LsmGeom& G, const T* __restric
     T s[3];
 #pragma unroll
     for (int c = 0; c < 3; c++)
-      if (used[c]) s[c] = (__ldg(p + c * nv + vp) + __ldg(p + c * nv + vm)) - T(2) * u0[c];
+      if (used[c]) {
+        s[c] = __ldg(p + c * nv + vp) + __ldg(p + c * nv + vm);
+        if constexpr (!kSums) s[c] -= T(2) * u0[c];
+      }
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
@@ -316,7 +331,7 @@ __global__ void __launch_bounds__(BLK) k_lsm_matvec(const LsmGeom G, const T* __
   block_sum_to<BLK>(pq, dot + blockIdx.x);
 }
 template <typename T, int BLK>
-__global__ void __launch_bounds__(BLK) k_lsm_matvec_surf(const LsmGeom G, const T* __restrict__ p,
+__global__ void __launch_bounds__(BLK, sizeof(T) == 4 ? 4 : 2) k_lsm_matvec_surf(const LsmGeom G, const T* __restrict__ p,
                                                          T* __restrict__ q, double* __restrict__ dot)
 {
   const double pq = mv_surf_tile<T, BLK>(G, p, q, blockIdx.x * kSfPer * BLK);
