@@ -131,3 +131,26 @@ def test_batch_solve_matches_individual(gpu, prec):
     finally:
         for N in nets:
             N.close()
+
+
+def test_batch_solve_with_a_network_above_the_group_budget(gpu):
+    """ps_lsm_batch_solve (mixed precision) groups networks by CG working
+    set: a 100^3 network (48 MB of FP32 CG vectors, above the 40 MB group
+    budget) runs the individual refinement in a group of its own, the small
+    ones share batched launches; every network's modulus and inner
+    iteration count equal its individual solve's exactly."""
+    from porescale_gb300.springs import batch_solve
+    inds = [geo.inclusions(100, 0.25, 5.0, 11), geo.inclusions(12, 0.25, 2.5, 12), geo.inclusions(14, 0.2, 3.0, 13),
+            geo.inclusions((10, 12, 16), 0.3, 2.0, 14)]
+    nets = [SpringNetwork(ind, A1, B1, A2, B2, 0.002 * ind.shape[2], LOAD_XSTRETCH, LSM_MIXED) for ind in inds]
+    try:
+        got = batch_solve(nets, 1e-10, 200000)
+        for N, r in zip(nets, got):
+            alone = N.solve(1e-10, 200000)
+            assert r.converged == 1
+            assert r.modulus == alone.modulus
+            assert r.inner_iterations == alone.inner_iterations
+            assert r.refinements == alone.refinements
+    finally:
+        for N in nets:
+            N.close()
