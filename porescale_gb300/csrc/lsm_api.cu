@@ -63,7 +63,6 @@ struct Springs {
   double* d_Kab = nullptr;                      // material-independent Ka, Kb (modulus gradients)
   double* fext = nullptr;                       // external nodal load [3][nvox] (fluid wall load)
   bool has_load = false;
-  float* d_K32 = nullptr;
   // FP64 vectors (3*nvox each)
   double *b = nullptr, *x = nullptr, *r = nullptr, *p64 = nullptr, *q64 = nullptr;
   // FP32 inner vectors
@@ -81,7 +80,7 @@ struct Springs {
 
   LsmGeom geom() const
   {
-    return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_K32, d_S64, {(float)p.alf1, (float)p.alf2},
+    return LsmGeom{nx, ny, nz, nvox, d_mat, d_node, d_K64, d_S64, {(float)p.alf1, (float)p.alf2},
                    {(float)p.bet1, (float)p.bet2}, {p.alf1, p.alf2}, {p.bet1, p.bet2}, d_surf, nsurf};
   }
 };
@@ -93,7 +92,6 @@ void free_springs(Springs* S)
   cudaFree(S->d_node);
   cudaFree(S->d_surf);
   cudaFree(S->d_K64);
-  cudaFree(S->d_K32);
   cudaFree(S->d_S64);
   cudaFree(S->d_Kab);
   cudaFree(S->fext);
@@ -1076,7 +1074,6 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
     return m;
   }();
   std::vector<double> K64(2 * 24 * 24), S64(2 * 9 * 24), Kab(2 * 24 * 24);
-  std::vector<float> K32(2 * 24 * 24);
   for (int i = 0; i < 24; i++)
     for (int j = 0; j < 24; j++) {
       Kab[i * 24 + j] = M.Ka[i][j];
@@ -1085,10 +1082,7 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   const double al[2] = {p->alf1, p->alf2}, be[2] = {p->bet1, p->bet2};
   for (int m = 0; m < 2; m++) {
     for (int i = 0; i < 24; i++)
-      for (int j = 0; j < 24; j++) {
-        K64[(m * 24 + i) * 24 + j] = al[m] * M.Ka[i][j] + be[m] * M.Kb[i][j];
-        K32[(m * 24 + i) * 24 + j] = (float)K64[(m * 24 + i) * 24 + j];
-      }
+      for (int j = 0; j < 24; j++) K64[(m * 24 + i) * 24 + j] = al[m] * M.Ka[i][j] + be[m] * M.Kb[i][j];
     for (int i = 0; i < 9; i++)
       for (int j = 0; j < 24; j++) S64[(m * 9 + i) * 24 + j] = al[m] * M.Sa[i][j] + be[m] * M.Sb[i][j];
   }
@@ -1113,11 +1107,9 @@ int ps_lsm_create(const ps_lsm_params* p, const int32_t* ind, int32_t nx, int32_
   if (int r = dalloc(S.get(), &S->scal, sizeof(double) * 32)) return r;
   PS_CUDA(cudaMemsetAsync(S->scal, 0, sizeof(double) * 32, S->stream));
   if (int r = dalloc(S.get(), &S->d_K64, sizeof(double) * K64.size())) return r;
-  if (int r = dalloc(S.get(), &S->d_K32, sizeof(float) * K32.size())) return r;
   if (int r = dalloc(S.get(), &S->d_S64, sizeof(double) * S64.size())) return r;
   if (int r = dalloc(S.get(), &S->d_Kab, sizeof(double) * Kab.size())) return r;
   PS_CUDA(cudaMemcpyAsync(S->d_K64, K64.data(), sizeof(double) * K64.size(), cudaMemcpyHostToDevice, S->stream));
-  PS_CUDA(cudaMemcpyAsync(S->d_K32, K32.data(), sizeof(float) * K32.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_S64, S64.data(), sizeof(double) * S64.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemcpyAsync(S->d_Kab, Kab.data(), sizeof(double) * Kab.size(), cudaMemcpyHostToDevice, S->stream));
   PS_CUDA(cudaMemsetAsync(S->x, 0, b64, S->stream));  // the dynamic state starts at zero displacement

@@ -31,8 +31,7 @@ struct LsmGeom {
   int nx, ny, nz, nvox;
   const uint8_t* mat;   // cube material per voxel (0 pore)
   const uint8_t* node;  // 1 where the node exists
-  const double* K64;    // per-material cube stiffness [2][24][24]
-  const float* K32;
+  const double* K64;    // per-material cube stiffness [2][24][24] (FP64 matvec)
   const double* S64;    // per-material cube stress rows [2][9][24]
   float alf[2], bet[2];  // spring constants of the two materials (FP32 matvec)
   double alfd[2], betd[2];  // the same in FP64 (FP64 bulk stencil)
@@ -98,17 +97,10 @@ __device__ const double kBKb[27][9] = PS_TAB(kBulkKb);
 #undef PS_TAB
 #undef PS_ROW
 
-template <typename T>
-__device__ __forceinline__ T kval(const LsmGeom& G, int m, int r, int c);
-template <>
-__device__ __forceinline__ double kval<double>(const LsmGeom& G, int m, int r, int c)
+// entry (r, c) of the handle's FP64 cube stiffness of material index m
+__device__ __forceinline__ double kval(const LsmGeom& G, int m, int r, int c)
 {
   return __ldg(G.K64 + (m * 24 + r) * 24 + c);
-}
-template <>
-__device__ __forceinline__ float kval<float>(const LsmGeom& G, int m, int r, int c)
-{
-  return __ldg(G.K32 + (m * 24 + r) * 24 + c);
 }
 
 __device__ __forceinline__ int wrap_add(int c, int d, int n) { return c + d < 0 ? c + d + n : (c + d >= n ? c + d - n : c + d); }
@@ -170,7 +162,7 @@ __device__ __forceinline__ double matvec_node(const LsmGeom& G, const T* __restr
 #pragma unroll
               for (int c = 0; c < 3; c++)
                 if (kKa[3 * e + r][3 * b + c] != 0.0 || kKb[3 * e + r][3 * b + c] != 0.0)
-                  acc[r] += kval<T>(G, m - 1, 3 * e + r, 3 * b + c) * u[c];
+                  acc[r] += kval(G, m - 1, 3 * e + r, 3 * b + c) * u[c];
           }
         }
       }
@@ -360,7 +352,7 @@ __global__ void k_lsm_rhs(const LsmGeom G, int pa, int jc, double jump, double* 
       // corners b with bit pa set sit across the tie
       for (int b = 0; b < 8; b++) {
         if (!((b >> pa) & 1)) continue;
-        for (int r = 0; r < 3; r++) acc[r] -= kval<double>(G, m - 1, 3 * e + r, 3 * b + jc) * jump;
+        for (int r = 0; r < 3; r++) acc[r] -= kval(G, m - 1, 3 * e + r, 3 * b + jc) * jump;
       }
     }
   }
