@@ -724,7 +724,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--prec", default="f16", choices=list(PREC_ID))
+    ap.add_argument("--prec", default=None, choices=list(PREC_ID),
+                    help="population storage (default f16; f32 for --batch, whose transient subvolume flows FP16's "
+                         "rounding noise moves by several percent)")
     ap.add_argument("--itw", type=int, default=100, help="steps per e2e step (check_state cadence)")
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -764,6 +766,8 @@ def main():
     ap.add_argument("--lsm-dr-max", type=int, default=1000000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.prec is None:
+        args.prec = "f32" if args.batch else "f16"
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
