@@ -15,7 +15,8 @@ of the 256^3 workload), which settles to a steady counter-current layered
 flow with flat interfaces.  In a steady flow every population takes the
 same value step after step, so a rounding that is not zero-mean biases the
 flux: this is the case the stochastic rounding of the 16-bit stores is for.
-Bounds: the benchmark spec's 1e-3 for FP16 storage, 2e-4 for FP32."""
+Bounds: 1e-3 (the headline metric's error bound) for FP16 storage, 2e-4
+for FP32."""
 import numpy as np
 import pytest
 

@@ -4,7 +4,7 @@ The oracle restates the reference's bond/angle tables and calc_stress and
 solves the same network by FP64 CG (and by the reference's damped Verlet
 relaxation on small boxes).  Tolerances: FP64 GPU moduli within 1e-9
 relative of the oracle; mixed precision (FP32 CG in FP64 refinement) within
-1e-6 relative, the benchmark spec's bound for moduli.
+1e-6 relative, the stated bound for moduli.
 """
 import numpy as np
 import pytest
