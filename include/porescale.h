@@ -260,12 +260,16 @@ int ps_lsm_get_info(void *handle, ps_lsm_info *out);
  * tolerance is not reached within maxit working-precision iterations. */
 int ps_lsm_solve(void *handle, double rtol, int32_t maxit, ps_lsm_result *out);
 /* Several networks solved together (extension): every CG kernel runs once
- * per iteration for all of them (tile lists over their nodes, per-network
- * scalars, a converged network stops moving), 16 iterations per captured
- * CUDA graph.  Same precision for all (PS_LSM_F64: one batched FP64 CG;
- * PS_LSM_MIXED: FP64 refinement rounds around a batched FP32 CG).  out[n]
- * as ps_lsm_solve's; PS_ERR_NOTCONV names the first network above rtol.
- * At most 64 networks. */
+ * per iteration for all of them (per-network scalars, a converged network
+ * stops moving), 16 iterations per captured CUDA graph.  Same precision for
+ * all.  PS_LSM_F64: one batched FP64 CG.  PS_LSM_MIXED: the networks in
+ * groups by working set, up to eight groups at a time on their own host
+ * threads and streams; in a group, FP64 refinement around a batched FP32 CG,
+ * each network refined as soon as its inner CG converges (a network too
+ * large for a group runs ps_lsm_solve's refinement alone).  The results
+ * equal ps_lsm_solve's bit for bit.  out[n] as ps_lsm_solve's;
+ * PS_ERR_NOTCONV names the first network above rtol.  At most 64 networks;
+ * the calling thread must not use the handles meanwhile. */
 int ps_lsm_batch_solve(void *const *handles, int32_t n, double rtol, int32_t maxit, ps_lsm_result *out);
 /* Displacements (3, ns) in the reference node order (k-j-i over the padded
  * grid, duplicate plane included, as LSM_displ_field) after a solve. */
